@@ -1,0 +1,198 @@
+/* pike.h -- C ABI of libpike.so, the GB300 (sm_103a) implementation of Pike's
+ * wavefront path tracer.
+ *
+ * The reference drives its passes from JavaScript through WebGPU: pass objects
+ * with a `static async create(device, ...)` factory and a
+ * `generateCommands(commandEncoder)` method (render/passes/*.js), sequenced by
+ * PikeRenderer.tick() (render/pike.js:120-162).  Each entry point below names
+ * the reference interface it replaces.  A JavaScript host binds them through
+ * N-API; the Python package pike_gb300 binds them through
+ * ctypes.
+ *
+ * Conventions
+ *  - Every function returns a status: PK_OK (0) or an error code; the message
+ *    of the last failure on a context is returned by pk_last_error().
+ *  - The library owns all device memory.  Host input pointers are read before
+ *    the call returns; output pointers must hold the documented element counts.
+ *  - A context is single-threaded and enqueues on one CUDA stream.  Pass entry
+ *    points enqueue work and return; pk_sync() waits and reports device-side
+ *    error flags (queue/stack overflow, bounded-wait timeouts) as PK_ERR_DEVICE.
+ *  - Results are bit-identical to the CPU oracle's restatement of the reference
+ *    (IEEE binary32, no FMA contraction, built-ins defined in pk_math.cuh).
+ */
+#ifndef PIKE_H_
+#define PIKE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PK_OK 0
+#define PK_ERR_ARG 1      /* invalid argument or size */
+#define PK_ERR_CUDA 2     /* CUDA runtime error (message in pk_last_error) */
+#define PK_ERR_STATE 3    /* call out of order (e.g. trace before a scene) */
+#define PK_ERR_DEVICE 4   /* a kernel raised an error flag (see pk_read_counters) */
+#define PK_ERR_UNSUPPORTED 5
+
+/* Device-side error bits, reported in pk_read_counters()[5]. */
+#define PK_DEVERR_STACK 1u
+#define PK_DEVERR_LOOKBACK 2u
+#define PK_DEVERR_QUEUE 4u
+#define PK_DEVERR_PIXEL 8u
+#define PK_DEVERR_BVH 16u
+
+typedef struct pk_ctx pk_ctx;
+
+/* CameraPass.setCameraState({pos, dir, fov, focalDepth, apertureSize,
+ * distortion, bokeh, invocationOffset}) (render/passes/camera_pass.js:118-125),
+ * packed as CameraStateStuct (render/util/structs.js:235-249).  fov is the
+ * vertical field of view in radians; positions are in the normalised frame
+ * the passes render in (trace_pass.js:202-211). */
+typedef struct pk_camera_state {
+  float pos[3];
+  float dir[3];
+  float fov;
+  float focal_depth;
+  float aperture_size;
+  float distortion;
+  float bokeh;
+  uint32_t invocation_offset;
+} pk_camera_state;
+
+/* ---- lifetime ----------------------------------------------------------
+ * navigator.gpu.requestAdapter()/requestDevice() (render/pike.js:92-97). */
+int pk_create(pk_ctx** out, int cuda_device);
+int pk_destroy(pk_ctx* ctx);
+const char* pk_last_error(const pk_ctx* ctx);
+/* Library version as 10000*major + 100*minor + patch. */
+int pk_version(void);
+
+/* CameraPass.create(device, resolution, batchSize) together with the
+ * RenderState it owns (render/passes/camera_pass.js:3-19,79-91) and the ray,
+ * hit and miss queues of TracePass (trace_pass.js:40-54).  batch_size is
+ * BATCH_SIZE of pike.js:18 (W*H for one batch per frame). */
+int pk_configure(pk_ctx* ctx, uint32_t width, uint32_t height, uint32_t batch_size);
+
+/* ---- scene (rows S and M) -----------------------------------------------
+ * Scene._createBuffers (render/scene.js:120-181) for vertices whose glTF
+ * node matrix is the identity and whose prop transform is {scale, translate}
+ * without rotations: quantises tangent/bitangent/normal to snorm8x4 and uv to
+ * snorm16x2 on the GPU.  pos3/nrm3: n_verts*3 doubles, tan4: n_verts*4
+ * (w = handedness), uv2: n_verts*2; tri4: n_tris*{i0, i1, i2, matId}. */
+int pk_scene_flatten(pk_ctx* ctx, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
+                     uint32_t n_verts, const int32_t* tri4, uint32_t n_tris, double scale,
+                     const double translate[3]);
+/* Upload already-flattened scene tables (scene.indices / scene.attributes). */
+int pk_scene_upload(pk_ctx* ctx, const int32_t* tri4, uint32_t n_tris, const double* pos3, const uint32_t* attr4,
+                    uint32_t n_verts);
+/* Read back the flattened tables: pos3 (n_verts*3 doubles), attr4 (n_verts*4). */
+int pk_scene_download(pk_ctx* ctx, double* pos3, uint32_t* attr4);
+/* Scene._createSceneMaterial (scene.js:43-70) for untextured glTF materials
+ * plus TexturePacker.addColor dedup and 1x1 layers (texture_packer.js:87-136).
+ * mats9 per material: base r,g,b,a, roughness, metallic, emissive r,g,b. */
+int pk_materials_set(pk_ctx* ctx, const double* mats9, uint32_t n_mats);
+/* Upload a material index table {diffMap, metRoughMap, normMap, emitMap}
+ * (MaterialIndexStruct, structs.js:251-260) and 1x1 rgba8 atlas layers. */
+int pk_materials_upload(pk_ctx* ctx, const int32_t* mat4, uint32_t n_mats, const uint8_t* layers_rgba8,
+                        uint32_t n_layers);
+/* n_layers, then mat4 (n_mats*4) and layers (n_layers*4 bytes); either pointer may be NULL. */
+int pk_materials_download(pk_ctx* ctx, uint32_t* n_mats, uint32_t* n_layers, int32_t* mat4, uint8_t* layers_rgba8);
+
+/* ---- BVH (rows BVH and Q) ----------------------------------------------
+ * new BVH(scene) + TracePass.initBVHBuffer (render/bvh.js:12-74,
+ * render/passes/trace_pass.js:202-263) on the GPU.
+ * mode PK_BVH_SWEEP: the reference's full-sweep object SAH (same topology,
+ * primitive order and quantised boxes as bvh.js). */
+#define PK_BVH_SWEEP 0
+int pk_bvh_build(pk_ctx* ctx, int mode);
+/* Upload a BVH serialised by the reference: nodes5 = n_nodes * BVHNodeStruct
+ * {childBaseIdx, triangles, xMask, yMask, zMask} (20 B), tri4_leaf = leaf-ordered
+ * VertexIndexStruct, verts4 = normalised VertexPositionStruct (16 B stride). */
+int pk_bvh_upload(pk_ctx* ctx, const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4_leaf,
+                  uint32_t n_leaf_tris, const float* verts4, uint32_t n_verts);
+/* n_nodes, n_leaf_tris, and the normaliser {center x,y,z, scale} (only set by pk_bvh_build). */
+int pk_bvh_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* n_leaf_tris, double norm4[4]);
+int pk_bvh_download(pk_ctx* ctx, int32_t* nodes5, int32_t* tri4_leaf, float* verts4);
+
+/* ---- environment (row E) --------------------------------------------------
+ * new EnvironmentGenerator(img) (render/env_sampler.js:8-29,59-157): luminance
+ * histogram, sorted texel coordinates and pdf texture from an RGBE-in-rgba8
+ * equirect image (w*h*4 bytes, row-major). */
+int pk_env_build(pk_ctx* ctx, const uint8_t* rgbe, uint32_t w, uint32_t h);
+int pk_env_upload(pk_ctx* ctx, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32_t* bins2, uint32_t nb,
+                  const int32_t* coords2, const float* pdf);
+int pk_env_info(pk_ctx* ctx, uint32_t* w, uint32_t* h, uint32_t* nb);
+int pk_env_download(pk_ctx* ctx, int32_t* bins2, int32_t* coords2, float* pdf);
+
+/* ---- render state ----------------------------------------------------
+ * RenderState.generateCommands header upload {samples, envTheta}
+ * (camera_pass.js:53-64); setEnvRotation/resetSamples. */
+int pk_set_render_state(pk_ctx* ctx, int32_t samples, float env_theta);
+int pk_set_camera(pk_ctx* ctx, const pk_camera_state* cam);
+/* PostProcessPass.setExposure / setSaturation (postprocess_pass.js). */
+int pk_set_postprocess(pk_ctx* ctx, float exposure, float saturation);
+/* RenderState.clearColorBuffer / clearNumHitsAndMisses / clearNumRays (camera_pass.js:66-77). */
+int pk_clear_color(pk_ctx* ctx);
+int pk_clear_hits_misses(pk_ctx* ctx);
+int pk_clear_rays(pk_ctx* ctx);
+
+/* ---- passes (one call per generateCommands) ------------------------------ */
+int pk_camera(pk_ctx* ctx);        /* CameraPass.generateCommands      (camera_pass.js:209-220, camera.wgsl) */
+int pk_trace(pk_ctx* ctx);         /* TracePass.generateCommands       (trace_pass.js:265-276, trace.wgsl) */
+int pk_shade_hit(pk_ctx* ctx);     /* ShadeHitPass.generateCommands    (shade_hit_pass.js:169-181, shade_hit.wgsl) */
+int pk_trace_shadow(pk_ctx* ctx);  /* TraceShadowPass.generateCommands (trace_shadow_pass.js, trace_shadow.wgsl) */
+int pk_shade_miss(pk_ctx* ctx);    /* ShadeMissPass.generateCommands   (shade_miss_pass.js, shade_miss.wgsl) */
+int pk_accumulate(pk_ctx* ctx);    /* AccumulatePass.generateCommands  (accumulate_pass.js, accumulate.wgsl) */
+int pk_postprocess(pk_ctx* ctx);   /* PostProcessPass: ACES + saturation + sRGB into a headless buffer */
+
+/* ---- whole frames ------------------------------------------------------
+ * PikeRenderer.tick() (pike.js:120-162) for one batch: clear, camera,
+ * `bounces` x (trace, shade, shadow, miss), accumulate, postprocess, then
+ * samples += 1.  Misses are shaded inside the traversal kernels instead of
+ * through a materialised miss queue; results are identical to the pass path. */
+int pk_render_frame(pk_ctx* ctx, uint32_t bounces);
+int pk_render_frames(pk_ctx* ctx, uint32_t frames, uint32_t bounces);
+
+/* ---- readback ---------------------------------------------------------- */
+int pk_sync(pk_ctx* ctx);
+/* samples, num_hits, num_misses, num_rays, num_shadow, device error bits,
+ * rays traced (low, high 32 bits) since the last pk_reset_stats. */
+int pk_read_counters(pk_ctx* ctx, uint32_t out8[8]);
+/* queue 0: current ray queue, 1: shadow rays, 2: miss queue; 12 floats per ray
+ * in the reference's DeferredRay layout {origin, 0, dir, 0, throughput}. */
+#define PK_QUEUE_RAYS 0
+#define PK_QUEUE_SHADOW 1
+#define PK_QUEUE_MISS 2
+int pk_read_rays(pk_ctx* ctx, int queue, uint32_t first, uint32_t count, float* out12);
+/* Hit entries in the reference layout: {t bits, index, bary_mask, 0, ray[12]} (64 B). */
+int pk_read_hits(pk_ctx* ctx, uint32_t first, uint32_t count, uint32_t* out16);
+/* W*H*4 floats: colour buffer, running mean, tonemapped display; W*H*4 bytes: display8. */
+int pk_read_color(pk_ctx* ctx, float* out);
+int pk_read_accum(pk_ctx* ctx, float* out);
+int pk_write_accum(pk_ctx* ctx, const float* in);
+int pk_read_display(pk_ctx* ctx, float* out, uint8_t* out8);
+
+/* ---- measurement --------------------------------------------------------
+ * counting != 0 selects traversal kernels that also count node fetches and
+ * triangle tests; pk_read_stats: closest {fetch, tests}, shadow {fetch, tests},
+ * rays traced, frames. */
+int pk_set_counting(pk_ctx* ctx, int counting);
+int pk_reset_stats(pk_ctx* ctx);
+int pk_read_stats(pk_ctx* ctx, uint64_t out6[6]);
+/* timing != 0 records CUDA events around every kernel of pk_render_frame on the
+ * context's stream; pk_read_timing returns summed milliseconds and launch
+ * counts per kernel kind: camera, trace, compact, shade, shadow, accumulate,
+ * postprocess, other (16 floats: 8 times then 8 counts). */
+int pk_set_timing(pk_ctx* ctx, int timing);
+int pk_read_timing(pk_ctx* ctx, float out16[16]);
+/* Elementwise evaluation of the library's built-in definitions on the GPU
+ * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */
+int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIKE_H_ */

@@ -1,0 +1,273 @@
+"""ctypes wrapper around liboracle.so, the CPU restatement of Pike's path.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() (as the
+checker) and bench.py's CPU-baseline legs (as the timed CPU restatement).
+The product package never imports this module.
+
+Parity unpinned: the reference has no tests or fixtures and cannot run here;
+see oracle/om_build.h and oracle/om_render.h for the reference lines followed.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    srcs = [os.path.join(_HERE, f) for f in ("pk_oracle.cpp", "om_math.h", "om_build.h", "om_render.h", "Makefile")]
+    if force or not os.path.exists(_LIB) or max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(_LIB):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B", "liboracle.so"], check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(_LIB)
+        _lib.or_last_error.restype = C.c_char_p
+        for name in ("or_bvh_build", "or_env_build", "or_renderer_new"):
+            getattr(_lib, name).restype = C.c_void_p
+        _lib.or_env_num_bins.restype = C.c_size_t
+        _lib.or_shadow_offset.restype = C.c_size_t
+        _lib.or_set_render_state.argtypes = [C.c_void_p, C.c_int32, C.c_float]
+        _lib.or_set_post.argtypes = [C.c_void_p, C.c_float, C.c_float]
+        for name in ("or_bvh_free", "or_env_free", "or_renderer_free", "or_begin_frame", "or_camera", "or_trace",
+                     "or_shade_hit", "or_trace_shadow", "or_shade_miss", "or_accumulate", "or_postprocess",
+                     "or_reset_stats", "or_clear_color", "or_clear_hits_misses", "or_clear_rays"):
+            getattr(_lib, name).argtypes = [C.c_void_p]
+        _lib.or_tick.argtypes = [C.c_void_p, C.c_uint32]
+        _lib.or_set_threads.argtypes = [C.c_void_p, C.c_int]
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _err(what):
+    raise RuntimeError(f"{what}: {lib().or_last_error().decode()}")
+
+
+def flatten(src, scale: float = 1.0, translate=(0.0, 0.0, 0.0)):
+    """Row S (scene.js:456-470): returns (pos f64 (V,3), attrs u32 (V,4))."""
+    L = lib()
+    n = src.pos.shape[0]
+    pos = np.ascontiguousarray(src.pos, np.float64)
+    nrm = np.ascontiguousarray(src.normal, np.float64)
+    tan = np.ascontiguousarray(src.tangent, np.float64)
+    uv = np.ascontiguousarray(src.uv, np.float64)
+    tr = np.asarray(translate, np.float64)
+    pos_out = np.zeros((n, 3), np.float64)
+    attrs = np.zeros((n, 4), np.uint32)
+    L.or_flatten(_p(pos), _p(nrm), _p(tan), _p(uv), C.c_size_t(n), C.c_double(scale), _p(tr), _p(pos_out), _p(attrs))
+    return pos_out, attrs
+
+
+def materials(mats9: np.ndarray):
+    """Row M: returns (index table i32 (M,4), layers u8 (L,4))."""
+    L = lib()
+    m = np.ascontiguousarray(mats9, np.float64)
+    idx = np.zeros((m.shape[0], 4), np.int32)
+    cap = 4 * m.shape[0]
+    layers = np.zeros((cap, 4), np.uint8)
+    nl = C.c_size_t(0)
+    if L.or_materials(_p(m), C.c_size_t(m.shape[0]), _p(idx), _p(layers), C.c_size_t(cap), C.byref(nl)):
+        _err("or_materials")
+    return idx, layers[: nl.value].copy()
+
+
+class BVH:
+    """bvh.js + trace_pass.js packing: nodes (N,5) i32, leaf-ordered tris (T,4) i32, verts (V,4) f32."""
+
+    def __init__(self, pos: np.ndarray, tris: np.ndarray):
+        L = lib()
+        pos = np.ascontiguousarray(pos, np.float64)
+        tris = np.ascontiguousarray(tris, np.int32)
+        h = L.or_bvh_build(_p(pos), C.c_size_t(pos.shape[0]), _p(tris), C.c_size_t(tris.shape[0]))
+        if not h:
+            _err("or_bvh_build")
+        info = np.zeros(4, np.uint64)
+        L.or_bvh_info(C.c_void_p(h), _p(info))
+        self.n_nodes, self.n_leaf_tris, self.max_depth, self.largest_leaf = (int(x) for x in info)
+        self.nodes = np.zeros((self.n_nodes, 5), np.int32)
+        self.tris = np.zeros((self.n_leaf_tris, 4), np.int32)
+        self.verts = np.zeros((pos.shape[0], 4), np.float32)
+        norm = np.zeros(10, np.float64)
+        L.or_bvh_copy(C.c_void_p(h), _p(self.nodes), _p(self.tris), _p(self.verts), _p(norm))
+        L.or_bvh_free(C.c_void_p(h))
+        self.center, self.scale = norm[:3].copy(), float(norm[3])
+        self.root_min, self.root_max = norm[4:7].copy(), norm[7:10].copy()
+
+
+class Env:
+    """env_sampler.js tables: bins (nb,2) i32, coords (N,2) i32, pdf (h,w) f32."""
+
+    def __init__(self, rgbe: np.ndarray):
+        L = lib()
+        rgbe = np.ascontiguousarray(rgbe, np.uint8)
+        h, w = rgbe.shape[:2]
+        hd = L.or_env_build(_p(rgbe), C.c_uint32(w), C.c_uint32(h))
+        if not hd:
+            _err("or_env_build")
+        nb = int(L.or_env_num_bins(C.c_void_p(hd)))
+        self.rgbe = rgbe
+        self.w, self.h = w, h
+        self.bins = np.zeros((nb, 2), np.int32)
+        self.coords = np.zeros((w * h, 2), np.int32)
+        self.pdf = np.zeros((h, w), np.float32)
+        tb = np.zeros(2, np.float64)
+        L.or_env_copy(C.c_void_p(hd), _p(self.bins), _p(self.coords), _p(self.pdf), _p(tb))
+        L.or_env_free(C.c_void_p(hd))
+        self.total, self.brightest = float(tb[0]), float(tb[1])
+
+
+def camera_bytes(state: dict, width: int, height: int) -> bytes:
+    """CameraStateStuct (structs.js:235-249) with dimsMask = W<<16 | H (camera_pass.js:118-125)."""
+    dims = ((width & 0xFFFF) << 16) | (height & 0xFFFF)
+    return struct.pack("<6fI5fI", *state["pos"], *state["dir"], dims, state["fov"], state["focalDepth"],
+                       state["apertureSize"], state["distortion"], state["bokeh"], state["invocationOffset"])
+
+
+class Renderer:
+    """The per-frame passes and RenderState of pike.js, restated on the CPU."""
+
+    def __init__(self, width: int, height: int, batch: int | None = None, threads: int | None = None):
+        L = lib()
+        self.w, self.h = width, height
+        self.batch = batch if batch is not None else width * height
+        self.threads = threads if threads is not None else (os.cpu_count() or 1)
+        self.h_ = L.or_renderer_new(C.c_uint32(width), C.c_uint32(height), C.c_uint32(self.batch), C.c_int(self.threads))
+        self.p = C.c_void_p(self.h_)
+
+    def __del__(self):
+        if getattr(self, "h_", None):
+            lib().or_renderer_free(self.p)
+            self.h_ = None
+
+    def set_scene(self, bvh: BVH, attrs: np.ndarray, mat_index: np.ndarray, layers: np.ndarray):
+        self._keep = [np.ascontiguousarray(bvh.nodes, np.int32), np.ascontiguousarray(bvh.tris, np.int32),
+                      np.ascontiguousarray(bvh.verts, np.float32), np.ascontiguousarray(attrs, np.uint32),
+                      np.ascontiguousarray(mat_index, np.int32), np.ascontiguousarray(layers, np.uint8)]
+        n, t, v, a, m, l = self._keep
+        lib().or_set_scene(self.p, _p(n), C.c_size_t(n.shape[0]), _p(t), C.c_size_t(t.shape[0]), _p(v),
+                           C.c_size_t(v.shape[0]), _p(a), _p(m), C.c_size_t(m.shape[0]), _p(l), C.c_size_t(l.shape[0]))
+
+    def set_env(self, env: Env):
+        lib().or_set_env(self.p, _p(env.rgbe), C.c_uint32(env.w), C.c_uint32(env.h), _p(env.bins),
+                         C.c_size_t(env.bins.shape[0]), _p(env.coords), _p(env.pdf))
+
+    def set_camera(self, state: dict):
+        self._cam = C.create_string_buffer(camera_bytes(state, self.w, self.h))
+        lib().or_set_camera(self.p, self._cam)
+
+    def set_render_state(self, samples: int, env_theta: float = 0.0):
+        lib().or_set_render_state(self.p, samples, env_theta)
+
+    def set_post(self, exposure: float = 1.0, saturation: float = 1.0):
+        lib().or_set_post(self.p, exposure, saturation)
+
+    def __getattr__(self, name):
+        if name in ("begin_frame", "camera", "trace", "shade_hit", "trace_shadow", "shade_miss", "accumulate",
+                    "postprocess", "reset_stats", "clear_color", "clear_hits_misses", "clear_rays"):
+            fn = getattr(lib(), "or_" + name)
+            return lambda: fn(self.p)
+        raise AttributeError(name)
+
+    def tick(self, bounces: int):
+        lib().or_tick(self.p, bounces)
+
+    def counters(self):
+        c = np.zeros(6, np.uint32)
+        lib().or_counters(self.p, _p(c))
+        return dict(samples=int(c[0]), num_hits=int(c[1]), num_misses=int(c[2]), num_rays=int(c[3]),
+                    num_shadow=int(c[4]), overflow=int(c[5]))
+
+    def shadow_offset(self) -> int:
+        return int(lib().or_shadow_offset(self.p))
+
+    def rays(self, first: int, count: int) -> np.ndarray:
+        out = np.zeros((count, 12), np.float32)
+        lib().or_read_rays(self.p, C.c_size_t(first), C.c_size_t(count), _p(out))
+        return out
+
+    def misses(self, count: int) -> np.ndarray:
+        out = np.zeros((count, 12), np.float32)
+        lib().or_read_misses(self.p, C.c_size_t(count), _p(out))
+        return out
+
+    def hits(self, count: int) -> np.ndarray:
+        out = np.zeros((count, 16), np.uint32)
+        lib().or_read_hits(self.p, C.c_size_t(count), _p(out))
+        return out
+
+    def color(self) -> np.ndarray:
+        out = np.zeros((self.h, self.w, 4), np.float32)
+        lib().or_read_color(self.p, _p(out))
+        return out
+
+    def accum(self) -> np.ndarray:
+        out = np.zeros((self.h, self.w, 4), np.float32)
+        lib().or_read_accum(self.p, _p(out))
+        return out
+
+    def display(self):
+        out = np.zeros((self.h, self.w, 4), np.float32)
+        out8 = np.zeros((self.h, self.w, 4), np.uint8)
+        lib().or_read_display(self.p, _p(out), _p(out8))
+        return out, out8
+
+    def stats(self) -> dict:
+        s = np.zeros(8, np.uint64)
+        lib().or_stats(self.p, _p(s))
+        return dict(trace_fetch=int(s[0]), trace_tests=int(s[1]), trace_rays=int(s[2]), trace_max_stack=int(s[3]),
+                    shadow_fetch=int(s[4]), shadow_tests=int(s[5]), shadow_rays=int(s[6]), shadow_max_stack=int(s[7]))
+
+    def trace_rays(self, rays8: np.ndarray, any_hit: bool = False) -> np.ndarray:
+        rays8 = np.ascontiguousarray(rays8, np.float32)
+        out = np.zeros((rays8.shape[0], 4), np.uint32)
+        lib().or_trace_rays(self.p, _p(rays8), C.c_size_t(rays8.shape[0]), C.c_int(1 if any_hit else 0), _p(out))
+        return out
+
+
+MATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan2": 3, "acos": 4, "exp2": 5, "log2": 6, "pow": 7}
+
+
+def math_fn(name: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros_like(x)
+    yp = _p(np.ascontiguousarray(y, np.float32)) if y is not None else None
+    if y is not None:
+        y = np.ascontiguousarray(y, np.float32)
+        yp = _p(y)
+    lib().or_math(C.c_int(MATH_FN[name]), _p(x), yp, _p(out), C.c_size_t(x.size))
+    return out
+
+
+def hash_stream(seed: int, n: int) -> np.ndarray:
+    out = np.zeros(n, np.uint32)
+    lib().or_hash_stream(C.c_uint32(seed), _p(out), C.c_size_t(n))
+    return out
+
+
+class Prepared:
+    """Everything the oracle renderer needs for one synthetic scene."""
+
+    def __init__(self, src, threads: int | None = None, batch: int | None = None):
+        self.src = src
+        self.pos, self.attrs = flatten(src)
+        self.mat_index, self.layers = materials(src.materials)
+        self.bvh = BVH(self.pos, src.tris)
+        self.env = Env(src.env_rgbe)
+        self.r = Renderer(src.width, src.height, batch=batch, threads=threads)
+        self.r.set_scene(self.bvh, self.attrs, self.mat_index, self.layers)
+        self.r.set_env(self.env)
+        self.r.set_camera(src.camera_state())

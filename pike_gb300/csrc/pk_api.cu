@@ -1,0 +1,866 @@
+// pk_api.cu -- the C ABI of libpike.so (declared in include/pike.h): context,
+// device memory, scene/material/BVH/env upload, pass sequencing and readback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "../../include/pike.h"
+#include "pk_bvh.h"
+#include "pk_host_tables.h"
+#include "pk_internal.cuh"
+#include "pk_render.h"
+#include "pk_util.h"
+
+using namespace pk;
+
+namespace {
+
+constexpr uint32_t MAX_BOUNCES = 16;
+constexpr int N_KINDS = 8;
+enum Kind { K_CAMERA = 0, K_TRACE, K_COMPACT, K_SHADE, K_SHADOW, K_ACCUM, K_POST, K_OTHER };
+
+struct EventPair {
+  int kind;
+  cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct pk_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // configuration
+  uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;
+  uint32_t ct = 0, st = 0;  // look-back tiles per compaction / shade launch
+  unsigned g_trace = 1, g_compact = 1, g_shade = 1;  // persistent grid sizes
+  // render state
+  DevBuf<Counters> ctr;
+  DevBuf<CamState> cam;
+  bool cam_set = false;
+  float exposure = 1.0f, saturation = 1.0f;
+  DevBuf<float4> color, accum, display;
+  DevBuf<uchar4> display8;
+  DevBuf<float4> rq[2][3], sq[3], mq[3];
+  int cur = 0;
+  DevBuf<uint4> hrec;
+  DevBuf<uint32_t> hflags, sflags, hit_list;
+  DevBuf<uint32_t> tickets;              // 4 per bounce slot
+  DevBuf<unsigned long long> tiles;      // per bounce slot: ct (compact) + st (shade) + ct (shadow compact)
+  // scene
+  uint32_t n_verts = 0, n_tris = 0;
+  DevBuf<double> pos;
+  DevBuf<uint4> attrs;
+  DevBuf<int4> tri4;
+  uint32_t n_mats = 0, n_layers = 0;
+  DevBuf<int4> mat4;
+  DevBuf<uchar4> layers;
+  // bvh
+  uint32_t n_nodes = 0, n_leaf_tris = 0, n_inner = 0, bvh_verts = 0;
+  double norm[4] = {0, 0, 0, 0};
+  DevBuf<int32_t> nodes5;
+  DevBuf<int4> tri4_leaf;
+  DevBuf<float4> verts4, inner, tris;
+  int root = 0;
+  bool bvh_ready = false;
+  // env
+  uint32_t env_w = 0, env_h = 0, env_nb = 0;
+  DevBuf<uchar4> rgbe;
+  DevBuf<int2> bins, coords;
+  DevBuf<float> pdf;
+  bool env_ready = false;
+  // measurement
+  bool counting = false;
+  bool timing = false;
+  std::vector<EventPair> events;
+  std::vector<cudaEvent_t> event_pool;
+  float kind_ms[N_KINDS] = {0};
+  float kind_n[N_KINDS] = {0};
+  unsigned long long frames = 0;
+
+  RayQ R(int i) { return RayQ{rq[i][0].p, rq[i][1].p, rq[i][2].p}; }
+  RayQ S() { return RayQ{sq[0].p, sq[1].p, sq[2].p}; }
+  RayQ M() { return RayQ{mq[0].p, mq[1].p, mq[2].p}; }
+  uint32_t* ticket(uint32_t slot, int k) { return tickets.p + 4 * slot + k; }
+  unsigned long long* tiles_compact(uint32_t slot) { return tiles.p + (size_t)slot * (2 * ct + st); }
+  unsigned long long* tiles_shade(uint32_t slot) { return tiles_compact(slot) + ct; }
+  unsigned long long* tiles_shadow(uint32_t slot) { return tiles_compact(slot) + ct + st; }
+
+  LaunchCtx launch() {
+    LaunchCtx L;
+    L.stream = stream;
+    L.ctr = ctr.p;
+    L.cam = cam.p;
+    L.scene = SceneDev{inner.p, tris.p, tri4_leaf.p, attrs.p, mat4.p, layers.p, (int)n_layers, root};
+    L.env = EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
+    L.color = color.p;
+    L.accum = accum.p;
+    L.display = display.p;
+    L.display8 = display8.p;
+    L.npix = npix;
+    L.capacity = cap;
+    L.miss_capacity = 2 * cap;
+    L.trace_blocks = g_trace;
+    L.compact_blocks = g_compact;
+    L.shade_blocks = g_shade;
+    return L;
+  }
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    check(cudaEventCreate(&e), "cudaEventCreate");
+    return e;
+  }
+  template <class F>
+  void timed(int kind, F fn) {
+    if (!timing) {
+      fn();
+      return;
+    }
+    EventPair p{kind, take_event(), take_event()};
+    check(cudaEventRecord(p.a, stream), "cudaEventRecord");
+    fn();
+    check(cudaEventRecord(p.b, stream), "cudaEventRecord");
+    events.push_back(p);
+  }
+  void collect_events() {
+    for (EventPair& p : events) {
+      float ms = 0;
+      check(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
+      kind_ms[p.kind] += ms;
+      kind_n[p.kind] += 1;
+      event_pool.push_back(p.a);
+      event_pool.push_back(p.b);
+    }
+    events.clear();
+  }
+};
+
+namespace {
+
+int fail(pk_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+template <class F>
+int guarded(pk_ctx* c, F fn) {
+  if (!c) return PK_ERR_ARG;
+  try {
+    check(cudaSetDevice(c->device), "cudaSetDevice");
+    return fn();
+  } catch (CudaError& e) {
+    return fail(c, PK_ERR_CUDA, e.what());
+  } catch (std::exception& e) {
+    return fail(c, PK_ERR_ARG, e.what());
+  }
+}
+
+template <class T>
+void upload(DevBuf<T>& d, const void* host, size_t count, cudaStream_t s) {
+  d.alloc(count);
+  if (count) check(cudaMemcpyAsync(d.p, host, count * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
+}
+
+void require_config(pk_ctx* c) {
+  if (!c->cap) throw std::runtime_error("pk_configure has not been called");
+}
+void require_render(pk_ctx* c) {
+  require_config(c);
+  if (!c->bvh_ready) throw std::runtime_error("no BVH: call pk_bvh_build or pk_bvh_upload");
+  if (!c->n_mats || !c->n_layers) throw std::runtime_error("no materials: call pk_materials_set/upload");
+  if (!c->attrs.p) throw std::runtime_error("no scene attributes: call pk_scene_flatten/upload");
+  if (!c->cam_set) throw std::runtime_error("no camera: call pk_set_camera");
+}
+
+}  // namespace
+
+extern "C" {
+
+int pk_version(void) { return 10000; }
+
+int pk_create(pk_ctx** out, int device) {
+  if (!out) return PK_ERR_ARG;
+  *out = nullptr;
+  pk_ctx* c = new pk_ctx();
+  c->device = device;
+  int rc = guarded(c, [&]() {
+    int n = 0;
+    check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (device < 0 || device >= n) throw std::runtime_error("no such CUDA device");
+    check(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "attr");
+    check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    c->ctr.alloc(1);
+    c->cam.alloc(1);
+    check(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->stream), "memset");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+  if (rc != PK_OK) {
+    std::fprintf(stderr, "pk_create: %s\n", c->err.c_str());
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return PK_OK;
+}
+
+int pk_destroy(pk_ctx* c) {
+  if (!c) return PK_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PK_OK;
+}
+
+const char* pk_last_error(const pk_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
+  return guarded(c, [&]() {
+    if (!width || !height || width > 0xffff || height > 0xffff) return fail(c, PK_ERR_ARG, "resolution out of range");
+    if ((uint64_t)width * height >= (1ull << 28)) return fail(c, PK_ERR_ARG, "more than 2^28 pixels");
+    if (!batch || batch > (1u << 28)) return fail(c, PK_ERR_ARG, "batch size out of range");
+    c->W = width; c->H = height; c->B = batch;
+    c->cap = (batch + 127u) / 128u * 128u;
+    c->npix = width * height;
+    c->ct = compact_tiles(c->cap);
+    c->st = shade_tiles(c->cap);
+    kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade);
+    for (int i = 0; i < 3; i++) {
+      c->rq[0][i].alloc(c->cap);
+      c->rq[1][i].alloc(c->cap);
+      c->sq[i].alloc(c->cap);
+      c->mq[i].alloc(2 * (size_t)c->cap);
+    }
+    c->hrec.alloc(c->cap);
+    c->hflags.alloc(c->cap / 32 + 1);
+    c->sflags.alloc(c->cap / 32 + 1);
+    c->hit_list.alloc(c->cap);
+    c->color.alloc(c->npix);
+    c->accum.alloc(c->npix);
+    c->display.alloc(c->npix);
+    c->display8.alloc(c->npix);
+    c->tickets.alloc(4 * MAX_BOUNCES);
+    c->tiles.alloc((size_t)MAX_BOUNCES * (2 * c->ct + c->st));
+    check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->accum.p, 0, c->accum.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->display.p, 0, c->display.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->display8.p, 0, c->display8.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->hflags.p, 0, c->hflags.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->sflags.p, 0, c->sflags.bytes(), c->stream), "memset");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->cur = 0;
+    return PK_OK;
+  });
+}
+
+// ---------------- scene ----------------
+int pk_scene_flatten(pk_ctx* c, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
+                     uint32_t n_verts, const int32_t* tri4, uint32_t n_tris, double scale, const double translate[3]) {
+  return guarded(c, [&]() {
+    if (!pos3 || !nrm3 || !tan4 || !uv2 || !tri4 || !n_verts || !n_tris) return fail(c, PK_ERR_ARG, "empty scene");
+    for (uint32_t t = 0; t < n_tris; t++)
+      for (int k = 0; k < 3; k++)
+        if (tri4[4 * t + k] < 0 || (uint32_t)tri4[4 * t + k] >= n_verts) return fail(c, PK_ERR_ARG, "vertex index out of range");
+    DevBuf<double> p, n, t, u;
+    upload(p, pos3, 3 * (size_t)n_verts, c->stream);
+    upload(n, nrm3, 3 * (size_t)n_verts, c->stream);
+    upload(t, tan4, 4 * (size_t)n_verts, c->stream);
+    upload(u, uv2, 2 * (size_t)n_verts, c->stream);
+    c->pos.alloc(3 * (size_t)n_verts);
+    c->attrs.alloc(n_verts);
+    const double tr[3] = {translate ? translate[0] : 0.0, translate ? translate[1] : 0.0, translate ? translate[2] : 0.0};
+    launch_flatten(c->stream, p.p, n.p, t.p, u.p, n_verts, scale, tr[0], tr[1], tr[2], c->pos.p, c->attrs.p);
+    check(cudaGetLastError(), "k_flatten");
+    upload(c->tri4, tri4, n_tris, c->stream);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->n_verts = n_verts;
+    c->n_tris = n_tris;
+    c->bvh_ready = false;
+    return PK_OK;
+  });
+}
+
+int pk_scene_upload(pk_ctx* c, const int32_t* tri4, uint32_t n_tris, const double* pos3, const uint32_t* attr4,
+                    uint32_t n_verts) {
+  return guarded(c, [&]() {
+    if (!tri4 || !pos3 || !attr4 || !n_tris || !n_verts) return fail(c, PK_ERR_ARG, "empty scene");
+    for (uint32_t t = 0; t < n_tris; t++)
+      for (int k = 0; k < 3; k++)
+        if (tri4[4 * t + k] < 0 || (uint32_t)tri4[4 * t + k] >= n_verts) return fail(c, PK_ERR_ARG, "vertex index out of range");
+    upload(c->tri4, tri4, n_tris, c->stream);
+    upload(c->pos, pos3, 3 * (size_t)n_verts, c->stream);
+    upload(c->attrs, attr4, n_verts, c->stream);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->n_verts = n_verts;
+    c->n_tris = n_tris;
+    c->bvh_ready = false;
+    return PK_OK;
+  });
+}
+
+int pk_scene_download(pk_ctx* c, double* pos3, uint32_t* attr4) {
+  return guarded(c, [&]() {
+    if (!c->attrs.p) return fail(c, PK_ERR_STATE, "no scene");
+    if (pos3) check(cudaMemcpyAsync(pos3, c->pos.p, c->pos.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (attr4) check(cudaMemcpyAsync(attr4, c->attrs.p, c->attrs.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+
+int pk_materials_set(pk_ctx* c, const double* mats9, uint32_t n_mats) {
+  return guarded(c, [&]() {
+    if (!mats9 || !n_mats) return fail(c, PK_ERR_ARG, "no materials");
+    std::vector<int32_t> index4;
+    std::vector<uint8_t> layers;
+    build_material_layers(mats9, n_mats, index4, layers);
+    upload(c->mat4, index4.data(), n_mats, c->stream);
+    upload(c->layers, layers.data(), layers.size() / 4, c->stream);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->n_mats = n_mats;
+    c->n_layers = (uint32_t)(layers.size() / 4);
+    return PK_OK;
+  });
+}
+
+int pk_materials_upload(pk_ctx* c, const int32_t* mat4, uint32_t n_mats, const uint8_t* layers, uint32_t n_layers) {
+  return guarded(c, [&]() {
+    if (!mat4 || !layers || !n_mats || !n_layers) return fail(c, PK_ERR_ARG, "no materials");
+    upload(c->mat4, mat4, n_mats, c->stream);
+    upload(c->layers, layers, n_layers, c->stream);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->n_mats = n_mats;
+    c->n_layers = n_layers;
+    return PK_OK;
+  });
+}
+
+int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32_t* mat4, uint8_t* layers) {
+  return guarded(c, [&]() {
+    if (n_mats) *n_mats = c->n_mats;
+    if (n_layers) *n_layers = c->n_layers;
+    if (mat4 && c->n_mats) check(cudaMemcpyAsync(mat4, c->mat4.p, c->mat4.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (layers && c->n_layers) check(cudaMemcpyAsync(layers, c->layers.p, c->layers.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+
+// ---------------- BVH ----------------
+static int finish_bvh(pk_ctx* c) {
+  c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
+  c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
+  DevBuf<int> root(1);
+  DevBuf<uint32_t> err(1);
+  check(cudaMemsetAsync(err.p, 0, 4, c->stream), "memset");
+  if (convert_bvh(c->stream, c->nodes5.p, c->n_nodes, c->tri4_leaf.p, c->n_leaf_tris, c->verts4.p, c->bvh_verts,
+                  c->inner.p, c->tris.p, root.p, err.p))
+    throw CudaError(std::string("convert_bvh: ") + cudaGetErrorString(cudaGetLastError()));
+  uint32_t herr = 0;
+  check(cudaMemcpy(&c->root, root.p, 4, cudaMemcpyDeviceToHost), "D2H");
+  check(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost), "D2H");
+  if (herr) return fail(c, PK_ERR_ARG, "malformed BVH (child index, leaf size >= 128 or vertex index out of range)");
+  c->bvh_ready = true;
+  return PK_OK;
+}
+
+int pk_bvh_upload(pk_ctx* c, const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4_leaf, uint32_t n_leaf_tris,
+                  const float* verts4, uint32_t n_verts) {
+  return guarded(c, [&]() {
+    if (!nodes5 || !n_nodes || !verts4 || !n_verts) return fail(c, PK_ERR_ARG, "empty BVH");
+    upload(c->nodes5, nodes5, 5 * (size_t)n_nodes, c->stream);
+    upload(c->tri4_leaf, tri4_leaf, n_leaf_tris, c->stream);
+    upload(c->verts4, verts4, n_verts, c->stream);
+    c->n_nodes = n_nodes;
+    c->n_leaf_tris = n_leaf_tris;
+    c->bvh_verts = n_verts;
+    for (double& x : c->norm) x = 0;
+    return finish_bvh(c);
+  });
+}
+
+int pk_bvh_build(pk_ctx* c, int mode) {
+  return guarded(c, [&]() {
+    if (mode != PK_BVH_SWEEP) return fail(c, PK_ERR_UNSUPPORTED, "unknown BVH mode");
+    if (!c->pos.p || !c->n_tris) return fail(c, PK_ERR_STATE, "no scene");
+    BvhOut out;
+    std::string why;
+    if (build_bvh_sweep(c->stream, c->pos.p, c->n_verts, c->tri4.p, c->n_tris, out, why))
+      return fail(c, PK_ERR_ARG, "pk_bvh_build: " + why);
+    c->nodes5 = std::move(out.nodes5);
+    c->tri4_leaf = std::move(out.tri4_leaf);
+    c->verts4 = std::move(out.verts4);
+    c->n_nodes = out.n_nodes;
+    c->n_leaf_tris = out.n_leaf_tris;
+    c->bvh_verts = c->n_verts;
+    for (int i = 0; i < 4; i++) c->norm[i] = out.norm[i];
+    return finish_bvh(c);
+  });
+}
+
+int pk_bvh_info(pk_ctx* c, uint32_t* n_nodes, uint32_t* n_leaf_tris, double norm4[4]) {
+  return guarded(c, [&]() {
+    if (!c->bvh_ready) return fail(c, PK_ERR_STATE, "no BVH");
+    if (n_nodes) *n_nodes = c->n_nodes;
+    if (n_leaf_tris) *n_leaf_tris = c->n_leaf_tris;
+    if (norm4) for (int i = 0; i < 4; i++) norm4[i] = c->norm[i];
+    return PK_OK;
+  });
+}
+
+int pk_bvh_download(pk_ctx* c, int32_t* nodes5, int32_t* tri4_leaf, float* verts4) {
+  return guarded(c, [&]() {
+    if (!c->bvh_ready) return fail(c, PK_ERR_STATE, "no BVH");
+    if (nodes5) check(cudaMemcpyAsync(nodes5, c->nodes5.p, c->nodes5.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (tri4_leaf && c->n_leaf_tris)
+      check(cudaMemcpyAsync(tri4_leaf, c->tri4_leaf.p, c->tri4_leaf.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (verts4) check(cudaMemcpyAsync(verts4, c->verts4.p, c->verts4.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+
+// ---------------- env ----------------
+static int env_set(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32_t* bins2, uint32_t nb,
+                   const int32_t* coords2, const float* pdf) {
+  upload(c->rgbe, rgbe, (size_t)w * h, c->stream);
+  upload(c->bins, bins2, nb, c->stream);
+  upload(c->coords, coords2, (size_t)w * h, c->stream);
+  upload(c->pdf, pdf, (size_t)w * h, c->stream);
+  check(cudaStreamSynchronize(c->stream), "sync");
+  c->env_w = w; c->env_h = h; c->env_nb = nb;
+  c->env_ready = true;
+  return PK_OK;
+}
+
+int pk_env_build(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h) {
+  return guarded(c, [&]() {
+    if (!rgbe || !w || !h) return fail(c, PK_ERR_ARG, "empty environment");
+    EnvHostTables t;
+    std::string why;
+    if (build_env_tables(rgbe, w, h, t, why)) return fail(c, PK_ERR_ARG, "pk_env_build: " + why);
+    return env_set(c, rgbe, w, h, t.bins2.data(), (uint32_t)(t.bins2.size() / 2), t.coords2.data(), t.pdf.data());
+  });
+}
+
+int pk_env_upload(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32_t* bins2, uint32_t nb,
+                  const int32_t* coords2, const float* pdf) {
+  return guarded(c, [&]() {
+    if (!rgbe || !bins2 || !coords2 || !pdf || !w || !h || !nb) return fail(c, PK_ERR_ARG, "empty environment");
+    const uint64_t N = (uint64_t)w * h;
+    for (uint32_t b = 0; b < nb; b++)
+      if (bins2[2 * b] < 0 || bins2[2 * b] >= bins2[2 * b + 1] || (uint64_t)bins2[2 * b + 1] > N)
+        return fail(c, PK_ERR_ARG, "malformed luminance bin");
+    for (uint64_t i = 0; i < N; i++)
+      if (coords2[2 * i] < 0 || (uint32_t)coords2[2 * i] >= w || coords2[2 * i + 1] < 0 || (uint32_t)coords2[2 * i + 1] >= h)
+        return fail(c, PK_ERR_ARG, "env coordinate out of range");
+    return env_set(c, rgbe, w, h, bins2, nb, coords2, pdf);
+  });
+}
+
+int pk_env_info(pk_ctx* c, uint32_t* w, uint32_t* h, uint32_t* nb) {
+  return guarded(c, [&]() {
+    if (w) *w = c->env_w;
+    if (h) *h = c->env_h;
+    if (nb) *nb = c->env_nb;
+    return PK_OK;
+  });
+}
+
+int pk_env_download(pk_ctx* c, int32_t* bins2, int32_t* coords2, float* pdf) {
+  return guarded(c, [&]() {
+    if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
+    if (bins2) check(cudaMemcpyAsync(bins2, c->bins.p, c->bins.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (coords2) check(cudaMemcpyAsync(coords2, c->coords.p, c->coords.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (pdf) check(cudaMemcpyAsync(pdf, c->pdf.p, c->pdf.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+
+// ---------------- render state ----------------
+int pk_set_render_state(pk_ctx* c, int32_t samples, float env_theta) {
+  return guarded(c, [&]() {
+    struct { int32_t s; float t; } h{samples, env_theta};
+    check(cudaMemcpyAsync(c->ctr.p, &h, 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+    return PK_OK;
+  });
+}
+
+int pk_set_camera(pk_ctx* c, const pk_camera_state* cam) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!cam) return fail(c, PK_ERR_ARG, "null camera");
+    CamState s;
+    std::memcpy(s.pos, cam->pos, 12);
+    std::memcpy(s.dir, cam->dir, 12);
+    // camera_pass.js:118-125: setUint16(0, H) | setUint16(2, W) -> W << 16 | H
+    s.dims_mask = (c->W << 16) | (c->H & 0xffffu);
+    s.fov = cam->fov;
+    s.focal_depth = cam->focal_depth;
+    s.aperture = cam->aperture_size;
+    s.distortion = cam->distortion;
+    s.bokeh = cam->bokeh;
+    s.invocation_offset = cam->invocation_offset;
+    check(cudaMemcpyAsync(c->cam.p, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream), "H2D");
+    c->cam_set = true;
+    return PK_OK;
+  });
+}
+
+int pk_set_postprocess(pk_ctx* c, float exposure, float saturation) {
+  return guarded(c, [&]() {
+    c->exposure = exposure;
+    c->saturation = saturation;
+    return PK_OK;
+  });
+}
+
+int pk_clear_color(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_config(c);
+    check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
+    return PK_OK;
+  });
+}
+int pk_clear_hits_misses(pk_ctx* c) {
+  return guarded(c, [&]() {
+    check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 8, c->stream), "memset");
+    return PK_OK;
+  });
+}
+int pk_clear_rays(pk_ctx* c) {
+  return guarded(c, [&]() {
+    check(cudaMemsetAsync(&c->ctr.p->num_rays, 0, 8, c->stream), "memset");
+    return PK_OK;
+  });
+}
+
+// ---------------- passes ----------------
+static void reset_slot(pk_ctx* c, uint32_t slot) {
+  check(cudaMemsetAsync(c->ticket(slot, 0), 0, 16, c->stream), "memset");
+  check(cudaMemsetAsync(c->tiles_compact(slot), 0, (size_t)(2 * c->ct + c->st) * 8, c->stream), "memset");
+}
+
+int pk_camera(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!c->cam_set) return fail(c, PK_ERR_STATE, "no camera");
+    LaunchCtx L = c->launch();
+    c->cur = 0;
+    c->timed(K_CAMERA, [&]() { launch_camera(L, c->R(c->cur), c->cap); });
+    check(cudaGetLastError(), "k_camera");
+    return PK_OK;
+  });
+}
+
+int pk_trace(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_render(c);
+    LaunchCtx L = c->launch();
+    reset_slot(c, 0);
+    check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 8, c->stream), "memset");  // clearNumHitsAndMisses
+    c->timed(K_TRACE, [&]() {
+      launch_trace(L, false, false, c->counting, &c->ctr.p->num_rays, c->R(c->cur), c->hrec.p, c->hflags.p,
+                   c->ticket(0, 0));
+    });
+    c->timed(K_COMPACT, [&]() {
+      launch_compact_trace(L, true, c->hflags.p, c->hit_list.p, c->R(c->cur), c->M(), c->ticket(0, 1),
+                           c->tiles_compact(0));
+    });
+    check(cudaGetLastError(), "trace");
+    return PK_OK;
+  });
+}
+
+int pk_shade_hit(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_render(c);
+    LaunchCtx L = c->launch();
+    reset_slot(c, 0);
+    c->timed(K_SHADE, [&]() {
+      launch_shade(L, c->hit_list.p, c->hrec.p, c->R(c->cur), c->R(c->cur ^ 1), c->S(), c->ticket(0, 2),
+                   c->tiles_shade(0));
+    });
+    c->cur ^= 1;
+    check(cudaGetLastError(), "shade");
+    return PK_OK;
+  });
+}
+
+int pk_trace_shadow(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_render(c);
+    LaunchCtx L = c->launch();
+    reset_slot(c, 0);
+    c->timed(K_SHADOW, [&]() {
+      launch_trace(L, true, false, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p, c->ticket(0, 3));
+    });
+    c->timed(K_COMPACT, [&]() { launch_compact_shadow(L, c->sflags.p, c->S(), c->M(), c->ticket(0, 1), c->tiles_shadow(0)); });
+    check(cudaGetLastError(), "trace_shadow");
+    return PK_OK;
+  });
+}
+
+int pk_shade_miss(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
+    LaunchCtx L = c->launch();
+    c->timed(K_OTHER, [&]() { launch_shade_miss(L, c->M()); });
+    check(cudaGetLastError(), "shade_miss");
+    return PK_OK;
+  });
+}
+
+int pk_accumulate(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_config(c);
+    LaunchCtx L = c->launch();
+    c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
+    check(cudaGetLastError(), "accumulate");
+    return PK_OK;
+  });
+}
+
+int pk_postprocess(pk_ctx* c) {
+  return guarded(c, [&]() {
+    require_config(c);
+    LaunchCtx L = c->launch();
+    c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
+    check(cudaGetLastError(), "postprocess");
+    return PK_OK;
+  });
+}
+
+static void render_frame(pk_ctx* c, uint32_t bounces) {
+  LaunchCtx L = c->launch();
+  const uint32_t nb = std::min(bounces, MAX_BOUNCES);
+  // RenderState.generateCommands + tick(): clear colour, hit/miss and ray counts
+  check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 16, c->stream), "memset");
+  check(cudaMemsetAsync(c->tickets.p, 0, c->tickets.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(c->tiles.p, 0, (size_t)std::max(nb, 1u) * (2 * c->ct + c->st) * 8, c->stream), "memset");
+  c->cur = 0;
+  c->timed(K_CAMERA, [&]() { launch_camera(L, c->R(0), c->cap); });
+  for (uint32_t b = 0; b < bounces; b++) {
+    const uint32_t slot = b % MAX_BOUNCES;
+    if (b && slot == 0) {
+      check(cudaMemsetAsync(c->tickets.p, 0, c->tickets.bytes(), c->stream), "memset");
+      check(cudaMemsetAsync(c->tiles.p, 0, c->tiles.bytes(), c->stream), "memset");
+    }
+    c->timed(K_TRACE, [&]() {
+      launch_trace(L, false, true, c->counting, &c->ctr.p->num_rays, c->R(c->cur), c->hrec.p, c->hflags.p,
+                   c->ticket(slot, 0));
+    });
+    c->timed(K_COMPACT, [&]() {
+      launch_compact_trace(L, false, c->hflags.p, c->hit_list.p, c->R(c->cur), c->M(), c->ticket(slot, 1),
+                           c->tiles_compact(slot));
+    });
+    c->timed(K_SHADE, [&]() {
+      launch_shade(L, c->hit_list.p, c->hrec.p, c->R(c->cur), c->R(c->cur ^ 1), c->S(), c->ticket(slot, 2),
+                   c->tiles_shade(slot));
+    });
+    c->cur ^= 1;
+    c->timed(K_SHADOW, [&]() {
+      launch_trace(L, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
+                   c->ticket(slot, 3));
+    });
+  }
+  c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
+  c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
+  c->timed(K_OTHER, [&]() { launch_end_frame(L); });
+  check(cudaGetLastError(), "render_frame");
+  c->frames++;
+}
+
+int pk_render_frame(pk_ctx* c, uint32_t bounces) {
+  return guarded(c, [&]() {
+    require_render(c);
+    if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
+    render_frame(c, bounces);
+    return PK_OK;
+  });
+}
+
+int pk_render_frames(pk_ctx* c, uint32_t frames, uint32_t bounces) {
+  return guarded(c, [&]() {
+    require_render(c);
+    if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
+    for (uint32_t f = 0; f < frames; f++) render_frame(c, bounces);
+    return PK_OK;
+  });
+}
+
+// ---------------- readback ----------------
+int pk_sync(pk_ctx* c) {
+  return guarded(c, [&]() {
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->collect_events();
+    uint32_t err = 0;
+    check(cudaMemcpy(&err, &c->ctr.p->err, 4, cudaMemcpyDeviceToHost), "D2H");
+    if (err) {
+      char buf[96];
+      std::snprintf(buf, sizeof buf, "device error flags 0x%x", err);
+      return fail(c, PK_ERR_DEVICE, buf);
+    }
+    return PK_OK;
+  });
+}
+
+int pk_read_counters(pk_ctx* c, uint32_t out8[8]) {
+  return guarded(c, [&]() {
+    if (!out8) return fail(c, PK_ERR_ARG, "null output");
+    Counters h;
+    check(cudaStreamSynchronize(c->stream), "sync");
+    check(cudaMemcpy(&h, c->ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
+    out8[0] = (uint32_t)h.samples; out8[1] = h.num_hits; out8[2] = h.num_misses; out8[3] = h.num_rays;
+    out8[4] = h.num_shadow; out8[5] = h.err;
+    out8[6] = (uint32_t)(h.rays_traced & 0xffffffffu); out8[7] = (uint32_t)(h.rays_traced >> 32);
+    return PK_OK;
+  });
+}
+
+static void gather_rays(pk_ctx* c, RayQ q, uint32_t first, uint32_t count, float* out12) {
+  std::vector<float4> o(count), d(count), t(count);
+  check(cudaStreamSynchronize(c->stream), "sync");
+  check(cudaMemcpy(o.data(), q.o + first, count * 16, cudaMemcpyDeviceToHost), "D2H");
+  check(cudaMemcpy(d.data(), q.d + first, count * 16, cudaMemcpyDeviceToHost), "D2H");
+  check(cudaMemcpy(t.data(), q.t + first, count * 16, cudaMemcpyDeviceToHost), "D2H");
+  for (uint32_t i = 0; i < count; i++) {
+    float* r = out12 + 12 * (size_t)i;
+    r[0] = o[i].x; r[1] = o[i].y; r[2] = o[i].z; r[3] = 0.0f;
+    r[4] = d[i].x; r[5] = d[i].y; r[6] = d[i].z; r[7] = 0.0f;
+    r[8] = t[i].x; r[9] = t[i].y; r[10] = t[i].z; r[11] = t[i].w;
+  }
+}
+
+int pk_read_rays(pk_ctx* c, int queue, uint32_t first, uint32_t count, float* out12) {
+  return guarded(c, [&]() {
+    require_config(c);
+    const uint64_t limit = queue == PK_QUEUE_MISS ? 2ull * c->cap : c->cap;
+    if (!out12 || (uint64_t)first + count > limit) return fail(c, PK_ERR_ARG, "range outside the queue");
+    if (queue != PK_QUEUE_RAYS && queue != PK_QUEUE_SHADOW && queue != PK_QUEUE_MISS) return fail(c, PK_ERR_ARG, "bad queue");
+    if (count) gather_rays(c, queue == PK_QUEUE_RAYS ? c->R(c->cur) : queue == PK_QUEUE_SHADOW ? c->S() : c->M(), first, count, out12);
+    return PK_OK;
+  });
+}
+
+int pk_read_hits(pk_ctx* c, uint32_t first, uint32_t count, uint32_t* out16) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!out16 || (uint64_t)first + count > c->cap) return fail(c, PK_ERR_ARG, "range outside the hit queue");
+    if (!count) return PK_OK;
+    std::vector<uint32_t> list(count);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    check(cudaMemcpy(list.data(), c->hit_list.p + first, count * 4, cudaMemcpyDeviceToHost), "D2H");
+    uint32_t maxj = 0;
+    for (uint32_t j : list) maxj = std::max(maxj, j);
+    if (maxj >= c->cap) return fail(c, PK_ERR_STATE, "hit list entry out of range");
+    std::vector<uint4> hr(maxj + 1);
+    std::vector<float> rays(12 * (size_t)(maxj + 1));
+    check(cudaMemcpy(hr.data(), c->hrec.p, hr.size() * 16, cudaMemcpyDeviceToHost), "D2H");
+    gather_rays(c, c->R(c->cur), 0, maxj + 1, rays.data());
+    for (uint32_t i = 0; i < count; i++) {
+      const uint32_t j = list[i];
+      uint32_t* o = out16 + 16 * (size_t)i;
+      o[0] = hr[j].x; o[1] = hr[j].y; o[2] = hr[j].z; o[3] = 0;
+      std::memcpy(o + 4, &rays[12 * (size_t)j], 48);
+    }
+    return PK_OK;
+  });
+}
+
+static int read_px(pk_ctx* c, const void* src, void* dst, size_t bytes) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!dst) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    check(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), "D2H");
+    return PK_OK;
+  });
+}
+int pk_read_color(pk_ctx* c, float* out) { return c ? read_px(c, c->color.p, out, c->color.bytes()) : PK_ERR_ARG; }
+int pk_read_accum(pk_ctx* c, float* out) { return c ? read_px(c, c->accum.p, out, c->accum.bytes()) : PK_ERR_ARG; }
+int pk_write_accum(pk_ctx* c, const float* in) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!in) return fail(c, PK_ERR_ARG, "null input");
+    check(cudaMemcpyAsync(c->accum.p, in, c->accum.bytes(), cudaMemcpyHostToDevice, c->stream), "H2D");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+int pk_read_display(pk_ctx* c, float* out, uint8_t* out8) {
+  return guarded(c, [&]() {
+    require_config(c);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    if (out) check(cudaMemcpy(out, c->display.p, c->display.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    if (out8) check(cudaMemcpy(out8, c->display8.p, c->display8.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    return PK_OK;
+  });
+}
+
+// ---------------- measurement ----------------
+int pk_set_counting(pk_ctx* c, int on) { return guarded(c, [&]() { c->counting = on != 0; return PK_OK; }); }
+int pk_reset_stats(pk_ctx* c) {
+  return guarded(c, [&]() {
+    check(cudaMemsetAsync(&c->ctr.p->rays_traced, 0, 8 * 8, c->stream), "memset");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->collect_events();
+    for (int k = 0; k < N_KINDS; k++) { c->kind_ms[k] = 0; c->kind_n[k] = 0; }
+    c->frames = 0;
+    return PK_OK;
+  });
+}
+int pk_read_stats(pk_ctx* c, uint64_t out6[6]) {
+  return guarded(c, [&]() {
+    if (!out6) return fail(c, PK_ERR_ARG, "null output");
+    Counters h;
+    check(cudaStreamSynchronize(c->stream), "sync");
+    check(cudaMemcpy(&h, c->ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
+    out6[0] = h.stat[0]; out6[1] = h.stat[1]; out6[2] = h.stat[2]; out6[3] = h.stat[3];
+    out6[4] = h.rays_traced; out6[5] = c->frames;
+    return PK_OK;
+  });
+}
+int pk_set_timing(pk_ctx* c, int on) { return guarded(c, [&]() { c->timing = on != 0; return PK_OK; }); }
+int pk_read_timing(pk_ctx* c, float out16[16]) {
+  return guarded(c, [&]() {
+    if (!out16) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->collect_events();
+    for (int k = 0; k < N_KINDS; k++) { out16[k] = c->kind_ms[k]; out16[8 + k] = c->kind_n[k]; }
+    return PK_OK;
+  });
+}
+
+int pk_math_eval(pk_ctx* c, int fn, const float* x, const float* y, float* out, uint32_t n) {
+  return guarded(c, [&]() {
+    if (!x || !out) return fail(c, PK_ERR_ARG, "null array");
+    DevBuf<float> dx, dy, dout(n);
+    upload(dx, x, n, c->stream);
+    if (y) upload(dy, y, n, c->stream);
+    launch_math(c->stream, fn, dx.p, y ? dy.p : nullptr, dout.p, n);
+    check(cudaGetLastError(), "k_math");
+    check(cudaMemcpyAsync(out, dout.p, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    return PK_OK;
+  });
+}
+
+}  // extern "C"

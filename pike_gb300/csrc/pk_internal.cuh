@@ -1,0 +1,166 @@
+// pk_internal.cuh -- device data layout and shared device helpers of libpike.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "pk_math.cuh"
+
+namespace pk {
+
+// ---- error bits reported through pk_ctx status --------------------------------
+enum : uint32_t {
+  ERR_STACK = 1u,      // traversal stack overflow (ray result incomplete)
+  ERR_LOOKBACK = 2u,   // decoupled look-back gave up waiting (bounded spin)
+  ERR_QUEUE = 4u,      // a queue write would exceed its capacity
+  ERR_PIXEL = 8u,      // a colour write addressed a pixel outside the image
+  ERR_BVH = 16u,       // BVH build: degenerate node / leaf too large
+};
+
+// Work-counter slots in Counters::work (reset before each launch that uses them).
+enum : int { W_TRACE = 0, W_TILE = 1, W_SHADE = 2, W_AUX = 3 };
+
+// Device-resident RenderState header (camera_pass.js:3-77) plus queue counters.
+struct Counters {
+  int32_t samples;
+  float env_theta;
+  uint32_t num_hits, num_misses, num_rays, num_shadow;
+  uint32_t err;
+  uint32_t pad0;
+  uint32_t work[8];
+  unsigned long long rays_traced;   // closest-hit + shadow rays, all frames since reset
+  unsigned long long trace_launch_rays;
+  unsigned long long stat[6];       // optional traversal counters (fetch, tests) per kind
+};
+
+// CameraStateStuct (structs.js:235-249): eye ray, dimsMask = W<<16|H, lens params.
+struct CamState {
+  float pos[3];
+  float dir[3];
+  uint32_t dims_mask;
+  float fov, focal_depth, aperture, distortion, bokeh;
+  uint32_t invocation_offset;
+};
+
+// One ray queue in SoA form.  Together the three float4 are the reference's
+// 48-byte DeferredRay {origin, dir, throughput}; t.w holds the pixel index bits.
+struct RayQ {
+  float4* o;
+  float4* d;
+  float4* t;
+};
+
+// Traversal-format BVH (built from the reference's 20-byte nodes without
+// changing any box or order): one 64-byte record per inner node holding both
+// children's decoded boxes and child codes.  Child code >= 0: inner record
+// index; child code < 0: leaf, (code & 0x7fffffff) = reference `triangles`
+// word (size << 24 | base).  Triangles are stored leaf-ordered as
+// {v0.xyz, e1.x}, {e1.yz, e2.xy}, {e2.z, -, -, -} with e1 = v1 - v0, e2 = v2 - v0.
+struct SceneDev {
+  const float4* inner;     // 4 float4 per inner record
+  const float4* tris;      // 3 float4 per leaf-ordered triangle
+  const int4* tri4;        // leaf-ordered {i0, i1, i2, matId}
+  const uint4* attrs;      // per-vertex {tangent, bitangent, normal (snorm8x4), uv (snorm16x2)}
+  const int4* mat4;        // per-material atlas layers {diff, metRough, norm, emit}
+  const uchar4* layers;    // 1x1 rgba8 atlas layers
+  int n_layers;
+  int root;                // child code of the root
+};
+
+struct EnvDev {
+  const uchar4* rgbe;      // rgba8 texels, alpha = exponent
+  const int2* bins;        // {h0, h1}
+  const int2* coords;      // {x, y}, descending radiance
+  const float* pdf;        // r32f per texel
+  int w, h, nb;
+  int enabled;             // SAMPLE_ENV_LIGHT
+};
+
+// ---- decoupled look-back over tiles carrying two 31-bit counts ------------
+constexpr unsigned long long TILE_AGG = 1ull << 62;
+constexpr unsigned long long TILE_PRE = 2ull << 62;
+constexpr unsigned long long TILE_VAL = (1ull << 62) - 1;
+constexpr int LOOKBACK_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long pack2(uint32_t a, uint32_t b) {
+  return (unsigned long long)a | ((unsigned long long)b << 31);
+}
+__device__ __forceinline__ uint32_t unpack_a(unsigned long long v) { return (uint32_t)(v & 0x7fffffffull); }
+__device__ __forceinline__ uint32_t unpack_b(unsigned long long v) { return (uint32_t)((v >> 31) & 0x7fffffffull); }
+
+// Exclusive prefix of this tile's two counts over all earlier tiles.  Called by
+// one thread.  Tiles are numbered in the order blocks claim them (an atomic
+// ticket), so every earlier tile belongs to a block that is already running;
+// waits are bounded and report ERR_LOOKBACK instead of hanging.
+__device__ __forceinline__ unsigned long long lookback2(unsigned long long* tiles, uint32_t tile,
+                                                        unsigned long long agg, uint32_t* err) {
+  if (tile == 0) {
+    st_release(&tiles[0], TILE_PRE | agg);
+    return 0ull;
+  }
+  st_release(&tiles[tile], TILE_AGG | agg);
+  unsigned long long excl = 0;
+  int i = (int)tile - 1;
+  while (i >= 0) {
+    unsigned long long v = ld_acquire(&tiles[i]);
+    int spins = 0;
+    while ((v & ~TILE_VAL) == 0) {
+      if (++spins > LOOKBACK_SPIN_LIMIT) {
+        atomicOr(err, ERR_LOOKBACK);
+        v = TILE_PRE;
+        break;
+      }
+      __nanosleep(64);
+      v = ld_acquire(&tiles[i]);
+    }
+    excl += v & TILE_VAL;
+    if ((v & ~TILE_VAL) == TILE_PRE) break;
+    --i;
+  }
+  st_release(&tiles[tile], TILE_PRE | (excl + agg));
+  return excl;
+}
+
+// Block-wide exclusive scan of two per-thread counts (blockDim.x <= 1024,
+// multiple of 32).  Returns this thread's exclusive offsets and the block totals.
+template <int NWARPS>
+__device__ __forceinline__ void block_scan2(uint32_t a, uint32_t b, uint32_t& ea, uint32_t& eb, uint32_t& ta,
+                                            uint32_t& tb, uint32_t (*s_warp)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t ia = a, ib = b;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t xa = __shfl_up_sync(0xffffffffu, ia, o);
+    uint32_t xb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) { ia += xa; ib += xb; }
+  }
+  if (lane == 31) { s_warp[warp][0] = ia; s_warp[warp][1] = ib; }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t wa = lane < NWARPS ? s_warp[lane][0] : 0u;
+    uint32_t wb = lane < NWARPS ? s_warp[lane][1] : 0u;
+    uint32_t sa = wa, sb = wb;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t xa = __shfl_up_sync(0xffffffffu, sa, o);
+      uint32_t xb = __shfl_up_sync(0xffffffffu, sb, o);
+      if (lane >= o) { sa += xa; sb += xb; }
+    }
+    if (lane < NWARPS) { s_warp[lane][0] = sa - wa; s_warp[lane][1] = sb - wb; }
+    if (lane == NWARPS - 1) { s_warp[NWARPS][0] = sa; s_warp[NWARPS][1] = sb; }
+  }
+  __syncthreads();
+  ea = s_warp[warp][0] + ia - a;
+  eb = s_warp[warp][1] + ib - b;
+  ta = s_warp[NWARPS][0];
+  tb = s_warp[NWARPS][1];
+}
+
+}  // namespace pk

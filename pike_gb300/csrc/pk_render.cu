@@ -1,0 +1,760 @@
+// pk_render.cu -- the per-frame passes of Pike's wavefront path tracer on sm_103a.
+//
+// Each kernel follows one WGSL entry point of the reference (cited per kernel)
+// and reproduces its results bit for bit under the arithmetic definition in
+// pk_math.cuh.  Queue slots are assigned by stable (order-preserving)
+// compaction, i.e. in increasing source slot, the order the reference's
+// atomic appends take when invocations run serially.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "pk_internal.cuh"
+#include "pk_render.h"
+
+namespace pk {
+
+constexpr float MAX_T = 100000.0f;
+constexpr float SHADE_EPS = 1e-7f;
+
+// =====================================================================
+// camera.wgsl:75-93 main + createPrimaryRay (:58-73)
+// =====================================================================
+__global__ void __launch_bounds__(128) k_camera(const CamState* __restrict__ camp, Counters* __restrict__ ctr,
+                                                RayQ R, uint32_t n_threads, uint32_t capacity) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n_threads) return;
+  const CamState cam = *camp;
+  const uint32_t W = cam.dims_mask >> 16, H = cam.dims_mask & 0xffffu;
+  const uint32_t idx = gid + cam.invocation_offset;
+  const uint32_t px = idx % W, py = idx / W;
+  if (px >= W || py >= H) return;
+  Hash h;
+  h.seed = (px * 1973u + py * 9277u + (uint32_t)ctr->samples * 26699u) | 1u;
+  h.seed = h.next();
+  const float fx = (float)px, fy = (float)py, rx = (float)W, ry = (float)H;
+  const float k = cam.distortion;
+  const float jx = h.rand();
+  const float jy = h.rand();
+  float ux = (2.0f * ((fx + jx) / rx) - 1.0f) * (rx / ry);
+  float uy = (2.0f * ((fy + jy) / ry) - 1.0f) * -1.0f;
+  const float rd = sqrtf(ux * ux + uy * uy);
+  const float ru = rd * (1.0f + k * rd * rd);
+  const float l = sqrtf(ux * ux + uy * uy);
+  const float nx = ux / l, ny = uy / l;
+  ux = ru * nx;
+  uy = ru * ny;
+  const V3 eo = v3(cam.pos[0], cam.pos[1], cam.pos[2]);
+  const V3 ed = v3(cam.dir[0], cam.dir[1], cam.dir[2]);
+  const float tf = tan_(cam.fov * 0.5f);
+  const V3 bx = scale(normalize(cross(ed, v3(0.0f, 1.0f, 0.0f))), tf);
+  const V3 by = scale(normalize(cross(bx, ed)), tf);
+  const float theta = h.rand() * c::TAU;
+  const float pw = pow_(h.rand(), cam.bokeh);
+  const V3 dof = scale(scale(add(scale(bx, cos_(theta)), scale(by, sin_(theta))), cam.aperture), pw);
+  const V3 screen = add(add(add(scale(bx, ux), scale(by, uy)), ed), eo);
+  const V3 dir = normalize(sub(add(screen, scale(dof, cam.focal_depth)), add(eo, dof)));
+  const V3 org = add(dof, eo);
+  if (gid < capacity) {
+    R.o[gid] = make_float4(org.x, org.y, org.z, 0.0f);
+    R.d[gid] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+    R.t[gid] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(idx));
+  } else {
+    atomicOr(&ctr->err, ERR_QUEUE);
+  }
+  atomicAdd(&ctr->num_rays, 1u);
+}
+
+// =====================================================================
+// shade_miss.wgsl:37-43 envColor: nearest texel with repeat addressing.
+// =====================================================================
+__device__ __forceinline__ V3 env_color(const EnvDev& env, float theta, V3 dir) {
+  const float u = theta + atan2_(dir.z, dir.x) / c::TAU;
+  const float v = acos_(dir.y) * c::INV_PI;
+  int x = f2i(floorf(u * (float)env.w)), y = f2i(floorf(v * (float)env.h));
+  x = ((x % env.w) + env.w) % env.w;
+  y = ((y % env.h) + env.h) % env.h;
+  const uchar4 cc = env.rgbe[(size_t)y * env.w + x];
+  const float r = (float)cc.x / 255.0f, g = (float)cc.y / 255.0f, b = (float)cc.z / 255.0f,
+              a = (float)cc.w / 255.0f;
+  const float p = pow_(2.0f, a * 255.0f - 128.0f);
+  return v3(r * p, g * p, b * p);
+}
+__device__ __forceinline__ void add_color(float4* color, uint32_t npix, uint32_t idx, float r, float g, float b,
+                                          float a, uint32_t* err) {
+  if (idx >= npix) { atomicOr(err, ERR_PIXEL); return; }
+  float4 c = color[idx];
+  c.x = c.x + r; c.y = c.y + g; c.z = c.z + b; c.w = c.w + a;
+  color[idx] = c;
+}
+
+// =====================================================================
+// trace.wgsl:83-189 / trace_shadow.wgsl:82-190: BVH traversal.
+// =====================================================================
+__device__ __forceinline__ float box_hit(float xa, float xb, float ya, float yb, float za, float zb, float ox,
+                                         float oy, float oz, float ix, float iy, float iz) {
+  // t1 uses the x_range.x bounds (quantised max), t2 the x_range.y bounds (min).
+  const float t1x = (xa - ox) * ix, t2x = (xb - ox) * ix;
+  const float t1y = (ya - oy) * iy, t2y = (yb - oy) * iy;
+  const float t1z = (za - oz) * iz, t2z = (zb - oz) * iz;
+  // fminf/fmaxf agree with minNum/maxNum except for the sign of a zero
+  // result, which only ever feeds comparisons here.
+  const float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
+  const float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
+  return (tmax >= tmin && tmax > 0.0f) ? tmin : MAX_T;
+}
+
+constexpr int TRACE_THREADS = 128;
+constexpr int STACK_SMEM = 32;   // per-thread entries kept in shared memory
+constexpr int STACK_LOCAL = 32;  // overflow entries in local memory (total depth 64)
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
+                                         float dz, float& best_t, int& best_i, uint32_t& best_b,
+                                         int (*sstack)[TRACE_THREADS], uint32_t* err, uint32_t& nfetch,
+                                         uint32_t& ntest) {
+  const float eps = ANY ? 1e-7f : 1e-8f;
+  const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  int lstack[STACK_LOCAL];
+  const int tid = threadIdx.x;
+  int sp = 0;
+  int cur = sc.root;
+  best_t = MAX_T;
+  best_i = -1;
+  best_b = 0u;
+  for (;;) {
+    if (cur >= 0) {
+      if (COUNT) nfetch += 3;
+      const float4* rec = sc.inner + 4 * (size_t)cur;
+      const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
+      const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
+      const float lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
+      const float rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+      const bool lok = lh < best_t, rok = rh < best_t;
+      if (lok && rok) {
+        int nearc, farc;
+        if (lh > rh) { nearc = ch.y; farc = ch.x; } else { nearc = ch.x; farc = ch.y; }
+        if (sp < STACK_SMEM) sstack[sp][tid] = farc;
+        else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+        else { atomicOr(err, ERR_STACK); break; }
+        ++sp;
+        cur = nearc;
+        continue;
+      }
+      if (lok) { cur = ch.x; continue; }
+      if (rok) { cur = ch.y; continue; }
+    } else {
+      if (COUNT) nfetch += 1;
+      const uint32_t word = (uint32_t)cur & 0x7fffffffu;
+      const int size = (int)(word >> 24);
+      const int base = (int)(word & 0x00ffffffu);
+      for (int i = 0; i < size; i++) {
+        if (COUNT) ntest += 1;
+        const float4* tp = sc.tris + 3 * (size_t)(base + i);
+        const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
+        const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
+        const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+        const float det = e1x * px + e1y * py + e1z * pz;
+        if (fabsf(det) < eps) continue;
+        const float inv_det = 1.0f / det;
+        const float tx = ox - A.x, ty = oy - A.y, tz = oz - A.z;
+        const float u = (tx * px + ty * py + tz * pz) * inv_det;
+        if (u < 0.0f || u > 1.0f) continue;
+        const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+        const float v = (dx * qx + dy * qy + dz * qz) * inv_det;
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
+        const float res = dist > eps ? dist : MAX_T;
+        if (res < best_t) {
+          best_t = res;
+          best_i = base + i;
+          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        }
+      }
+      if (ANY && best_i != -1) break;
+    }
+    if (sp == 0) break;
+    --sp;
+    cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+  }
+}
+
+// trace.wgsl:191-213 main (closest hit) and trace_shadow.wgsl:192-207 main (any
+// hit).  Warps claim 32 consecutive queue slots at a time; the outcome bit of
+// every slot goes to flags[slot / 32].  FUSED: a ray that reaches the
+// environment adds its shade_miss.wgsl contribution directly (the miss queue
+// is not materialised); otherwise the compaction kernel builds the miss queue.
+template <bool ANY, bool FUSED, bool COUNT>
+__global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+                                                          const uint32_t* __restrict__ countp, RayQ R,
+                                                          uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
+                                                          float4* __restrict__ color, uint32_t npix,
+                                                          uint32_t* __restrict__ ticket) {
+  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+  const uint32_t n = *countp;
+  const int lane = threadIdx.x & 31;
+  const float theta = ctr->env_theta;
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays_traced, (unsigned long long)n);
+  uint32_t nfetch = 0, ntest = 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(ticket, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const uint32_t j = base + lane;
+    bool hit = false;
+    if (j < n) {
+      const float4 o = R.o[j], d = R.d[j];
+      float bt;
+      int bi;
+      uint32_t bb;
+      traverse<ANY, COUNT>(sc, o.x, o.y, o.z, d.x, d.y, d.z, bt, bi, bb, sstack, &ctr->err, nfetch, ntest);
+      hit = bi != -1;
+      if (hit && !ANY) hrec[j] = make_uint4(__float_as_uint(bt), (uint32_t)bi, bb, 0u);
+      if (!hit && FUSED) {
+        const float4 tp = R.t[j];
+        const V3 e = env_color(env, theta, v3(d.x, d.y, d.z));
+        add_color(color, npix, __float_as_uint(tp.w) & 0x0fffffffu, e.x * tp.x, e.y * tp.y, e.z * tp.z, 1.0f,
+                  &ctr->err);
+      }
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) flags[base >> 5] = m;
+  }
+  if (COUNT) {
+    atomicAdd(&ctr->stat[ANY ? 2 : 0], (unsigned long long)nfetch);
+    atomicAdd(&ctr->stat[ANY ? 3 : 1], (unsigned long long)ntest);
+  }
+}
+
+// =====================================================================
+// Stable compaction of trace / shadow outcomes.
+//   MODE 0: closest-hit flags -> hit list (+ miss queue when MISSQ)
+//   MODE 1: any-hit flags     -> unoccluded shadow rays appended to the miss queue
+// =====================================================================
+constexpr int COMPACT_THREADS = 256;
+
+template <int MODE, bool MISSQ>
+__global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restrict__ ctr,
+                                                              const uint32_t* __restrict__ flags,
+                                                              uint32_t* __restrict__ hit_list, RayQ src, RayQ M,
+                                                              uint32_t miss_capacity, uint32_t* __restrict__ ticket,
+                                                              unsigned long long* __restrict__ tiles) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[COMPACT_THREADS / 32 + 1][2];
+  __shared__ unsigned long long s_excl;
+  const uint32_t n = MODE == 0 ? ctr->num_rays : ctr->num_shadow;
+  const uint32_t miss_base = MODE == 0 ? 0u : ctr->num_misses;
+  const uint32_t nwords = (n + 31) >> 5;
+  const uint32_t ntiles = (nwords + COMPACT_THREADS - 1) / COMPACT_THREADS;
+  if (ntiles == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (MODE == 0) { ctr->num_hits = 0; if (MISSQ) ctr->num_misses = 0; }
+    }
+    return;
+  }
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t w = tile * COMPACT_THREADS + threadIdx.x;
+    uint32_t valid = 0u, hm = 0u;
+    if (w < nwords) {
+      valid = (w == nwords - 1 && (n & 31u)) ? ((1u << (n & 31u)) - 1u) : 0xffffffffu;
+      hm = flags[w] & valid;
+    }
+    const uint32_t mm = valid & ~hm;
+    // MODE 0 counts hits (a) and misses (b); MODE 1 counts unoccluded rays (b).
+    const uint32_t ca = MODE == 0 ? (uint32_t)__popc(hm) : 0u;
+    const uint32_t cb = (MODE == 1 || MISSQ) ? (uint32_t)__popc(mm) : 0u;
+    uint32_t ea, eb, ta, tb;
+    block_scan2<COMPACT_THREADS / 32>(ca, cb, ea, eb, ta, tb, s_warp);
+    if (threadIdx.x == 0) s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    __syncthreads();
+    const uint32_t pa = unpack_a(s_excl) + ea;
+    uint32_t pb = unpack_b(s_excl) + eb;
+    if (MODE == 0) {
+      uint32_t bits = hm, k = pa;
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        hit_list[k++] = w * 32u + (uint32_t)b;
+      }
+    }
+    if (MODE == 1 || MISSQ) {
+      uint32_t bits = mm, k = miss_base + pb;
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        const uint32_t j = w * 32u + (uint32_t)b;
+        if (k < miss_capacity) {
+          M.o[k] = src.o[j];
+          M.d[k] = src.d[j];
+          M.t[k] = src.t[j];
+        } else {
+          atomicOr(&ctr->err, ERR_QUEUE);
+        }
+        ++k;
+      }
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+      const uint32_t tot_a = unpack_a(s_excl) + ta, tot_b = unpack_b(s_excl) + tb;
+      if (MODE == 0) {
+        ctr->num_hits = tot_a;
+        if (MISSQ) ctr->num_misses = tot_b;
+      } else {
+        ctr->num_misses = miss_base + tot_b;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// =====================================================================
+// shade_hit.wgsl:153-483
+// =====================================================================
+struct SI {
+  V3 b1, b2, n;
+  V3 wo, origin, base, spec, emission;
+  float metallic, opacity, alpha;
+};
+struct Sample {
+  V3 wi;
+  float pdf;
+};
+__device__ __forceinline__ float4 texel(const SceneDev& sc, int layer) {
+  const int l = layer < 0 ? 0 : (layer >= sc.n_layers ? sc.n_layers - 1 : layer);
+  const uchar4 t = sc.layers[l];
+  return make_float4((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f, (float)t.w / 255.0f);
+}
+__device__ __forceinline__ void unpack_snorm8x3(uint32_t w, V3& o) {
+  o.x = snorm8((int)(int8_t)(w & 0xffu));
+  o.y = snorm8((int)(int8_t)((w >> 8) & 0xffu));
+  o.z = snorm8((int)(int8_t)((w >> 16) & 0xffu));
+}
+// branchlessONB (:166-177)
+__device__ __forceinline__ void onb(V3 n, V3& b1, V3& b2) {
+  const float sign = n.z > 0.0f ? 1.0f : -1.0f;
+  const float a = -1.0f / (sign + n.z);
+  const float b = n.x * n.y * a;
+  b1 = v3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+  b2 = v3(b, sign + n.y * n.y * a, -n.y);
+}
+// getSurfaceInteraction (:179-200) + interpolateVertexAttribute (:363-394)
+__device__ __forceinline__ SI surface(const SceneDev& sc, V3 ro, V3 rd, float t, int index, uint32_t bary_mask) {
+  SI si;
+  const int4 tri = __ldg(sc.tri4 + index);
+  const float u = unorm16(bary_mask & 0xffffu), v = unorm16(bary_mask >> 16);
+  const V3 bary = v3(1.0f - u - v, u, v);
+  const uint4 a0 = __ldg(sc.attrs + tri.x), a1 = __ldg(sc.attrs + tri.y), a2 = __ldg(sc.attrs + tri.z);
+  V3 t0, t1, t2, q0, q1, q2, n0, n1, n2;
+  unpack_snorm8x3(a0.x, t0); unpack_snorm8x3(a1.x, t1); unpack_snorm8x3(a2.x, t2);
+  unpack_snorm8x3(a0.y, q0); unpack_snorm8x3(a1.y, q1); unpack_snorm8x3(a2.y, q2);
+  unpack_snorm8x3(a0.z, n0); unpack_snorm8x3(a1.z, n1); unpack_snorm8x3(a2.z, n2);
+  const V3 T = normalize(matvec(t0, t1, t2, bary));
+  const V3 B = normalize(matvec(q0, q1, q2, bary));
+  const V3 N = normalize(matvec(n0, n1, n2, bary));
+  const int4 mat = __ldg(sc.mat4 + tri.w);
+  const float4 nm = texel(sc, mat.z);
+  const V3 map_normal = mul(sub(v3(nm.x, nm.y, nm.z), v3(0.5f, 0.5f, 0.0f)), v3(2.0f, 2.0f, 1.0f));
+  si.n = normalize(matvec(T, B, N, map_normal));
+  si.origin = add(ro, scale(rd, t - SHADE_EPS * 40.0f));
+  onb(si.n, si.b1, si.b2);
+  si.wo = vecmat(neg(rd), si.b1, si.b2, si.n);
+  const float4 dif = texel(sc, mat.x);
+  si.base = v3(dif.x, dif.y, dif.z);
+  si.opacity = dif.w;
+  const float4 mr = texel(sc, mat.y);
+  si.metallic = mr.z;
+  si.alpha = mr.y * mr.y;
+  const float4 em = texel(sc, mat.w);
+  si.emission = v3(em.x, em.y, em.z);
+  si.spec = v3(mix1(1.0f, si.base.x, si.metallic), mix1(1.0f, si.base.y, si.metallic),
+               mix1(1.0f, si.base.z, si.metallic));
+  return si;
+}
+__device__ __forceinline__ float pdf_texel(const EnvDev& env, int x, int y) {
+  if (x < 0 || y < 0 || x >= env.w || y >= env.h) return 0.0f;
+  return __ldg(env.pdf + (size_t)x + (size_t)env.w * (size_t)y);
+}
+// envPdf (:202-210)
+__device__ __forceinline__ float env_pdf_dir(const EnvDev& env, float theta, V3 dir) {
+  const float a = 1.0f + theta + atan2_(dir.z, dir.x) / c::TAU;
+  const float u = a - truncf(a);
+  const float v = acos_(dir.y) * c::INV_PI;
+  const int cx = f2i(u * (float)env.w), cy = f2i(v * (float)env.h);
+  const float sin_phi = sin_(v * c::PI);
+  return pdf_texel(env, cx, cy) / sin_phi;
+}
+// sampleEnv (:213-227)
+__device__ __forceinline__ Sample sample_env(const EnvDev& env, float theta, Hash& h, const SI& si) {
+  const int idx = (int)(h.next() % (uint32_t)env.nb);
+  const int2 bin = __ldg(env.bins + idx);
+  const int ci = (int)(h.next() % (uint32_t)(bin.y - bin.x)) + bin.x;
+  const int2 cc = __ldg(env.coords + ci);
+  const float u = -theta + ((0.5f + (float)cc.x) / (float)env.w);
+  const float v = (0.5f + (float)cc.y) / (float)env.h;
+  const float th = u * c::TAU;
+  const float phi = v * c::PI;
+  const float sin_phi = sin_(phi);
+  const V3 dir = v3(cos_(th) * sin_phi, cos_(phi), sin_(th) * sin_phi);
+  Sample s;
+  s.pdf = pdf_texel(env, cc.x, cc.y) / sin_phi;
+  s.wi = vecmat(dir, si.b1, si.b2, si.n);
+  return s;
+}
+__device__ __forceinline__ float lambert_pdf(V3 wi) { return fmax_(wi.z, SHADE_EPS) * c::INV_PI; }
+__device__ __forceinline__ V3 eval_lambert(const SI& si, const Sample& s) {
+  const float w = fmax_(SHADE_EPS, s.wi.z);
+  return v3(si.base.x * c::INV_PI * w / s.pdf, si.base.y * c::INV_PI * w / s.pdf, si.base.z * c::INV_PI * w / s.pdf);
+}
+__device__ __forceinline__ float ggx_d(V3 m, float au, float av) {
+  const float auv = au * av;
+  const float tx = m.x / au;
+  const float ty = m.y / av;
+  const float ell = tx * tx + ty * ty + m.z * m.z;
+  return 1.0f / (c::PI * auv * ell * ell);
+}
+__device__ __forceinline__ float ggx_g1(V3 w, V3 m, float au, float av) {
+  const float ax = w.x * au;
+  const float ay = w.y * av;
+  const float axy2 = ax * ax + ay * ay;
+  const float tan_theta = axy2 / (w.z * w.z);
+  const float result = 2.0f / (1.0f + sqrtf(1.0f + tan_theta));
+  return (dot(w, m) * dot(w, v3(0.0f, 0.0f, 1.0f)) <= 0.0f) ? 0.0f : result;
+}
+__device__ __forceinline__ float specular_pdf(const SI& si, V3 m) {
+  const float a = si.alpha;
+  return fmax_(SHADE_EPS, ggx_d(m, a, a) * ggx_g1(si.wo, m, a, a) / (4.0f * si.wo.z));
+}
+__device__ __forceinline__ V3 eval_specular(const SI& si, const Sample& s) {
+  const float a = si.alpha;
+  const V3 hv = normalize(add(si.wo, s.wi));
+  const float D = ggx_d(hv, a, a);
+  const float G = ggx_g1(s.wi, hv, a, a) * ggx_g1(si.wo, hv, a, a);
+  const float k = fmax_(D * G / (4.0f * si.wo.z * s.pdf), 0.0f);
+  return scale(si.spec, k);
+}
+__device__ __forceinline__ float power_heuristic(float p0, float p1) {
+  const float p02 = p0 * p0;
+  return p02 / (p02 + p1 * p1);
+}
+// sampleGGX (:295-316)
+__device__ __forceinline__ V3 sample_ggx(Hash& h, const SI& si) {
+  const float au = si.alpha, av = si.alpha;
+  const V3 vh = normalize(v3(au * si.wo.x, av * si.wo.y, si.wo.z));
+  const float lensq = vh.x * vh.x + vh.y * vh.y;
+  const V3 t1v = lensq > 0.0f ? scale(v3(-vh.y, vh.x, 0.0f), 1.0f / sqrtf(lensq)) : v3(1.0f, 0.0f, 0.0f);
+  const V3 t2v = cross(vh, t1v);
+  const float r = sqrtf(h.rand());
+  const float phi = c::TAU * h.rand();
+  const float t1 = r * cos_(phi);
+  float t2 = r * sin_(phi);
+  const float s = 0.5f * (1.0f + vh.z);
+  t2 = (1.0f - s) * sqrtf(1.0f - t1 * t1) + s * t2;
+  const V3 nh = add(add(scale(t1v, t1), scale(t2v, t2)), scale(vh, sqrtf(fmax_(0.0f, 1.0f - t1 * t1 - t2 * t2))));
+  return normalize(v3(au * nh.x, av * nh.y, fmax_(0.0f, nh.z)));
+}
+__device__ __forceinline__ float schlick(float cos_theta, float ior) {
+  float r0 = (1.0f - ior) / (1.0f + ior);
+  r0 = r0 * r0;
+  const float tmp = 1.0f - cos_theta;
+  const float tmp2 = tmp * tmp;
+  return r0 + (1.0f - r0) * tmp2 * tmp2 * tmp;
+}
+
+constexpr int SHADE_THREADS = 128;
+
+// main (:407-483).  Tiles of SHADE_THREADS hits are claimed in order; bounce
+// and shadow rays are written at their stable ranks found by a block scan plus
+// decoupled look-back, so slot order equals the serial order of the reference.
+__global__ void __launch_bounds__(SHADE_THREADS) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+                                                          const uint32_t* __restrict__ hit_list,
+                                                          const uint4* __restrict__ hrec, RayQ Rin, RayQ Rout,
+                                                          RayQ S, uint32_t capacity, float4* __restrict__ color,
+                                                          uint32_t npix, uint32_t* __restrict__ ticket,
+                                                          unsigned long long* __restrict__ tiles) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[SHADE_THREADS / 32 + 1][2];
+  __shared__ unsigned long long s_excl;
+  const uint32_t nh = ctr->num_hits;
+  const int32_t samples = ctr->samples;
+  const float theta = ctr->env_theta;
+  const uint32_t ntiles = (nh + SHADE_THREADS - 1) / SHADE_THREADS;
+  if (ntiles == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) { ctr->num_rays = 0; ctr->num_shadow = 0; }
+    return;
+  }
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t r = tile * SHADE_THREADS + threadIdx.x;
+    bool eb = false, es = false;
+    float4 bo, bd, bt, so, sd, st;
+    if (r < nh) {
+      const uint32_t j = hit_list[r];
+      const uint4 hr = hrec[j];
+      const float4 o4 = Rin.o[j], d4 = Rin.d[j], t4 = Rin.t[j];
+      const V3 ro = v3(o4.x, o4.y, o4.z), rd = v3(d4.x, d4.y, d4.z);
+      const float ht = __uint_as_float(hr.x);
+      const uint32_t mask = __float_as_uint(t4.w);
+      const uint32_t color_idx = mask & 0x0fffffffu;
+      const uint32_t ray_type = mask & 0xf0000000u;
+      Hash h;
+      h.seed = (r * 1973u + color_idx * 9277u + (uint32_t)samples * 26699u) | 1u;
+      h.seed = h.next();
+      const SI si = surface(sc, ro, rd, ht, (int)hr.y, hr.z);
+      if (h.rand() > si.opacity) {
+        const V3 ao = add(ro, scale(rd, ht + SHADE_EPS * 40.0f));
+        eb = true;
+        bo = make_float4(ao.x, ao.y, ao.z, 0.0f);
+        bd = d4;
+        bt = t4;
+      } else if (dot(si.emission, v3(1.0f, 1.0f, 1.0f)) > 0.0f) {
+        const float att = fmax_(dot(si.n, matvec(si.b1, si.b2, si.n, si.wo)), 0.0f);
+        add_color(color, npix, color_idx, 50.0f * si.emission.x * t4.x * att, 50.0f * si.emission.y * t4.y * att,
+                  50.0f * si.emission.z * t4.z * att, 1.0f, &ctr->err);
+      } else if (ray_type != 0x10000000u) {
+        const V3 m = sample_ggx(h, si);
+        const float f = mix1(schlick(fmax_(dot(si.wo, m), 0.0f), 1.5f), 1.0f, si.metallic);
+        Sample bs;
+        V3 bsdf;
+        if (h.rand() > f) {
+          const float lr = sqrtf(h.rand());
+          const float lphi = c::TAU * h.rand();
+          const float x = lr * cos_(lphi);
+          const float y = lr * sin_(lphi);
+          const float z = sqrtf(fmax_(0.0f, 1.0f - x * x - y * y));
+          bs.wi = v3(x, y, z);
+          bs.pdf = lambert_pdf(bs.wi);
+          bsdf = eval_lambert(si, bs);
+        } else {
+          bs.wi = reflect(neg(si.wo), m);
+          bs.pdf = specular_pdf(si, m);
+          bsdf = eval_specular(si, bs);
+        }
+        if (bs.wi.z > 0.0f) {
+          const V3 dir = matvec(si.b1, si.b2, si.n, bs.wi);
+          const float weight = env.enabled ? power_heuristic(bs.pdf, env_pdf_dir(env, theta, dir)) : 1.0f;
+          eb = true;
+          bo = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
+          bd = make_float4(dir.x, dir.y, dir.z, 0.0f);
+          bt = make_float4(bsdf.x * t4.x * weight, bsdf.y * t4.y * weight, bsdf.z * t4.z * weight, t4.w);
+        }
+        if (env.enabled) {
+          const Sample es_ = sample_env(env, theta, h, si);
+          if (dot(es_.wi, m) > 0.0f && es_.wi.z > 0.0f) {
+            // createMaterialSampleRay (:339-348)
+            const float lw = power_heuristic(es_.pdf, lambert_pdf(es_.wi));
+            const V3 el = eval_lambert(si, es_);
+            V3 scv = scale(v3((1.0f - f) * el.x, (1.0f - f) * el.y, (1.0f - f) * el.z), lw);
+            const V3 hv = normalize(add(si.wo, es_.wi));
+            const float sw = power_heuristic(es_.pdf, specular_pdf(si, hv));
+            const V3 ev = eval_specular(si, es_);
+            scv = add(scv, scale(v3(f * ev.x, f * ev.y, f * ev.z), sw));
+            const V3 sdir = matvec(si.b1, si.b2, si.n, es_.wi);
+            es = true;
+            so = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
+            sd = make_float4(sdir.x, sdir.y, sdir.z, 0.0f);
+            st = make_float4(scv.x * t4.x, scv.y * t4.y, scv.z * t4.z, t4.w);
+          }
+        }
+      }
+    }
+    uint32_t ea, es2, ta, tb;
+    block_scan2<SHADE_THREADS / 32>(eb ? 1u : 0u, es ? 1u : 0u, ea, es2, ta, tb, s_warp);
+    if (threadIdx.x == 0) s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    __syncthreads();
+    const uint32_t pb = unpack_a(s_excl) + ea, ps = unpack_b(s_excl) + es2;
+    if (eb) {
+      if (pb < capacity) { Rout.o[pb] = bo; Rout.d[pb] = bd; Rout.t[pb] = bt; }
+      else atomicOr(&ctr->err, ERR_QUEUE);
+    }
+    if (es) {
+      if (ps < capacity) { S.o[ps] = so; S.d[ps] = sd; S.t[ps] = st; }
+      else atomicOr(&ctr->err, ERR_QUEUE);
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) {
+      ctr->num_rays = unpack_a(s_excl) + ta;
+      ctr->num_shadow = unpack_b(s_excl) + tb;
+    }
+    __syncthreads();
+  }
+}
+
+// shade_miss.wgsl:45-57 over the materialised miss queue.
+__global__ void __launch_bounds__(128) k_shade_miss(EnvDev env, Counters* __restrict__ ctr, RayQ M,
+                                                    float4* __restrict__ color, uint32_t npix) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= ctr->num_misses) return;
+  const float4 d = M.d[tid], tp = M.t[tid];
+  const V3 e = env_color(env, ctr->env_theta, v3(d.x, d.y, d.z));
+  add_color(color, npix, __float_as_uint(tp.w) & 0x0fffffffu, e.x * tp.x, e.y * tp.y, e.z * tp.z, 1.0f, &ctr->err);
+}
+
+// accumulate.wgsl:20-34 (pixels x < W only; the reference's `>` bound lets
+// invocation x == W alias pixel (0, y+1) in a race, which is not reproduced).
+__global__ void __launch_bounds__(256) k_accumulate(const Counters* __restrict__ ctr, const float4* __restrict__ color,
+                                                    float4* __restrict__ accum, uint32_t npix) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const float s = (float)ctr->samples, s1 = (float)(ctr->samples + 1);
+  const float4 c = color[i];
+  float4 a = accum[i];
+  a.x = (fmax_(c.x, 0.0f) + a.x * s) / s1;
+  a.y = (fmax_(c.y, 0.0f) + a.y * s) / s1;
+  a.z = (fmax_(c.z, 0.0f) + a.z * s) / s1;
+  a.w = 1.0f;
+  accum[i] = a;
+}
+
+// postprocess.wgsl:36-99 frag_main as a compute kernel writing a headless buffer.
+__device__ __forceinline__ float rrt(float v) {
+  const float a = v * (v + 0.0245786f) - 0.000090537f;
+  const float b = v * (0.983729f * v + 0.4329510f) + 0.238081f;
+  return a / b;
+}
+__global__ void __launch_bounds__(256) k_postprocess(const float4* __restrict__ accum, float4* __restrict__ out,
+                                                     uchar4* __restrict__ out8, uint32_t npix, float exposure,
+                                                     float saturation) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const float4 a4 = accum[i];
+  V3 cc = scale(v3(a4.x, a4.y, a4.z), exposure);
+  V3 o = vecmat(cc, v3(0.59719f, 0.35458f, 0.04823f), v3(0.07600f, 0.90834f, 0.01566f), v3(0.02840f, 0.13383f, 0.83777f));
+  o = v3(rrt(o.x), rrt(o.y), rrt(o.z));
+  o = vecmat(o, v3(1.60475f, -0.53108f, -0.07367f), v3(-0.10208f, 1.10813f, -0.00605f), v3(-0.00327f, -0.07276f, 1.07602f));
+  o = v3(clamp_(o.x, 0.0f, 1.0f), clamp_(o.y, 0.0f, 1.0f), clamp_(o.z, 0.0f, 1.0f));
+  const float oms = 1.0f - saturation;
+  const V3 red = add(v3(0.3086f * oms, 0.3086f * oms, 0.3086f * oms), v3(saturation, 0.0f, 0.0f));
+  const V3 green = add(v3(0.6094f * oms, 0.6094f * oms, 0.6094f * oms), v3(0.0f, saturation, 0.0f));
+  const V3 blue = add(v3(0.0820f * oms, 0.0820f * oms, 0.0820f * oms), v3(0.0f, 0.0f, saturation));
+  o = matvec(red, green, blue, o);
+  float ch[3] = {o.x, o.y, o.z};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float cut = ch[k] <= 0.0031308f ? 1.0f : 0.0f;
+    const float higher = 1.055f * pow_(ch[k], 1.0f / 2.4f) - 0.055f;
+    const float lower = ch[k] * 12.92f;
+    ch[k] = higher * (1.0f - cut) + lower * cut;
+  }
+  out[i] = make_float4(ch[0], ch[1], ch[2], 1.0f);
+  uchar4 q;
+  q.x = (unsigned char)floorf(clamp_(ch[0], 0.0f, 1.0f) * 255.0f + 0.5f);
+  q.y = (unsigned char)floorf(clamp_(ch[1], 0.0f, 1.0f) * 255.0f + 0.5f);
+  q.z = (unsigned char)floorf(clamp_(ch[2], 0.0f, 1.0f) * 255.0f + 0.5f);
+  q.w = 255;
+  out8[i] = q;
+}
+
+__global__ void k_end_frame(Counters* ctr) { ctr->samples += 1; }
+
+// Elementwise math probes (same numbering as the oracle's or_math).
+__global__ void k_math(int fn, const float* __restrict__ x, const float* __restrict__ y, float* __restrict__ out,
+                       uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float a = x[i], b = y ? y[i] : 0.0f;
+  float r;
+  switch (fn) {
+    case 0: r = sin_(a); break;
+    case 1: r = cos_(a); break;
+    case 2: r = tan_(a); break;
+    case 3: r = atan2_(a, b); break;
+    case 4: r = acos_(a); break;
+    case 5: r = exp2_(a); break;
+    case 6: r = log2_(a); break;
+    case 7: r = pow_(a, b); break;
+    default: r = __int_as_float(0x7fc00000);
+  }
+  out[i] = r;
+}
+
+// =====================================================================
+// launchers
+// =====================================================================
+static unsigned grid_for(uint32_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+uint32_t compact_tiles(uint32_t capacity) { return ((capacity + 31u) / 32u + COMPACT_THREADS - 1) / COMPACT_THREADS; }
+uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) / SHADE_THREADS; }
+
+// Persistent grids: enough resident blocks to fill every multiprocessor, never
+// more blocks than there can be work items.
+void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade) {
+  int t = 0, c = 0, s = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace<false, true, false>, TRACE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_shade, SHADE_THREADS, 0);
+  const unsigned warps = (capacity + 31u) / 32u;
+  *trace = std::max(1u, std::min((unsigned)(sms * std::max(t, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
+  *compact = std::max(1u, std::min((unsigned)(sms * std::max(c, 1)), compact_tiles(capacity)));
+  *shade = std::max(1u, std::min((unsigned)(sms * std::max(s, 1)), shade_tiles(capacity)));
+}
+
+void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
+  if (n_threads == 0) return;
+  k_camera<<<grid_for(n_threads, 128), 128, 0, L.stream>>>(L.cam, L.ctr, R, n_threads, L.capacity);
+}
+
+void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
+                  uint4* hrec, uint32_t* flags, uint32_t* ticket) {
+  const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
+#define PK_TRACE(A, F, C) \
+  k_trace<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
+  if (!any_hit) {
+    if (fused) { if (count) PK_TRACE(false, true, true); else PK_TRACE(false, true, false); }
+    else { if (count) PK_TRACE(false, false, true); else PK_TRACE(false, false, false); }
+  } else {
+    if (fused) { if (count) PK_TRACE(true, true, true); else PK_TRACE(true, true, false); }
+    else { if (count) PK_TRACE(true, false, true); else PK_TRACE(true, false, false); }
+  }
+#undef PK_TRACE
+}
+
+void launch_compact_trace(const LaunchCtx& L, bool missq, const uint32_t* flags, uint32_t* hit_list, RayQ src,
+                          RayQ M, uint32_t* ticket, unsigned long long* tiles) {
+  const unsigned grid = L.compact_blocks;
+  if (missq)
+    k_compact<0, true><<<grid, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, hit_list, src, M, L.miss_capacity,
+                                                                ticket, tiles);
+  else
+    k_compact<0, false><<<grid, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, hit_list, src, M, L.miss_capacity,
+                                                                 ticket, tiles);
+}
+
+void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, RayQ M, uint32_t* ticket,
+                           unsigned long long* tiles) {
+  k_compact<1, true><<<L.compact_blocks, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, nullptr, S, M,
+                                                                           L.miss_capacity, ticket, tiles);
+}
+
+void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,
+                  uint32_t* ticket, unsigned long long* tiles) {
+  k_shade<<<L.shade_blocks, SHADE_THREADS, 0, L.stream>>>(L.scene, L.env, L.ctr, hit_list, hrec, Rin, Rout, S,
+                                                          L.capacity, L.color, L.npix, ticket, tiles);
+}
+
+void launch_shade_miss(const LaunchCtx& L, RayQ M) {
+  k_shade_miss<<<grid_for(L.miss_capacity, 128), 128, 0, L.stream>>>(L.env, L.ctr, M, L.color, L.npix);
+}
+
+void launch_accumulate(const LaunchCtx& L) {
+  k_accumulate<<<grid_for(L.npix, 256), 256, 0, L.stream>>>(L.ctr, L.color, L.accum, L.npix);
+}
+
+void launch_postprocess(const LaunchCtx& L, float exposure, float saturation) {
+  k_postprocess<<<grid_for(L.npix, 256), 256, 0, L.stream>>>(L.accum, L.display, L.display8, L.npix, exposure,
+                                                             saturation);
+}
+
+void launch_end_frame(const LaunchCtx& L) { k_end_frame<<<1, 1, 0, L.stream>>>(L.ctr); }
+
+void launch_math(cudaStream_t s, int fn, const float* x, const float* y, float* out, uint32_t n) {
+  if (n == 0) return;
+  k_math<<<grid_for(n, 256), 256, 0, s>>>(fn, x, y, out, n);
+}
+
+}  // namespace pk

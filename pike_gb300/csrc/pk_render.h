@@ -1,0 +1,59 @@
+// pk_render.h -- host-side launchers of the per-frame kernels (pk_render.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "pk_internal.cuh"
+
+namespace pk {
+
+// Everything a launch needs that is fixed for a configured context.
+struct LaunchCtx {
+  cudaStream_t stream;
+  Counters* ctr;
+  const CamState* cam;
+  SceneDev scene;
+  EnvDev env;
+  float4* color;
+  float4* accum;
+  float4* display;
+  uchar4* display8;
+  uint32_t npix;
+  uint32_t capacity;       // ray / hit / shadow queue capacity (batch rounded up to 128)
+  uint32_t miss_capacity;  // 2 * capacity
+  unsigned trace_blocks, compact_blocks, shade_blocks;
+};
+
+void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads);
+// Kernels that claim work through an atomic ticket take it as `ticket`; the
+// look-back kernels also take a zeroed tile-state array (one word per tile).
+void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
+                  uint4* hrec, uint32_t* flags, uint32_t* ticket);
+void launch_compact_trace(const LaunchCtx& L, bool missq, const uint32_t* flags, uint32_t* hit_list, RayQ src,
+                          RayQ M, uint32_t* ticket, unsigned long long* tiles);
+void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, RayQ M, uint32_t* ticket,
+                           unsigned long long* tiles);
+void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,
+                  uint32_t* ticket, unsigned long long* tiles);
+// Grid sizes for a queue capacity on a GPU with `sms` multiprocessors.
+void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade);
+// Tile counts the look-back kernels need for a given queue capacity.
+uint32_t compact_tiles(uint32_t capacity);
+uint32_t shade_tiles(uint32_t capacity);
+void launch_shade_miss(const LaunchCtx& L, RayQ M);
+void launch_accumulate(const LaunchCtx& L);
+void launch_postprocess(const LaunchCtx& L, float exposure, float saturation);
+void launch_end_frame(const LaunchCtx& L);
+void launch_math(cudaStream_t s, int fn, const float* x, const float* y, float* out, uint32_t n);
+
+// pk_scene.cu
+// Convert the reference 20-byte BFS nodes + leaf-ordered triangles + 16-byte
+// vertices into the traversal format (inner records, v0/e1/e2 triangles).
+int convert_bvh(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4* tri4, uint32_t n_tris,
+                const float4* verts4, uint32_t n_verts, float4* inner, float4* tris, int* root_code,
+                uint32_t* err);
+// Row S: per-vertex attribute quantisation (scene.js:456-470).
+void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
+                    uint32_t n, double scale, double tx, double ty, double tz, double* pos_out3, uint4* attrs);
+
+}  // namespace pk

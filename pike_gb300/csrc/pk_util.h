@@ -1,0 +1,56 @@
+// pk_util.h -- small host helpers: owned device buffers, device-wide scans and sorts.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace pk {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+inline void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Owned device allocation (cudaMalloc / cudaFree).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    if (count) check(cudaMalloc(&p, count * sizeof(T) > 0 ? count * sizeof(T) : 1), "cudaMalloc");
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// Exclusive prefix sum of n u32 values (in may alias out).  If total is not
+// null it receives the sum (device pointer).  Counts must stay below 2^31.
+void scan_exclusive_u32(cudaStream_t s, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total);
+
+// Stable LSD radix sort of (key, value) pairs by the low `bits` bits of the
+// 64-bit keys, ascending.  Sorts in place using the given scratch buffers.
+void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64_t* keys_tmp, uint32_t* vals_tmp,
+                          uint32_t n, int bits);
+
+}  // namespace pk

@@ -1,0 +1,131 @@
+"""Whole-frame parity: pk_render_frame (misses shaded inside the traversal
+kernels) against the oracle's tick(), and against the GPU's own pass-by-pass
+path; plus size-independent properties at the benchmark's full size."""
+import numpy as np
+import pytest
+
+from pike_gb300 import _lib, synth
+from pike_gb300._lib import ptr
+
+from helpers import Pair, assert_bits_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def fused_frames(pair: Pair, frames: int, bounces: int, start: int = 0):
+    pair.ctx.call("pk_set_render_state", start, 0.0)
+    pair.ctx.call("pk_render_frames", frames, bounces)
+    pair.ctx.call("pk_sync")
+
+
+def oracle_frames(pair: Pair, frames: int, bounces: int, start: int = 0):
+    P = pair.P.r
+    P.set_render_state(start)
+    for _ in range(frames):
+        P.tick(bounces)
+
+
+def test_fused_small_scene_matches_oracle(oracle, pk_built):
+    src = synth.small_scene()  # 256x256, 770 triangles, 4 spp, 4 bounces
+    pair = Pair(src, oracle)
+    fused_frames(pair, src.spp, src.bounces)
+    oracle_frames(pair, src.spp, src.bounces)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "accumulated radiance")
+    assert np.array_equal(pair.image("display"), pair.P.r.display()[1])
+    c = pair.counters()
+    assert c["samples"] == src.spp and c["err"] == 0
+
+
+def test_fused_sphere_matches_oracle(oracle, pk_built):
+    src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
+    pair = Pair(src, oracle)
+    fused_frames(pair, 3, 8)
+    oracle_frames(pair, 3, 8)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "accumulated radiance")
+
+
+@pytest.mark.slow
+def test_fused_full_geometry_matches_oracle(oracle, pk_built):
+    """The 1.3M-triangle scene and 2048x1024 environment of the benchmark, at a
+    reduced resolution the oracle finishes in seconds."""
+    src = synth.displaced_sphere_scene(width=192, height=108)
+    pair = Pair(src, oracle, threads=16)
+    fused_frames(pair, 2, 8)
+    oracle_frames(pair, 2, 8)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "accumulated radiance")
+
+
+def test_fused_equals_pass_path(oracle, pk_built):
+    src = synth.displaced_sphere_scene(subdivisions=6, width=320, height=180, env_size=(512, 256))
+    a = Pair(src, oracle)
+    fused_frames(a, 2, 8)
+    fused = a.image("accum")
+    c = a.ctx
+    c.call("pk_write_accum", ptr(np.zeros_like(fused)))
+    for f in range(2):
+        c.call("pk_set_render_state", f, 0.0)
+        for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
+            c.call("pk_" + name)
+        for _ in range(8):
+            for name in ("trace", "shade_hit", "trace_shadow", "shade_miss"):
+                c.call("pk_" + name)
+        c.call("pk_accumulate")
+    assert_bits_equal(a.image("accum"), fused, "pass path vs fused frame")
+
+
+def test_full_size_determinism_and_counts(oracle, pk_built):
+    """1920x1080 on the 1.3M-triangle scene: two renders are bit-identical, no
+    device error flags, and the ray counts obey the queue invariants."""
+    src = synth.displaced_sphere_scene()
+    pair = Pair(src, oracle, threads=16)
+    c = pair.ctx
+    c.call("pk_reset_stats")
+    fused_frames(pair, 2, 8)
+    first = pair.image("accum").copy()
+    cnt = pair.counters()
+    assert cnt["err"] == 0
+    npix = src.width * src.height
+    assert npix * 2 <= cnt["rays_traced"] <= npix * 2 * 8 * 2
+    c.call("pk_write_accum", ptr(np.zeros_like(first)))
+    fused_frames(pair, 2, 8)
+    assert_bits_equal(pair.image("accum"), first, "re-render")
+    assert np.isfinite(first).all()
+
+
+def test_empty_queues_all_rays_miss(oracle, pk_built):
+    src = synth.small_scene(width=64, height=64)
+    pair = Pair(src, oracle)
+    st = dict(src.camera_state(), dir=[0.0, 1.0, 0.0])  # looking straight up at the sky
+    st["dir"] = [0.0, 0.9999999, 0.0004]
+    pair.set_camera(st)
+    fused_frames(pair, 1, 4)
+    oracle_frames(pair, 1, 4)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "sky-only frame")
+    assert pair.counters()["num_hits"] == 0
+
+
+def test_odd_resolution_accumulate(oracle, pk_built):
+    src = synth.small_scene(width=131, height=77)
+    pair = Pair(src, oracle)
+    fused_frames(pair, 2, 3)
+    oracle_frames(pair, 2, 3)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "odd resolution")
+
+
+def test_pass_before_scene_is_an_error(pk_built):
+    ctx = _lib.Context(0)
+    ctx.call("pk_configure", 8, 8, 64)
+    with pytest.raises(_lib.PikeError) as e:
+        ctx.call("pk_trace")
+    assert e.value.code == _lib.PK_ERR_ARG or e.value.code == _lib.PK_ERR_STATE
+
+
+def test_malformed_bvh_upload_rejected(oracle, pk_built):
+    src = synth.small_scene(width=8, height=8)
+    pair = Pair(src, oracle)
+    b = pair.P.bvh
+    nodes = b.nodes.copy()
+    nodes[0, 0] = 10**6  # child index outside the node array
+    with pytest.raises(_lib.PikeError):
+        pair.ctx.call("pk_bvh_upload", ptr(nodes), nodes.shape[0], ptr(b.tris), b.tris.shape[0], ptr(b.verts),
+                      b.verts.shape[0])
