@@ -1,0 +1,418 @@
+#!/usr/bin/env python
+"""Benchmark of Pike's wavefront path tracer on one GB300 (or N replicas).
+
+Workload: the incoherent 1080p scene -- an icosphere subdivided 8 times
+(1,310,720 triangles) displaced by value noise inside an open 10x10x10 box
+(10 triangles), 256 GGX/Lambert material groups, a 2048x1024 log-normal HDR
+environment with a sun -- rendered at 1920x1080 with 8 bounces.  One step is
+one PikeRenderer.tick(): one sample per pixel, camera rays, 8 x (closest-hit
+trace, shade, shadow trace), accumulate and tonemap.  The 64-spp job is 64
+steps.  Inputs are synthetic (seeded generators of that shape).
+
+Metric: Mrays/s (closest-hit + shadow rays traced per second, whole job),
+with spp*Mpix/s alongside.  `value` is device time (CUDA events on the
+library's stream) with the scene resident in HBM; `e2e` runs the same steps
+through the C ABI with the per-step render state and camera uploaded from
+pinned host memory and the 8-bit image read back into pinned host memory.
+
+--impl reference times the CPU restatement of the reference path (the oracle;
+the reference itself is JavaScript + WGSL on WebGPU and cannot run here) on
+the host cores, on a bounded band of the same frame.
+
+Multi-GPU: the path shards by sample, so N ranks render N independent
+replicas (rank r renders samples r, r+N, ...); no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s, spp/s @1080p"
+UNIT = "Mrays/s"
+WORKLOAD = "icosphere8+openbox 1920x1080, 8 bounces, 1 spp per step (64-spp job = 64 steps)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--bounces", type=int, default=8)
+    ap.add_argument("--subdivisions", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for the replica runs (torch.distributed when world > 1)."""
+
+    def __init__(self, world: int, local: int):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.dist, self.torch = dist, torch
+            self.dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.dist:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples (every 200 ms) while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict | None:
+        if not self.p:
+            return None
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "trace_closest_dram.txt")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch_full_frame:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def make_scene(args):
+    from pike_gb300 import synth
+    return synth.displaced_sphere_scene(subdivisions=args.subdivisions, width=args.width, height=args.height,
+                                        bounces=args.bounces)
+
+
+# ---------------------------------------------------------------- CPU (oracle)
+def cpu_run(src, bounces: int, seconds: float, threads: int):
+    """The CPU restatement on a bounded band of the frame: frames of a batch of
+    rows in the middle of the image (the reference's BATCH_SIZE/invocationOffset
+    mechanism, pike.js:133-147), repeated until `seconds` of rendering."""
+    from oracle import pyoracle
+    t0 = time.perf_counter()
+    pos, attrs = pyoracle.flatten(src)
+    idx, layers = pyoracle.materials(src.materials)
+    bvh = pyoracle.BVH(pos, src.tris)
+    bvh_s = time.perf_counter() - t0
+    env = pyoracle.Env(src.env_rgbe)
+    rows = max(1, src.height // 10)
+    batch = src.width * rows
+    r = pyoracle.Renderer(src.width, src.height, batch=batch, threads=threads)
+    r.set_scene(bvh, attrs, idx, layers)
+    r.set_env(env)
+    r.set_camera(src.camera_state(invocation_offset=(src.height // 2 - rows // 2) * src.width))
+    frames, rays, elapsed = 0, 0, 0.0
+    while elapsed < seconds or frames == 0:
+        r.reset_stats()
+        r.set_render_state(frames)
+        t = time.perf_counter()
+        r.tick(bounces)
+        elapsed += time.perf_counter() - t
+        s = r.stats()
+        rays += s["trace_rays"] + s["shadow_rays"]
+        frames += 1
+    return {"mrays": rays / elapsed / 1e6, "frames": frames, "rays": rays, "seconds": elapsed, "bvh_s": bvh_s,
+            "sample": f"{frames} frame(s) of a {src.width}x{rows}-pixel band ({batch} pixels, {bounces} bounces)"}
+
+
+def reference_arm(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    src = make_scene(args)
+    threads = os.cpu_count() or 1
+    per_step = max(args.cpu_seconds / max(args.steps, 1), 0.5)
+    for _ in range(args.warmup):
+        pass  # the CPU restatement has no warm-up state beyond the scene build
+    res = cpu_run(src, args.bounces, per_step * args.steps, threads)
+    value = res["mrays"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * res["seconds"] / res["frames"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
+                   "bounces": args.bounces, "bvh_build_s": res["bvh_s"],
+                   "note": "CPU restatement of the reference path (oracle); the reference is JavaScript+WGSL "
+                           "on WebGPU, which cannot run on this machine"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": res["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- GPU
+def setup_context(src, local: int):
+    import numpy as np
+    from pike_gb300 import _lib
+    from pike_gb300._lib import Context, ptr
+    from pike_gb300.passes import CameraPass  # noqa: F401  (API mirror; the bench drives the C ABI directly)
+    ctx = Context(local)
+    ctx.call("pk_configure", src.width, src.height, src.width * src.height)
+    tr = np.zeros(3)
+    ctx.call("pk_scene_flatten", ptr(src.pos), ptr(src.normal), ptr(src.tangent), ptr(src.uv), src.pos.shape[0],
+             ptr(src.tris), src.tris.shape[0], 1.0, ptr(tr))
+    ctx.call("pk_materials_set", ptr(src.materials), src.materials.shape[0])
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    ctx.call("pk_bvh_build", _lib.PK_BVH_SWEEP)
+    bvh_ms = ctx.timer_stop()
+    env = np.ascontiguousarray(src.env_rgbe)
+    ctx.call("pk_env_build", ptr(env), env.shape[1], env.shape[0])
+    return ctx, bvh_ms
+
+
+def camera_struct(src):
+    from pike_gb300._lib import CameraState
+    st = src.camera_state()
+    cs = CameraState()
+    cs.pos[:] = st["pos"]
+    cs.dir[:] = st["dir"]
+    cs.fov, cs.focal_depth, cs.aperture_size = st["fov"], st["focalDepth"], st["apertureSize"]
+    cs.distortion, cs.bokeh, cs.invocation_offset = st["distortion"], st["bokeh"], 0
+    return cs
+
+
+def read_stats(ctx):
+    import numpy as np
+    from pike_gb300._lib import ptr
+    s = np.zeros(10, np.uint64)
+    ctx.call("pk_read_stats", ptr(s))
+    keys = ["closest_fetch", "closest_tests", "shadow_fetch", "shadow_tests", "closest_rays", "shadow_rays",
+            "closest_hits", "shadow_hits", "rays_traced", "frames"]
+    return {k: int(v) for k, v in zip(keys, s)}
+
+
+def read_timing(ctx):
+    import numpy as np
+    from pike_gb300._lib import ptr
+    t = np.zeros(16, np.float32)
+    ctx.call("pk_read_timing", ptr(t))
+    kinds = ["camera", "trace", "compact", "shade", "shadow", "accumulate", "postprocess", "other"]
+    return {k: {"ms": float(t[i]), "launches": int(t[8 + i])} for i, k in enumerate(kinds)}
+
+
+def gpu_arm(args):
+    import ctypes as C
+
+    rank, world, local = dist_env()
+    D = Dist(world, local)
+    src = make_scene(args)
+    ctx, bvh_ms = setup_context(src, local)
+    cam = camera_struct(src)
+    ctx.call("pk_set_camera", cam)
+    B = args.bounces
+    first_sample = rank  # replicas render interleaved samples r, r+N, ...
+
+    # warm-up
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", max(args.warmup, 0), B)
+    ctx.call("pk_sync")
+
+    # counting frame: the reference algorithm's node fetches / triangle tests (not timed)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_counting", 1)
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", 1, B)
+    ctx.call("pk_sync")
+    counts = read_stats(ctx)
+    ctx.call("pk_set_counting", 0)
+
+    # per-kernel CUDA-event timing (instrumented frames, not the headline)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_timing", 1)
+    tf = 4
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", tf, B)
+    ctx.call("pk_sync")
+    kt = read_timing(ctx)
+    ctx.call("pk_set_timing", 0)
+
+    # timed region (device time, CUDA events on the library's stream)
+    clocks = Clocks(local)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    D.barrier()
+    ctx.call("pk_sync")
+    clocks.start()
+    ctx.timer_start()
+    ctx.call("pk_render_frames", args.steps, B)
+    ms = ctx.timer_stop()
+    clk = clocks.stop()
+    st = read_stats(ctx)
+    rays_local = st["rays_traced"]
+    D.barrier()
+    ms_max = D.max(ms)
+    rays_total = D.sum(float(rays_local))
+    value = rays_total / (ms_max / 1000.0) / 1e6
+    npix = src.width * src.height
+    spp_mpix = world * args.steps * npix / (ms_max / 1000.0) / 1e6
+
+    # end to end through the C ABI with host buffers
+    e2e_steps = args.steps
+    img = ctx.pinned((src.height, src.width, 4), "uint8")
+    h2d = C.sizeof(cam) + 8
+    ctx.call("pk_reset_stats")
+    D.barrier()
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    for s in range(e2e_steps):
+        ctx.call("pk_set_render_state", first_sample + s, 0.0)
+        ctx.call("pk_set_camera", cam)
+        ctx.call("pk_render_frame", B)
+        ctx.call("pk_read_display_async", img.array.ctypes.data_as(C.c_void_p))
+    e2e_ms = ctx.timer_stop()
+    e2e_rays = read_stats(ctx)["rays_traced"]
+    e2e_ms_max = D.max(e2e_ms)
+    e2e_value = D.sum(float(e2e_rays)) / (e2e_ms_max / 1000.0) / 1e6
+    img.free()
+    ctx.call("pk_sync")
+
+    if rank == 0:
+        peak, peak_kind = load_peak_hbm()
+        tr = kt["trace"]
+        trace_ms = tr["ms"] / max(tr["launches"], 1)
+        R, H = counts["closest_rays"], counts["closest_hits"]
+        alg_bytes_frame = (20 * counts["closest_fetch"] + 52 * counts["closest_tests"] + 48 * R + 64 * H
+                           + 48 * (R - H))
+        alg_bytes_launch = alg_bytes_frame / B
+        achieved = alg_bytes_launch / (trace_ms / 1000.0) / 1e9
+        traffic = profiled_traffic()
+        total_ms = sum(v["ms"] for v in kt.values())
+        launches_per_frame = 4 * B + 4
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
+                       "bounces": B, "env": "2048x1024 RGBE8", "spp_mpix_per_s": spp_mpix,
+                       "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
+                       "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}",
+                       "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
+                       "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},
+            "roofline": {"bound": "hbm", "kernel": "k_trace<closest, fused miss>", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes_launch,
+                         "launch_ms": trace_ms,
+                         "bytes_model": "20*node_fetch + 52*tri_test + 48*ray + 64*hit + 48*miss"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": src.width * src.height * 4, "steps": e2e_steps},
+            "gpu_launches": launches_per_frame * args.steps,
+            "clocks": clk,
+            "counts_per_frame": counts,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            res = cpu_run(src, B, args.cpu_seconds, os.cpu_count() or 1)
+            line["cpu_baseline"] = {"value": res["mrays"], "unit": UNIT, "cores": os.cpu_count() or 1,
+                                    "kind": "port", "sample": res["sample"], "bvh_build_s": res["bvh_s"]}
+        print(json.dumps(line))
+    ctx.close()
+    D.close()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -176,18 +176,30 @@ int pk_write_accum(pk_ctx* ctx, const float* in);
 int pk_read_display(pk_ctx* ctx, float* out, uint8_t* out8);
 
 /* ---- measurement --------------------------------------------------------
- * counting != 0 selects traversal kernels that also count node fetches and
- * triangle tests; pk_read_stats: closest {fetch, tests}, shadow {fetch, tests},
- * rays traced, frames. */
+ * counting != 0 selects traversal kernels that also count, per ray kind, the
+ * node fetches and triangle tests of the reference algorithm (trace.wgsl:
+ * the current node plus both children per inner step, one per leaf).
+ * pk_read_stats: closest {fetch, tests}, shadow {fetch, tests}, rays
+ * {closest, shadow}, hits {closest, occluded shadow} (counting kernels only),
+ * then rays traced by all kernels and frames rendered. */
 int pk_set_counting(pk_ctx* ctx, int counting);
 int pk_reset_stats(pk_ctx* ctx);
-int pk_read_stats(pk_ctx* ctx, uint64_t out6[6]);
+int pk_read_stats(pk_ctx* ctx, uint64_t out10[10]);
 /* timing != 0 records CUDA events around every kernel of pk_render_frame on the
  * context's stream; pk_read_timing returns summed milliseconds and launch
  * counts per kernel kind: camera, trace, compact, shade, shadow, accumulate,
  * postprocess, other (16 floats: 8 times then 8 counts). */
 int pk_set_timing(pk_ctx* ctx, int timing);
 int pk_read_timing(pk_ctx* ctx, float out16[16]);
+/* CUDA events on the context's stream: op 0 records the start event, op 1
+ * records the stop event, waits for it and returns the elapsed milliseconds. */
+int pk_stream_timer(pk_ctx* ctx, int op, float* ms);
+/* Page-locked host memory for the asynchronous readback below. */
+int pk_host_alloc(pk_ctx* ctx, size_t bytes, void** out);
+int pk_host_free(pk_ctx* ctx, void* p);
+/* Enqueue a copy of the W*H*4-byte display image into host memory (pinned for
+ * the copy to overlap); completes at the next pk_sync or stop timer. */
+int pk_read_display_async(pk_ctx* ctx, uint8_t* out8);
 /* Elementwise evaluation of the library's built-in definitions on the GPU
  * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */
 int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);

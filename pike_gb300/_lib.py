@@ -75,6 +75,8 @@ def load(path: str = LIB_PATH):
         "pk_read_display": [_P, _P, _P], "pk_set_counting": [_P, C.c_int], "pk_reset_stats": [_P],
         "pk_read_stats": [_P, _P], "pk_set_timing": [_P, C.c_int], "pk_read_timing": [_P, _P],
         "pk_math_eval": [_P, C.c_int, _P, _P, _P, u32],
+        "pk_stream_timer": [_P, C.c_int, C.POINTER(C.c_float)], "pk_host_alloc": [_P, C.c_size_t, C.POINTER(_P)],
+        "pk_host_free": [_P, _P], "pk_read_display_async": [_P, _P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -118,5 +120,35 @@ class Context:
             raise PikeError(rc, f"{name}: {self.L.pk_last_error(self.h).decode(errors='replace')}")
         return rc
 
+    def timer_start(self):
+        self.call("pk_stream_timer", 0, None)
+
+    def timer_stop(self) -> float:
+        ms = C.c_float(0.0)
+        self.call("pk_stream_timer", 1, C.byref(ms))
+        return float(ms.value)
+
+    def pinned(self, shape, dtype) -> "PinnedArray":
+        return PinnedArray(self, shape, dtype)
+
     def last_error(self) -> str:
         return self.L.pk_last_error(self.h).decode(errors="replace")
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory owned by the library."""
+
+    def __init__(self, ctx: Context, shape, dtype):
+        self.ctx = ctx
+        dt = np.dtype(dtype)
+        n = int(np.prod(shape)) * dt.itemsize
+        p = _P()
+        ctx.call("pk_host_alloc", n, C.byref(p))
+        self.p = p
+        buf = (C.c_uint8 * n).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def free(self):
+        if self.p is not None and getattr(self.ctx, "h", None):
+            self.ctx.call("pk_host_free", self.p)
+        self.p = None

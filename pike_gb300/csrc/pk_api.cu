@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <exception>
@@ -80,6 +81,7 @@ struct pk_ctx {
   bool timing = false;
   std::vector<EventPair> events;
   std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
   float kind_ms[N_KINDS] = {0};
   float kind_n[N_KINDS] = {0};
   unsigned long long frames = 0;
@@ -97,7 +99,8 @@ struct pk_ctx {
     L.stream = stream;
     L.ctr = ctr.p;
     L.cam = cam.p;
-    L.scene = SceneDev{inner.p, tris.p, tri4_leaf.p, attrs.p, mat4.p, layers.p, (int)n_layers, root};
+    L.scene = SceneDev{inner.p, tris.p, tri4_leaf.p, attrs.p, mat4.p, layers.p, (int)n_layers, root,
+                       n_leaf_tris, n_verts, n_mats};
     L.env = EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
     L.color = color.p;
     L.accum = accum.p;
@@ -180,6 +183,7 @@ void require_render(pk_ctx* c) {
   if (!c->bvh_ready) throw std::runtime_error("no BVH: call pk_bvh_build or pk_bvh_upload");
   if (!c->n_mats || !c->n_layers) throw std::runtime_error("no materials: call pk_materials_set/upload");
   if (!c->attrs.p) throw std::runtime_error("no scene attributes: call pk_scene_flatten/upload");
+  if (c->bvh_verts > c->n_verts) throw std::runtime_error("BVH vertices exceed the scene's vertex attributes");
   if (!c->cam_set) throw std::runtime_error("no camera: call pk_set_camera");
 }
 
@@ -221,6 +225,8 @@ int pk_destroy(pk_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto e : c->event_pool) cudaEventDestroy(e);
+  if (c->t0) cudaEventDestroy(c->t0);
+  if (c->t1) cudaEventDestroy(c->t1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PK_OK;
@@ -261,6 +267,9 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
     check(cudaMemsetAsync(c->display8.p, 0, c->display8.bytes(), c->stream), "memset");
     check(cudaMemsetAsync(c->hflags.p, 0, c->hflags.bytes(), c->stream), "memset");
     check(cudaMemsetAsync(c->sflags.p, 0, c->sflags.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->hit_list.p, 0, c->hit_list.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(c->hrec.p, 0, c->hrec.bytes(), c->stream), "memset");
+    check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 16, c->stream), "memset");
     check(cudaStreamSynchronize(c->stream), "sync");
     c->cur = 0;
     return PK_OK;
@@ -819,7 +828,7 @@ int pk_read_display(pk_ctx* c, float* out, uint8_t* out8) {
 int pk_set_counting(pk_ctx* c, int on) { return guarded(c, [&]() { c->counting = on != 0; return PK_OK; }); }
 int pk_reset_stats(pk_ctx* c) {
   return guarded(c, [&]() {
-    check(cudaMemsetAsync(&c->ctr.p->rays_traced, 0, 8 * 8, c->stream), "memset");
+    check(cudaMemsetAsync(&c->ctr.p->rays_traced, 0, sizeof(Counters) - offsetof(Counters, rays_traced), c->stream), "memset");
     check(cudaStreamSynchronize(c->stream), "sync");
     c->collect_events();
     for (int k = 0; k < N_KINDS; k++) { c->kind_ms[k] = 0; c->kind_n[k] = 0; }
@@ -827,14 +836,15 @@ int pk_reset_stats(pk_ctx* c) {
     return PK_OK;
   });
 }
-int pk_read_stats(pk_ctx* c, uint64_t out6[6]) {
+int pk_read_stats(pk_ctx* c, uint64_t out10[10]) {
   return guarded(c, [&]() {
-    if (!out6) return fail(c, PK_ERR_ARG, "null output");
+    if (!out10) return fail(c, PK_ERR_ARG, "null output");
     Counters h;
     check(cudaStreamSynchronize(c->stream), "sync");
     check(cudaMemcpy(&h, c->ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
-    out6[0] = h.stat[0]; out6[1] = h.stat[1]; out6[2] = h.stat[2]; out6[3] = h.stat[3];
-    out6[4] = h.rays_traced; out6[5] = c->frames;
+    for (int i = 0; i < 8; i++) out10[i] = h.stat[i];
+    out10[8] = h.rays_traced;
+    out10[9] = c->frames;
     return PK_OK;
   });
 }
@@ -845,6 +855,46 @@ int pk_read_timing(pk_ctx* c, float out16[16]) {
     check(cudaStreamSynchronize(c->stream), "sync");
     c->collect_events();
     for (int k = 0; k < N_KINDS; k++) { out16[k] = c->kind_ms[k]; out16[8 + k] = c->kind_n[k]; }
+    return PK_OK;
+  });
+}
+
+int pk_stream_timer(pk_ctx* c, int op, float* ms) {
+  return guarded(c, [&]() {
+    if (!c->t0) check(cudaEventCreate(&c->t0), "cudaEventCreate");
+    if (!c->t1) check(cudaEventCreate(&c->t1), "cudaEventCreate");
+    if (op == 0) {
+      check(cudaEventRecord(c->t0, c->stream), "cudaEventRecord");
+      return PK_OK;
+    }
+    if (op != 1 || !ms) return fail(c, PK_ERR_ARG, "pk_stream_timer: op must be 0 or 1 with an output");
+    check(cudaEventRecord(c->t1, c->stream), "cudaEventRecord");
+    check(cudaEventSynchronize(c->t1), "cudaEventSynchronize");
+    check(cudaEventElapsedTime(ms, c->t0, c->t1), "cudaEventElapsedTime");
+    return PK_OK;
+  });
+}
+
+int pk_host_alloc(pk_ctx* c, size_t bytes, void** out) {
+  return guarded(c, [&]() {
+    if (!out) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault), "cudaHostAlloc");
+    return PK_OK;
+  });
+}
+
+int pk_host_free(pk_ctx* c, void* p) {
+  return guarded(c, [&]() {
+    if (p) check(cudaFreeHost(p), "cudaFreeHost");
+    return PK_OK;
+  });
+}
+
+int pk_read_display_async(pk_ctx* c, uint8_t* out8) {
+  return guarded(c, [&]() {
+    require_config(c);
+    if (!out8) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaMemcpyAsync(out8, c->display8.p, c->display8.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
     return PK_OK;
   });
 }

@@ -29,7 +29,9 @@ struct Counters {
   uint32_t work[8];
   unsigned long long rays_traced;   // closest-hit + shadow rays, all frames since reset
   unsigned long long trace_launch_rays;
-  unsigned long long stat[6];       // optional traversal counters (fetch, tests) per kind
+  // traversal counters of the counting kernels: closest {fetch, tests}, shadow
+  // {fetch, tests}, rays {closest, shadow}, hits {closest, occluded shadow}
+  unsigned long long stat[8];
 };
 
 // CameraStateStuct (structs.js:235-249): eye ray, dimsMask = W<<16|H, lens params.
@@ -64,6 +66,9 @@ struct SceneDev {
   const uchar4* layers;    // 1x1 rgba8 atlas layers
   int n_layers;
   int root;                // child code of the root
+  uint32_t n_tris;         // leaf-ordered triangles
+  uint32_t n_verts;        // vertex attributes
+  uint32_t n_mats;         // material index entries
 };
 
 struct EnvDev {

@@ -194,7 +194,11 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
   const uint32_t n = *countp;
   const int lane = threadIdx.x & 31;
   const float theta = ctr->env_theta;
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays_traced, (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&ctr->rays_traced, (unsigned long long)n);
+    if (COUNT) atomicAdd(&ctr->stat[ANY ? 5 : 4], (unsigned long long)n);
+  }
+  uint32_t nhit = 0;
   uint32_t nfetch = 0, ntest = 0;
   for (;;) {
     uint32_t base = 0;
@@ -220,10 +224,12 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
     }
     const uint32_t m = __ballot_sync(0xffffffffu, hit);
     if (lane == 0) flags[base >> 5] = m;
+    if (COUNT && lane == 0) nhit += (uint32_t)__popc(m);
   }
   if (COUNT) {
     atomicAdd(&ctr->stat[ANY ? 2 : 0], (unsigned long long)nfetch);
     atomicAdd(&ctr->stat[ANY ? 3 : 1], (unsigned long long)ntest);
+    if (lane == 0) atomicAdd(&ctr->stat[ANY ? 7 : 6], (unsigned long long)nhit);
   }
 }
 
@@ -344,7 +350,9 @@ __device__ __forceinline__ void onb(V3 n, V3& b1, V3& b2) {
 // getSurfaceInteraction (:179-200) + interpolateVertexAttribute (:363-394)
 __device__ __forceinline__ SI surface(const SceneDev& sc, V3 ro, V3 rd, float t, int index, uint32_t bary_mask) {
   SI si;
-  const int4 tri = __ldg(sc.tri4 + index);
+  int4 tri = __ldg(sc.tri4 + index);
+  if ((uint32_t)tri.x >= sc.n_verts || (uint32_t)tri.y >= sc.n_verts || (uint32_t)tri.z >= sc.n_verts) tri.x = tri.y = tri.z = 0;
+  if ((uint32_t)tri.w >= sc.n_mats) tri.w = 0;
   const float u = unorm16(bary_mask & 0xffffu), v = unorm16(bary_mask >> 16);
   const V3 bary = v3(1.0f - u - v, u, v);
   const uint4 a0 = __ldg(sc.attrs + tri.x), a1 = __ldg(sc.attrs + tri.y), a2 = __ldg(sc.attrs + tri.z);
@@ -494,9 +502,15 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_shade(SceneDev sc, EnvDev env
     const uint32_t r = tile * SHADE_THREADS + threadIdx.x;
     bool eb = false, es = false;
     float4 bo, bd, bt, so, sd, st;
-    if (r < nh) {
-      const uint32_t j = hit_list[r];
-      const uint4 hr = hrec[j];
+    uint32_t j = 0;
+    uint4 hr = make_uint4(0u, 0u, 0u, 0u);
+    bool valid = r < nh;
+    if (valid) {
+      j = hit_list[r];
+      if (j < capacity) hr = hrec[j];
+      if (j >= capacity || hr.y >= sc.n_tris) { atomicOr(&ctr->err, ERR_QUEUE); valid = false; }
+    }
+    if (valid) {
       const float4 o4 = Rin.o[j], d4 = Rin.d[j], t4 = Rin.t[j];
       const V3 ro = v3(o4.x, o4.y, o4.z), rd = v3(d4.x, d4.y, d4.z);
       const float ht = __uint_as_float(hr.x);

@@ -85,25 +85,40 @@ __device__ __forceinline__ void decode_box(const int32_t* nd, float* b6) {
     b6[2 * a + 1] = snorm16((int)(int16_t)(uint16_t)(m[a] >> 16));      // x_range.y (quantised min)
   }
 }
+// Leaf words must address triangles inside the leaf-ordered array.
 __device__ __forceinline__ int child_code(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ rank,
-                                          uint32_t i, uint32_t* err) {
+                                          uint32_t i, uint32_t n_tris, uint32_t* err) {
   const int32_t tri = nodes5[5 * (size_t)i + 1];
   if (tri > -1) {
-    if ((tri >> 24) >= 128) atomicOr(err, ERR_BVH);
+    const uint32_t size = (uint32_t)tri >> 24, base = (uint32_t)tri & 0x00ffffffu;
+    if (size >= 128u || base + size > n_tris) {
+      atomicOr(err, ERR_BVH);
+      return (int)0x80000000u;  // an empty leaf
+    }
     return (int)(0x80000000u | (uint32_t)tri);
   }
   return (int)rank[i];
 }
 
+// Children must come after their parent in BFS order (serializeTree), which
+// also rules out cycles: every traversal step moves to a larger node index.
 __global__ void k_inner_records(const int32_t* __restrict__ nodes5, uint32_t n, const uint32_t* __restrict__ rank,
-                                float4* __restrict__ inner, int* __restrict__ root_code, uint32_t* err) {
+                                uint32_t n_tris, float4* __restrict__ inner, int* __restrict__ root_code,
+                                uint32_t* err) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int32_t* nd = nodes5 + 5 * (size_t)i;
-  if (i == 0) *root_code = child_code(nodes5, rank, 0, err);
+  if (i == 0) *root_code = child_code(nodes5, rank, 0, n_tris, err);
   if (nd[1] > -1) return;
   const int32_t l = nd[0];
-  if (l < 1 || (uint32_t)l + 1 >= n) { atomicOr(err, ERR_BVH); return; }
+  if (l < 1 || (uint32_t)l <= i || (uint32_t)l + 1 >= n) {
+    atomicOr(err, ERR_BVH);
+    float4* r = inner + 4 * (size_t)rank[i];
+    const float4 none = make_float4(0.f, 0.f, 0.f, 0.f);
+    r[0] = none; r[1] = none; r[2] = none;
+    reinterpret_cast<int4*>(r)[3] = make_int4((int)0x80000000u, (int)0x80000000u, 0, 0);
+    return;
+  }
   float lb[6], rb[6];
   decode_box(nodes5 + 5 * (size_t)l, lb);
   decode_box(nodes5 + 5 * (size_t)(l + 1), rb);
@@ -111,8 +126,8 @@ __global__ void k_inner_records(const int32_t* __restrict__ nodes5, uint32_t n, 
   r[0] = make_float4(lb[0], lb[1], lb[2], lb[3]);
   r[1] = make_float4(lb[4], lb[5], rb[0], rb[1]);
   r[2] = make_float4(rb[2], rb[3], rb[4], rb[5]);
-  reinterpret_cast<int4*>(r)[3] = make_int4(child_code(nodes5, rank, (uint32_t)l, err),
-                                            child_code(nodes5, rank, (uint32_t)l + 1, err), 0, 0);
+  reinterpret_cast<int4*>(r)[3] = make_int4(child_code(nodes5, rank, (uint32_t)l, n_tris, err),
+                                            child_code(nodes5, rank, (uint32_t)l + 1, n_tris, err), 0, 0);
 }
 
 __global__ void k_tri_edges(const int4* __restrict__ tri4, uint32_t n, const float4* __restrict__ verts4,
@@ -142,7 +157,7 @@ int convert_bvh(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const i
   DevBuf<uint32_t> flag(n_nodes), rank(n_nodes);
   k_inner_flags<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, flag.p);
   scan_exclusive_u32(s, flag.p, rank.p, n_nodes, nullptr);
-  k_inner_records<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, rank.p, inner, root_code, err);
+  k_inner_records<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, rank.p, n_tris, inner, root_code, err);
   if (n_tris) k_tri_edges<<<(n_tris + 255) / 256, 256, 0, s>>>(tri4, n_tris, verts4, n_verts, tris, err);
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : 1;
 }

@@ -129,3 +129,24 @@ def test_malformed_bvh_upload_rejected(oracle, pk_built):
     with pytest.raises(_lib.PikeError):
         pair.ctx.call("pk_bvh_upload", ptr(nodes), nodes.shape[0], ptr(b.tris), b.tris.shape[0], ptr(b.verts),
                       b.verts.shape[0])
+
+
+def test_counting_kernels_match_oracle_counts(oracle, pk_built):
+    """The counting traversal variants report the reference algorithm's node
+    fetches and triangle tests; they must equal the oracle's counts."""
+    src = synth.displaced_sphere_scene(subdivisions=5, width=96, height=64, env_size=(256, 128))
+    pair = Pair(src, oracle)
+    c = pair.ctx
+    c.call("pk_reset_stats")
+    c.call("pk_set_counting", 1)
+    fused_frames(pair, 1, 6)
+    c.call("pk_set_counting", 0)
+    s = np.zeros(10, np.uint64)
+    c.call("pk_read_stats", ptr(s))
+    P = pair.P.r
+    P.reset_stats()
+    oracle_frames(pair, 1, 6)
+    o = P.stats()
+    assert int(s[4]) == o["trace_rays"] and int(s[5]) == o["shadow_rays"]
+    assert int(s[0]) == o["trace_fetch"] and int(s[1]) == o["trace_tests"]
+    assert int(s[2]) == o["shadow_fetch"] and int(s[3]) == o["shadow_tests"]

@@ -84,7 +84,8 @@ def test_passes_env_rotation_and_lens(oracle, pk_built):
     P = pair.P.r
     for f in range(2):
         pair.set_render_state(f, 0.3)
-        pair.ctx.call("pk_clear_color")
+        for name in ("clear_color", "clear_hits_misses", "clear_rays"):
+            pair.ctx.call("pk_" + name)
         P.begin_frame()
         for name in ("camera", "trace", "shade_hit", "trace_shadow", "shade_miss", "trace", "shade_hit",
                      "trace_shadow", "shade_miss", "accumulate"):
