@@ -156,6 +156,18 @@ int pk_postprocess(pk_ctx* ctx);   /* PostProcessPass: ACES + saturation + sRGB 
 int pk_render_frame(pk_ctx* ctx, uint32_t bounces);
 int pk_render_frames(pk_ctx* ctx, uint32_t frames, uint32_t bounces);
 
+/* ---- ray queries -------------------------------------------------------
+ * Trace n rays held in caller-owned DEVICE buffers against the context's BVH:
+ * the GPU form of the reference's autofocus Raycaster (render/raycaster.js:
+ * 114-131, pike.js:88-90), with trace.wgsl closest-hit (any_hit = 0) or
+ * trace_shadow.wgsl any-hit (any_hit = 1) semantics.  ray_o4 / ray_d4: n
+ * float4 each (xyz used, normalised frame); hits4: n * {t bits, triangle index
+ * or 0xffffffff, bary_mask, 0}; hit_index: the indices of the rays that hit,
+ * increasing; n_hits: one u32 (device).  Runs on the context's stream and
+ * returns when the results are written. */
+int pk_cast_rays(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit, uint32_t* hits4,
+                 uint32_t* hit_index, uint32_t* n_hits);
+
 /* ---- readback ---------------------------------------------------------- */
 int pk_sync(pk_ctx* ctx);
 /* samples, num_hits, num_misses, num_rays, num_shadow, device error bits,

@@ -12,142 +12,13 @@
 
 #include "../../include/pike.h"
 #include "pk_bvh.h"
+#include "pk_ctx.h"
 #include "pk_host_tables.h"
 #include "pk_internal.cuh"
 #include "pk_render.h"
 #include "pk_util.h"
 
 using namespace pk;
-
-namespace {
-
-constexpr uint32_t MAX_BOUNCES = 16;
-constexpr int N_KINDS = 8;
-enum Kind { K_CAMERA = 0, K_TRACE, K_COMPACT, K_SHADE, K_SHADOW, K_ACCUM, K_POST, K_OTHER };
-
-struct EventPair {
-  int kind;
-  cudaEvent_t a, b;
-};
-
-}  // namespace
-
-struct pk_ctx {
-  int device = 0;
-  int sms = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // configuration
-  uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;
-  uint32_t ct = 0, st = 0;  // look-back tiles per compaction / shade launch
-  unsigned g_trace = 1, g_compact = 1, g_shade = 1;  // persistent grid sizes
-  // render state
-  DevBuf<Counters> ctr;
-  DevBuf<CamState> cam;
-  bool cam_set = false;
-  float exposure = 1.0f, saturation = 1.0f;
-  DevBuf<float4> color, accum, display;
-  DevBuf<uchar4> display8;
-  DevBuf<float4> rq[2][3], sq[3], mq[3];
-  int cur = 0;
-  DevBuf<uint4> hrec;
-  DevBuf<uint32_t> hflags, sflags, hit_list;
-  DevBuf<uint32_t> tickets;              // 4 per bounce slot
-  DevBuf<unsigned long long> tiles;      // per bounce slot: ct (compact) + st (shade) + ct (shadow compact)
-  // scene
-  uint32_t n_verts = 0, n_tris = 0;
-  DevBuf<double> pos;
-  DevBuf<uint4> attrs;
-  DevBuf<int4> tri4;
-  uint32_t n_mats = 0, n_layers = 0;
-  DevBuf<int4> mat4;
-  DevBuf<uchar4> layers;
-  // bvh
-  uint32_t n_nodes = 0, n_leaf_tris = 0, n_inner = 0, bvh_verts = 0;
-  double norm[4] = {0, 0, 0, 0};
-  DevBuf<int32_t> nodes5;
-  DevBuf<int4> tri4_leaf;
-  DevBuf<float4> verts4, inner, tris;
-  int root = 0;
-  bool bvh_ready = false;
-  // env
-  uint32_t env_w = 0, env_h = 0, env_nb = 0;
-  DevBuf<uchar4> rgbe;
-  DevBuf<int2> bins, coords;
-  DevBuf<float> pdf;
-  bool env_ready = false;
-  // measurement
-  bool counting = false;
-  bool timing = false;
-  std::vector<EventPair> events;
-  std::vector<cudaEvent_t> event_pool;
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
-  float kind_ms[N_KINDS] = {0};
-  float kind_n[N_KINDS] = {0};
-  unsigned long long frames = 0;
-
-  RayQ R(int i) { return RayQ{rq[i][0].p, rq[i][1].p, rq[i][2].p}; }
-  RayQ S() { return RayQ{sq[0].p, sq[1].p, sq[2].p}; }
-  RayQ M() { return RayQ{mq[0].p, mq[1].p, mq[2].p}; }
-  uint32_t* ticket(uint32_t slot, int k) { return tickets.p + 4 * slot + k; }
-  unsigned long long* tiles_compact(uint32_t slot) { return tiles.p + (size_t)slot * (2 * ct + st); }
-  unsigned long long* tiles_shade(uint32_t slot) { return tiles_compact(slot) + ct; }
-  unsigned long long* tiles_shadow(uint32_t slot) { return tiles_compact(slot) + ct + st; }
-
-  LaunchCtx launch() {
-    LaunchCtx L;
-    L.stream = stream;
-    L.ctr = ctr.p;
-    L.cam = cam.p;
-    L.scene = SceneDev{inner.p, tris.p, tri4_leaf.p, attrs.p, mat4.p, layers.p, (int)n_layers, root,
-                       n_leaf_tris, n_verts, n_mats};
-    L.env = EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
-    L.color = color.p;
-    L.accum = accum.p;
-    L.display = display.p;
-    L.display8 = display8.p;
-    L.npix = npix;
-    L.capacity = cap;
-    L.miss_capacity = 2 * cap;
-    L.trace_blocks = g_trace;
-    L.compact_blocks = g_compact;
-    L.shade_blocks = g_shade;
-    return L;
-  }
-  cudaEvent_t take_event() {
-    if (!event_pool.empty()) {
-      cudaEvent_t e = event_pool.back();
-      event_pool.pop_back();
-      return e;
-    }
-    cudaEvent_t e;
-    check(cudaEventCreate(&e), "cudaEventCreate");
-    return e;
-  }
-  template <class F>
-  void timed(int kind, F fn) {
-    if (!timing) {
-      fn();
-      return;
-    }
-    EventPair p{kind, take_event(), take_event()};
-    check(cudaEventRecord(p.a, stream), "cudaEventRecord");
-    fn();
-    check(cudaEventRecord(p.b, stream), "cudaEventRecord");
-    events.push_back(p);
-  }
-  void collect_events() {
-    for (EventPair& p : events) {
-      float ms = 0;
-      check(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
-      kind_ms[p.kind] += ms;
-      kind_n[p.kind] += 1;
-      event_pool.push_back(p.a);
-      event_pool.push_back(p.b);
-    }
-    events.clear();
-  }
-};
 
 namespace {
 

@@ -1,0 +1,153 @@
+// pk_cast.cu -- ray queries against the context's BVH on caller-owned device
+// buffers: the GPU counterpart of the reference's CPU Raycaster used for
+// autofocus (render/raycaster.js:114-131), with the closest-hit and any-hit
+// semantics of trace.wgsl / trace_shadow.wgsl.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "../../include/pike.h"
+#include "pk_ctx.h"
+#include "pk_internal.cuh"
+#include "pk_traverse.cuh"
+#include "pk_util.h"
+
+namespace pk {
+namespace {
+
+constexpr int CAST_THREADS = TRACE_THREADS;
+constexpr int LIST_THREADS = 256;
+
+// Every ray gets a record {t bits, triangle index or 0xffffffff, bary_mask, 0};
+// bit j of flags is set when ray j hit.
+template <bool ANY>
+__global__ void __launch_bounds__(CAST_THREADS) k_cast(SceneDev sc, const float4* __restrict__ o4,
+                                                        const float4* __restrict__ d4, uint32_t n,
+                                                        uint4* __restrict__ hits4, uint32_t* __restrict__ flags,
+                                                        uint32_t* __restrict__ ticket, uint32_t* __restrict__ err) {
+  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+  const int lane = threadIdx.x & 31;
+  uint32_t nf = 0, nt = 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(ticket, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const uint32_t j = base + lane;
+    bool hit = false;
+    if (j < n) {
+      const float4 o = o4[j], d = d4[j];
+      float bt;
+      int bi;
+      uint32_t bb;
+      traverse<ANY, false>(sc, o.x, o.y, o.z, d.x, d.y, d.z, bt, bi, bb, sstack, err, nf, nt);
+      hit = bi != -1;
+      hits4[j] = make_uint4(__float_as_uint(bt), (uint32_t)bi, bb, 0u);
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0) flags[base >> 5] = m;
+  }
+}
+
+// Stable list of the rays that hit (increasing ray index) and its length.
+__global__ void __launch_bounds__(LIST_THREADS) k_hit_list(const uint32_t* __restrict__ flags, uint32_t n,
+                                                            uint32_t* __restrict__ list, uint32_t* __restrict__ count,
+                                                            uint32_t* __restrict__ ticket,
+                                                            unsigned long long* __restrict__ tiles,
+                                                            uint32_t* __restrict__ err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[LIST_THREADS / 32 + 1][2];
+  __shared__ unsigned long long s_excl;
+  const uint32_t nwords = (n + 31) >> 5;
+  const uint32_t ntiles = (nwords + LIST_THREADS - 1) / LIST_THREADS;
+  if (ntiles == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *count = 0;
+    return;
+  }
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t w = tile * LIST_THREADS + threadIdx.x;
+    uint32_t hm = 0u;
+    if (w < nwords) {
+      const uint32_t valid = (w == nwords - 1 && (n & 31u)) ? ((1u << (n & 31u)) - 1u) : 0xffffffffu;
+      hm = flags[w] & valid;
+    }
+    uint32_t ea, eb, ta, tb;
+    block_scan2<LIST_THREADS / 32>((uint32_t)__popc(hm), 0u, ea, eb, ta, tb, s_warp);
+    if (threadIdx.x == 0) s_excl = lookback2(tiles, tile, pack2(ta, 0u), err);
+    __syncthreads();
+    uint32_t k = unpack_a(s_excl) + ea;
+    uint32_t bits = hm;
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1u;
+      list[k++] = w * 32u + (uint32_t)b;
+    }
+    if (tile == ntiles - 1 && threadIdx.x == 0) *count = unpack_a(s_excl) + ta;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// Scratch words the two kernels need for n rays: two tickets, an error word,
+// the hit bitmask, and one look-back tile state per LIST_THREADS words.
+struct CastScratch {
+  uint32_t* tickets;  // [0] trace, [1] list, [2] error flags, [3] unused
+  uint32_t* flags;
+  unsigned long long* tiles;
+};
+size_t cast_flag_words(uint32_t n) { return ((size_t)n + 31) / 32; }
+size_t cast_tiles(uint32_t n) { return (cast_flag_words(n) + LIST_THREADS - 1) / LIST_THREADS; }
+
+// Enqueue the query on `stream`: zero what must start at zero, then trace and list.
+int cast_enqueue(pk_ctx* c, const float4* o4, const float4* d4, uint32_t n, int any_hit, uint4* hits4,
+                 uint32_t* hit_index, uint32_t* n_hits, const CastScratch& s, cudaStream_t stream) {
+  check(cudaMemsetAsync(s.tickets, 0, 16, stream), "memset");
+  if (cast_tiles(n)) check(cudaMemsetAsync(s.tiles, 0, cast_tiles(n) * 8, stream), "memset");
+  LaunchCtx L = c->launch();
+  const unsigned warps = (unsigned)((n + 31) / 32);
+  const unsigned grid = std::max(1u, std::min(L.trace_blocks, (warps + CAST_THREADS / 32 - 1) / (CAST_THREADS / 32)));
+  if (n) {
+    if (any_hit)
+      k_cast<true><<<grid, CAST_THREADS, 0, stream>>>(L.scene, o4, d4, n, hits4, s.flags, s.tickets, s.tickets + 2);
+    else
+      k_cast<false><<<grid, CAST_THREADS, 0, stream>>>(L.scene, o4, d4, n, hits4, s.flags, s.tickets, s.tickets + 2);
+  }
+  const unsigned lgrid = (unsigned)std::max<size_t>(1, std::min<size_t>(cast_tiles(n), (size_t)c->sms * 4));
+  k_hit_list<<<lgrid, LIST_THREADS, 0, stream>>>(s.flags, n, hit_index, n_hits, s.tickets + 1, s.tiles,
+                                                  s.tickets + 2);
+  check(cudaGetLastError(), "pk_cast_rays");
+  return PK_OK;
+}
+
+}  // namespace pk
+
+using namespace pk;
+
+extern "C" int pk_cast_rays(pk_ctx* c, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
+                            uint32_t* hits4, uint32_t* hit_index, uint32_t* n_hits) {
+  if (!c) return PK_ERR_ARG;
+  try {
+    check(cudaSetDevice(c->device), "cudaSetDevice");
+    if (!c->bvh_ready) { c->err = "pk_cast_rays: no BVH"; return PK_ERR_STATE; }
+    if ((n && (!ray_o4 || !ray_d4 || !hits4 || !hit_index)) || !n_hits) { c->err = "pk_cast_rays: null buffer"; return PK_ERR_ARG; }
+    if (n > (1u << 30)) { c->err = "pk_cast_rays: too many rays"; return PK_ERR_ARG; }
+    DevBuf<uint32_t> tickets(4), flags(std::max<size_t>(cast_flag_words(n), 1));
+    DevBuf<unsigned long long> tiles(std::max<size_t>(cast_tiles(n), 1));
+    const CastScratch s{tickets.p, flags.p, tiles.p};
+    cast_enqueue(c, reinterpret_cast<const float4*>(ray_o4), reinterpret_cast<const float4*>(ray_d4), n, any_hit,
+                 reinterpret_cast<uint4*>(hits4), hit_index, n_hits, s, c->stream);
+    uint32_t err = 0;
+    check(cudaMemcpyAsync(&err, tickets.p + 2, 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    if (err) { c->err = "pk_cast_rays: device error flags"; return PK_ERR_DEVICE; }
+    return PK_OK;
+  } catch (CudaError& e) {
+    c->err = e.what();
+    return PK_ERR_CUDA;
+  }
+}

@@ -1,0 +1,101 @@
+// pk_traverse.cuh -- binary-BVH traversal of trace.wgsl / trace_shadow.wgsl
+// on the traversal-format BVH (see SceneDev in pk_internal.cuh).
+#pragma once
+#include "pk_internal.cuh"
+
+namespace pk {
+
+constexpr float MAX_T = 100000.0f;
+
+// =====================================================================
+// trace.wgsl:83-189 / trace_shadow.wgsl:82-190: BVH traversal.
+// =====================================================================
+__device__ __forceinline__ float box_hit(float xa, float xb, float ya, float yb, float za, float zb, float ox,
+                                         float oy, float oz, float ix, float iy, float iz) {
+  // t1 uses the x_range.x bounds (quantised max), t2 the x_range.y bounds (min).
+  const float t1x = (xa - ox) * ix, t2x = (xb - ox) * ix;
+  const float t1y = (ya - oy) * iy, t2y = (yb - oy) * iy;
+  const float t1z = (za - oz) * iz, t2z = (zb - oz) * iz;
+  // fminf/fmaxf agree with minNum/maxNum except for the sign of a zero
+  // result, which only ever feeds comparisons here.
+  const float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
+  const float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
+  return (tmax >= tmin && tmax > 0.0f) ? tmin : MAX_T;
+}
+
+constexpr int TRACE_THREADS = 128;
+constexpr int STACK_SMEM = 32;   // per-thread entries kept in shared memory
+constexpr int STACK_LOCAL = 32;  // overflow entries in local memory (total depth 64)
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
+                                         float dz, float& best_t, int& best_i, uint32_t& best_b,
+                                         int (*sstack)[TRACE_THREADS], uint32_t* err, uint32_t& nfetch,
+                                         uint32_t& ntest) {
+  const float eps = ANY ? 1e-7f : 1e-8f;
+  const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
+  int lstack[STACK_LOCAL];
+  const int tid = threadIdx.x;
+  int sp = 0;
+  int cur = sc.root;
+  best_t = MAX_T;
+  best_i = -1;
+  best_b = 0u;
+  for (;;) {
+    if (cur >= 0) {
+      if (COUNT) nfetch += 3;
+      const float4* rec = sc.inner + 4 * (size_t)cur;
+      const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
+      const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
+      const float lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
+      const float rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+      const bool lok = lh < best_t, rok = rh < best_t;
+      if (lok && rok) {
+        int nearc, farc;
+        if (lh > rh) { nearc = ch.y; farc = ch.x; } else { nearc = ch.x; farc = ch.y; }
+        if (sp < STACK_SMEM) sstack[sp][tid] = farc;
+        else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+        else { atomicOr(err, ERR_STACK); break; }
+        ++sp;
+        cur = nearc;
+        continue;
+      }
+      if (lok) { cur = ch.x; continue; }
+      if (rok) { cur = ch.y; continue; }
+    } else {
+      if (COUNT) nfetch += 1;
+      const uint32_t word = (uint32_t)cur & 0x7fffffffu;
+      const int size = (int)(word >> 24);
+      const int base = (int)(word & 0x00ffffffu);
+      for (int i = 0; i < size; i++) {
+        if (COUNT) ntest += 1;
+        const float4* tp = sc.tris + 3 * (size_t)(base + i);
+        const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
+        const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
+        const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+        const float det = e1x * px + e1y * py + e1z * pz;
+        if (fabsf(det) < eps) continue;
+        const float inv_det = 1.0f / det;
+        const float tx = ox - A.x, ty = oy - A.y, tz = oz - A.z;
+        const float u = (tx * px + ty * py + tz * pz) * inv_det;
+        if (u < 0.0f || u > 1.0f) continue;
+        const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+        const float v = (dx * qx + dy * qy + dz * qz) * inv_det;
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
+        const float res = dist > eps ? dist : MAX_T;
+        if (res < best_t) {
+          best_t = res;
+          best_i = base + i;
+          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        }
+      }
+      if (ANY && best_i != -1) break;
+    }
+    if (sp == 0) break;
+    --sp;
+    cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+  }
+}
+
+}  // namespace pk
