@@ -167,6 +167,20 @@ int pk_render_frames(pk_ctx* ctx, uint32_t frames, uint32_t bounces);
  * returns when the results are written. */
 int pk_cast_rays(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit, uint32_t* hits4,
                  uint32_t* hit_index, uint32_t* n_hits);
+/* pk_cast_rays without any device allocation.  No counterpart in the reference.
+ * For callers that must not allocate device memory when they query: a host
+ * that handed its device memory budget to its own pool up front, or a
+ * latency-sensitive render thread, where cudaMalloc can fail and cudaFree
+ * waits for the whole device (stalling work queued by other threads).  It
+ * makes no cudaMalloc/cudaFree call: its scratch is a 132,352-byte static
+ * device array that every GPU loading the library keeps until the process
+ * exits.  Limit: at most 1,048,576 rays per call (more returns PK_ERR_ARG).
+ * The first call on a device looks up that array's address, so make it before
+ * any stream capture.  All calls share the array (each call re-zeroes what must
+ * start at zero): calls that overlap on the GPU race.  Same arguments and
+ * results as pk_cast_rays. */
+int pk_cast_rays_noalloc(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
+                         uint32_t* hits4, uint32_t* hit_index, uint32_t* n_hits);
 
 /* ---- readback ---------------------------------------------------------- */
 int pk_sync(pk_ctx* ctx);

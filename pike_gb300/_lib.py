@@ -78,6 +78,7 @@ def load(path: str = LIB_PATH):
         "pk_stream_timer": [_P, C.c_int, C.POINTER(C.c_float)], "pk_host_alloc": [_P, C.c_size_t, C.POINTER(_P)],
         "pk_host_free": [_P, _P], "pk_read_display_async": [_P, _P],
         "pk_cast_rays": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
+        "pk_cast_rays_noalloc": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/pike.h"
 #include "pk_ctx.h"
@@ -145,6 +146,75 @@ extern "C" int pk_cast_rays(pk_ctx* c, const float* ray_o4, const float* ray_d4,
     check(cudaMemcpyAsync(&err, tickets.p + 2, 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "sync");
     if (err) { c->err = "pk_cast_rays: device error flags"; return PK_ERR_DEVICE; }
+    return PK_OK;
+  } catch (CudaError& e) {
+    c->err = e.what();
+    return PK_ERR_CUDA;
+  }
+}
+
+// ---- allocation-free variant -------------------------------------------------
+// pk_cast_rays allocates its scratch (work tickets, the per-ray hit bitmask and
+// the look-back tile states of the hit list) with cudaMalloc on every call.
+// pk_cast_rays_noalloc takes it from the file-scope array below instead, so it
+// calls neither cudaMalloc nor cudaFree.  Every GPU that loads the library
+// holds one copy of the array until the process exits.
+namespace pk {
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_RAYS = 1u << 20;                      // rays per call
+constexpr size_t NOALLOC_FLAG_WORDS = NOALLOC_MAX_RAYS / 32;          // 32768 u32
+constexpr size_t NOALLOC_TILES = (NOALLOC_FLAG_WORDS + LIST_THREADS - 1) / LIST_THREADS;  // 128 u64
+constexpr size_t NOALLOC_FLAGS_OFF = 256;
+constexpr size_t NOALLOC_TILES_OFF = NOALLOC_FLAGS_OFF + NOALLOC_FLAG_WORDS * 4;
+constexpr size_t NOALLOC_BYTES = NOALLOC_TILES_OFF + NOALLOC_TILES * 8;  // 132,352 bytes
+
+static __device__ __align__(256) unsigned char g_cast_scratch[NOALLOC_BYTES];
+
+std::mutex g_scratch_mu;
+constexpr int MAX_DEVICES = 256;
+void* g_scratch_addr[MAX_DEVICES] = {};
+
+// The array's device address on the current device.  In host code the name
+// g_cast_scratch is only a host-side stand-in, so the address is looked up once
+// per device (with that device current) and cached.
+unsigned char* noalloc_scratch(int device) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (device < 0 || device >= MAX_DEVICES) throw CudaError("pk_cast_rays_noalloc: device id out of range");
+  if (!g_scratch_addr[device]) {
+    void* p = nullptr;
+    check(cudaGetSymbolAddress(&p, g_cast_scratch), "cudaGetSymbolAddress(g_cast_scratch)");
+    g_scratch_addr[device] = p;
+  }
+  return static_cast<unsigned char*>(g_scratch_addr[device]);
+}
+
+}  // namespace
+}  // namespace pk
+
+extern "C" int pk_cast_rays_noalloc(pk_ctx* c, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
+                                    uint32_t* hits4, uint32_t* hit_index, uint32_t* n_hits) {
+  if (!c) return PK_ERR_ARG;
+  try {
+    check(cudaSetDevice(c->device), "cudaSetDevice");
+    if (!c->bvh_ready) { c->err = "pk_cast_rays_noalloc: no BVH"; return PK_ERR_STATE; }
+    if ((n && (!ray_o4 || !ray_d4 || !hits4 || !hit_index)) || !n_hits) {
+      c->err = "pk_cast_rays_noalloc: null buffer";
+      return PK_ERR_ARG;
+    }
+    if (n > NOALLOC_MAX_RAYS) {
+      c->err = "pk_cast_rays_noalloc: at most 1048576 rays per call (the size of its static scratch)";
+      return PK_ERR_ARG;
+    }
+    unsigned char* base = noalloc_scratch(c->device);
+    const CastScratch s{reinterpret_cast<uint32_t*>(base), reinterpret_cast<uint32_t*>(base + NOALLOC_FLAGS_OFF),
+                        reinterpret_cast<unsigned long long*>(base + NOALLOC_TILES_OFF)};
+    cast_enqueue(c, reinterpret_cast<const float4*>(ray_o4), reinterpret_cast<const float4*>(ray_d4), n, any_hit,
+                 reinterpret_cast<uint4*>(hits4), hit_index, n_hits, s, c->stream);
+    uint32_t err = 0;
+    check(cudaMemcpyAsync(&err, s.tickets + 2, 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    if (err) { c->err = "pk_cast_rays_noalloc: device error flags"; return PK_ERR_DEVICE; }
     return PK_OK;
   } catch (CudaError& e) {
     c->err = e.what();
