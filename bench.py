@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--subdivisions", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked"],
+                    help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
+    ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
+                    help="inner-node record size (identical results): decoded float boxes (64) or snorm16 (32)")
     return ap.parse_args()
 
 
@@ -295,6 +299,11 @@ def gpu_arm(args):
     D = Dist(world, local)
     src = make_scene(args)
     ctx, bvh_ms = setup_context(src, local)
+    from pike_gb300 import _lib
+    mode = _lib.PK_TRACE_PERSISTENT if args.trace_mode == "persistent" else _lib.PK_TRACE_CHUNKED
+    if args.node_records == 32:
+        mode |= _lib.PK_TRACE_COMPACT_RECORDS
+    ctx.call("pk_set_trace_mode", mode)
     cam = camera_struct(src)
     ctx.call("pk_set_camera", cam)
     B = args.bounces
@@ -383,10 +392,10 @@ def gpu_arm(args):
             "config": {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
                        "bounces": B, "env": "2048x1024 RGBE8", "spp_mpix_per_s": spp_mpix,
                        "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
-                       "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}",
+                       "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}", "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
                        "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
                        "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},
-            "roofline": {"bound": "hbm", "kernel": "k_trace<closest, fused miss>", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "closest-hit traversal (trace.wgsl + fused shade_miss)", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes_launch,
                          "launch_ms": trace_ms,

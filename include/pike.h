@@ -226,6 +226,17 @@ int pk_host_free(pk_ctx* ctx, void* p);
 /* Enqueue a copy of the W*H*4-byte display image into host memory (pinned for
  * the copy to overlap); completes at the next pk_sync or stop timer. */
 int pk_read_display_async(pk_ctx* ctx, uint8_t* out8);
+/* Traversal scheduling of pk_trace / pk_trace_shadow / pk_render_frame:
+ * PK_TRACE_CHUNKED gives each warp 32 consecutive rays at a time;
+ * PK_TRACE_PERSISTENT (default) keeps warps resident and refills idle lanes in
+ * batches.  OR PK_TRACE_COMPACT_RECORDS to traverse 32-byte inner records that
+ * keep the reference's snorm16 boxes (decoded in the kernel) instead of the
+ * default 64-byte records with the same boxes pre-decoded: half the node bytes,
+ * more instructions per step.  Every combination gives identical results. */
+#define PK_TRACE_CHUNKED 0
+#define PK_TRACE_PERSISTENT 1
+#define PK_TRACE_COMPACT_RECORDS 2
+int pk_set_trace_mode(pk_ctx* ctx, int mode);
 /* Elementwise evaluation of the library's built-in definitions on the GPU
  * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */
 int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);

@@ -239,7 +239,7 @@ void or_trace_rays(void* p, const float* rays8, size_t n, int any_hit, uint32_t*
 }
 
 // Elementwise math probes for parity of the built-in definitions:
-// fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y).
+// fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y), 8 snorm16 decode.
 void or_math(int fn, const float* x, const float* y, float* out, size_t n) {
   for (size_t i = 0; i < n; i++) {
     float a = x[i], b = y ? y[i] : 0.0f;
@@ -253,6 +253,7 @@ void or_math(int fn, const float* x, const float* y, float* out, size_t n) {
       case 5: r = exp2_(a); break;
       case 6: r = log2_(a); break;
       case 7: r = pow_(a, b); break;
+      case 8: r = snorm16((int32_t)f2u(a)); break;  // unpack2x16snorm of an integer held in the bits of a
       default: r = NAN;
     }
     out[i] = r;

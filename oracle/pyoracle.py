@@ -238,7 +238,7 @@ class Renderer:
         return out
 
 
-MATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan2": 3, "acos": 4, "exp2": 5, "log2": 6, "pow": 7}
+MATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan2": 3, "acos": 4, "exp2": 5, "log2": 6, "pow": 7, "snorm16": 8}
 
 
 def math_fn(name: str, x: np.ndarray, y: np.ndarray | None = None) -> np.ndarray:

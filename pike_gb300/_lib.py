@@ -19,6 +19,7 @@ HEADER = os.path.join(HERE, "..", "include", "pike.h")
 PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED = range(6)
 PK_BVH_SWEEP = 0
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
+PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS = 0, 1, 2
 
 
 class PikeError(RuntimeError):
@@ -79,6 +80,7 @@ def load(path: str = LIB_PATH):
         "pk_host_free": [_P, _P], "pk_read_display_async": [_P, _P],
         "pk_cast_rays": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
         "pk_cast_rays_noalloc": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
+        "pk_set_trace_mode": [_P, C.c_int],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -94,6 +94,7 @@ int pk_destroy(pk_ctx* c) {
   if (!c) return PK_ERR_ARG;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->frame_graph) cudaGraphExecDestroy(c->frame_graph);
   for (auto& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto e : c->event_pool) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
@@ -107,6 +108,7 @@ const char* pk_last_error(const pk_ctx* c) { return c ? c->err.c_str() : "null c
 
 int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
   return guarded(c, [&]() {
+    c->invalidate_graph();
     if (!width || !height || width > 0xffff || height > 0xffff) return fail(c, PK_ERR_ARG, "resolution out of range");
     if ((uint64_t)width * height >= (1ull << 28)) return fail(c, PK_ERR_ARG, "more than 2^28 pixels");
     if (!batch || batch > (1u << 28)) return fail(c, PK_ERR_ARG, "batch size out of range");
@@ -170,6 +172,7 @@ int pk_scene_flatten(pk_ctx* c, const double* pos3, const double* nrm3, const do
     c->n_verts = n_verts;
     c->n_tris = n_tris;
     c->bvh_ready = false;
+    c->invalidate_graph();
     return PK_OK;
   });
 }
@@ -188,6 +191,7 @@ int pk_scene_upload(pk_ctx* c, const int32_t* tri4, uint32_t n_tris, const doubl
     c->n_verts = n_verts;
     c->n_tris = n_tris;
     c->bvh_ready = false;
+    c->invalidate_graph();
     return PK_OK;
   });
 }
@@ -213,6 +217,7 @@ int pk_materials_set(pk_ctx* c, const double* mats9, uint32_t n_mats) {
     check(cudaStreamSynchronize(c->stream), "sync");
     c->n_mats = n_mats;
     c->n_layers = (uint32_t)(layers.size() / 4);
+    c->invalidate_graph();
     return PK_OK;
   });
 }
@@ -225,6 +230,7 @@ int pk_materials_upload(pk_ctx* c, const int32_t* mat4, uint32_t n_mats, const u
     check(cudaStreamSynchronize(c->stream), "sync");
     c->n_mats = n_mats;
     c->n_layers = n_layers;
+    c->invalidate_graph();
     return PK_OK;
   });
 }
@@ -243,18 +249,20 @@ int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32
 // ---------------- BVH ----------------
 static int finish_bvh(pk_ctx* c) {
   c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
+  c->inner32.alloc(2 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
   DevBuf<int> root(1);
   DevBuf<uint32_t> err(1);
   check(cudaMemsetAsync(err.p, 0, 4, c->stream), "memset");
   if (convert_bvh(c->stream, c->nodes5.p, c->n_nodes, c->tri4_leaf.p, c->n_leaf_tris, c->verts4.p, c->bvh_verts,
-                  c->inner.p, c->tris.p, root.p, err.p))
+                  c->inner.p, c->inner32.p, c->tris.p, root.p, err.p))
     throw CudaError(std::string("convert_bvh: ") + cudaGetErrorString(cudaGetLastError()));
   uint32_t herr = 0;
   check(cudaMemcpy(&c->root, root.p, 4, cudaMemcpyDeviceToHost), "D2H");
   check(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost), "D2H");
   if (herr) return fail(c, PK_ERR_ARG, "malformed BVH (child index, leaf size >= 128 or vertex index out of range)");
   c->bvh_ready = true;
+  c->invalidate_graph();
   return PK_OK;
 }
 
@@ -324,6 +332,7 @@ static int env_set(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const
   check(cudaStreamSynchronize(c->stream), "sync");
   c->env_w = w; c->env_h = h; c->env_nb = nb;
   c->env_ready = true;
+  c->invalidate_graph();
   return PK_OK;
 }
 
@@ -404,6 +413,7 @@ int pk_set_camera(pk_ctx* c, const pk_camera_state* cam) {
 
 int pk_set_postprocess(pk_ctx* c, float exposure, float saturation) {
   return guarded(c, [&]() {
+    c->invalidate_graph();
     c->exposure = exposure;
     c->saturation = saturation;
     return PK_OK;
@@ -527,7 +537,45 @@ int pk_postprocess(pk_ctx* c) {
   });
 }
 
+static void render_frame_launches(pk_ctx* c, uint32_t bounces);
+
+// pk_render_frame's launches are captured once into a CUDA graph and replayed
+// (the sequence only reads device-side counts, so it is the same every frame);
+// with per-kernel timing on, the launches are issued directly instead.
 static void render_frame(pk_ctx* c, uint32_t bounces) {
+  if (c->timing) {
+    render_frame_launches(c, bounces);
+    return;
+  }
+  if (!c->frame_graph || c->graph_bounces != bounces || c->graph_counting != c->counting ||
+      c->graph_key != c->state_version) {
+    if (c->frame_graph) cudaGraphExecDestroy(c->frame_graph);
+    c->frame_graph = nullptr;
+    cudaGraph_t g = nullptr;
+    check(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    try {
+      render_frame_launches(c, bounces);
+    } catch (...) {
+      cudaStreamEndCapture(c->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    check(cudaStreamEndCapture(c->stream, &g), "cudaStreamEndCapture");
+    cudaGraphExec_t e = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
+    cudaGraphDestroy(g);
+    check(ie, "cudaGraphInstantiate");
+    c->frame_graph = e;
+    c->graph_bounces = bounces;
+    c->graph_counting = c->counting;
+    c->graph_key = c->state_version;
+    c->frames--;  // the capture itself rendered nothing
+  }
+  check(cudaGraphLaunch(c->frame_graph, c->stream), "cudaGraphLaunch");
+  c->frames++;
+}
+
+static void render_frame_launches(pk_ctx* c, uint32_t bounces) {
   LaunchCtx L = c->launch();
   const uint32_t nb = std::min(bounces, MAX_BOUNCES);
   // RenderState.generateCommands + tick(): clear colour, hit/miss and ray counts
@@ -716,6 +764,16 @@ int pk_read_stats(pk_ctx* c, uint64_t out10[10]) {
     for (int i = 0; i < 8; i++) out10[i] = h.stat[i];
     out10[8] = h.rays_traced;
     out10[9] = c->frames;
+    return PK_OK;
+  });
+}
+int pk_set_trace_mode(pk_ctx* c, int mode) {
+  return guarded(c, [&]() {
+    c->invalidate_graph();
+    const int sched = mode & 1;
+    if (mode & ~(1 | PK_TRACE_COMPACT_RECORDS)) return fail(c, PK_ERR_ARG, "unknown trace mode");
+    c->trace_mode = sched;
+    c->compact_nodes = (mode & PK_TRACE_COMPACT_RECORDS) != 0;
     return PK_OK;
   });
 }

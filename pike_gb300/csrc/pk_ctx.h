@@ -38,6 +38,18 @@ struct pk_ctx {
   uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;
   uint32_t ct = 0, st = 0;  // look-back tiles per compaction / shade launch
   unsigned g_trace = 1, g_compact = 1, g_shade = 1;  // persistent grid sizes
+  int trace_mode = pk::TRACE_PERSISTENT;
+  // CUDA graph of one pk_render_frame (replayed per frame); rebuilt when any
+  // pointer or launch parameter captured in it changes.
+  cudaGraphExec_t frame_graph = nullptr;
+  uint32_t graph_bounces = 0;
+  bool graph_counting = false;
+  unsigned long long graph_key = 0, state_version = 1;
+  void invalidate_graph() {
+    if (frame_graph) cudaGraphExecDestroy(frame_graph);
+    frame_graph = nullptr;
+    state_version++;
+  }
   // render state
   DevBuf<Counters> ctr;
   DevBuf<CamState> cam;
@@ -65,6 +77,8 @@ struct pk_ctx {
   DevBuf<int32_t> nodes5;
   DevBuf<int4> tri4_leaf;
   DevBuf<float4> verts4, inner, tris;
+  DevBuf<int4> inner32;
+  bool compact_nodes = false;  // traverse 32-byte records (same boxes as the 64-byte ones)
   int root = 0;
   bool bvh_ready = false;
   // env
@@ -96,7 +110,8 @@ struct pk_ctx {
     L.stream = stream;
     L.ctr = ctr.p;
     L.cam = cam.p;
-    L.scene = pk::SceneDev{inner.p, tris.p, tri4_leaf.p, attrs.p, mat4.p, layers.p, (int)n_layers, root,
+    L.scene = pk::SceneDev{inner.p, compact_nodes ? inner32.p : nullptr, tris.p, tri4_leaf.p, attrs.p, mat4.p,
+                           layers.p, (int)n_layers, root,
                        n_leaf_tris, n_verts, n_mats};
     L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
     L.color = color.p;
@@ -109,6 +124,7 @@ struct pk_ctx {
     L.trace_blocks = g_trace;
     L.compact_blocks = g_compact;
     L.shade_blocks = g_shade;
+    L.trace_mode = trace_mode;
     return L;
   }
   cudaEvent_t take_event() {

@@ -58,7 +58,8 @@ struct RayQ {
 // word (size << 24 | base).  Triangles are stored leaf-ordered as
 // {v0.xyz, e1.x}, {e1.yz, e2.xy}, {e2.z, -, -, -} with e1 = v1 - v0, e2 = v2 - v0.
 struct SceneDev {
-  const float4* inner;     // 4 float4 per inner record
+  const float4* inner;     // 4 float4 per inner record (64-byte format)
+  const int4* inner32;     // 2 int4 per inner record (32-byte format); used when not null
   const float4* tris;      // 3 float4 per leaf-ordered triangle
   const int4* tri4;        // leaf-ordered {i0, i1, i2, matId}
   const uint4* attrs;      // per-vertex {tangent, bitangent, normal (snorm8x4), uv (snorm16x2)}

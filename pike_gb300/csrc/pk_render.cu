@@ -142,6 +142,148 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
   }
 }
 
+// Persistent variant of the same two entry points.  Each lane owns one ray at a
+// time; when at least REFILL_MIN lanes of a warp are idle (or no lane has work)
+// they claim new queue slots together with one atomic, so a warp no longer
+// waits for the slowest of a fixed group of 32 rays.  The loop is split into an
+// inner-node loop and a leaf loop (while-while).  There is no speculation: a
+// leaf is intersected as soon as the ray reaches it, so each ray visits the
+// same nodes in the same order as trace.wgsl's loop and gets the same hit.
+// Hit bits are set with atomicOr in a flag array zeroed before the launch.
+constexpr int REFILL_MIN = 16;
+
+template <bool ANY, bool FUSED, bool COUNT>
+__global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+                                                              const uint32_t* __restrict__ countp, RayQ R,
+                                                              uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
+                                                              float4* __restrict__ color, uint32_t npix,
+                                                              uint32_t* __restrict__ ticket) {
+  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+  int lstack[STACK_LOCAL];
+  const uint32_t n = *countp;
+  const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x;
+  const uint32_t ltmask = (1u << lane) - 1u;
+  const float theta = ctr->env_theta;
+  const float eps = ANY ? 1e-7f : 1e-8f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&ctr->rays_traced, (unsigned long long)n);
+    if (COUNT) atomicAdd(&ctr->stat[ANY ? 5 : 4], (unsigned long long)n);
+  }
+  uint32_t nfetch = 0, ntest = 0, nhit = 0;
+  uint32_t j = 0;
+  bool have = false, exhausted = false;
+  float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, ix = 0.f, iy = 0.f, iz = 0.f;
+  float best_t = MAX_T;
+  int best_i = -1;
+  uint32_t best_b = 0u;
+  int sp = 0, cur = 0;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
+    const uint32_t busy = __ballot_sync(0xffffffffu, have);
+    if (idle && (__popc(idle) >= REFILL_MIN || busy == 0u)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(ticket, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!have && !exhausted) {
+        j = base + (uint32_t)__popc(idle & ltmask);
+        if (j < n) {
+          const float4 o = R.o[j], d = R.d[j];
+          ox = o.x; oy = o.y; oz = o.z;
+          dx = d.x; dy = d.y; dz = d.z;
+          ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
+          best_t = MAX_T; best_i = -1; best_b = 0u;
+          sp = 0;
+          cur = sc.root;
+          have = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) break;
+    if (!have) continue;
+    bool fin = false;
+    // inner nodes
+    while (cur >= 0) {
+      if (COUNT) nfetch += 3;
+      float lh, rh;
+      int cl, cr;
+      inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
+      const bool lok = lh < best_t, rok = rh < best_t;
+      if (lok && rok) {
+        int nearc, farc;
+        if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
+        if (sp < STACK_SMEM) sstack[sp][tid] = farc;
+        else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+        else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
+        ++sp;
+        cur = nearc;
+        continue;
+      }
+      if (lok) { cur = cl; continue; }
+      if (rok) { cur = cr; continue; }
+      if (sp == 0) { fin = true; break; }
+      --sp;
+      cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+    }
+    // leaves
+    while (!fin && cur < 0) {
+      if (COUNT) nfetch += 1;
+      const uint32_t word = (uint32_t)cur & 0x7fffffffu;
+      const int size = (int)(word >> 24);
+      const int base = (int)(word & 0x00ffffffu);
+      for (int i = 0; i < size; i++) {
+        if (COUNT) ntest += 1;
+        const float4* tp = sc.tris + 3 * (size_t)(base + i);
+        const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
+        const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
+        const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+        const float det = e1x * px + e1y * py + e1z * pz;
+        if (fabsf(det) < eps) continue;
+        const float inv_det = 1.0f / det;
+        const float tx = ox - A.x, ty = oy - A.y, tz = oz - A.z;
+        const float u = (tx * px + ty * py + tz * pz) * inv_det;
+        if (u < 0.0f || u > 1.0f) continue;
+        const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+        const float v = (dx * qx + dy * qy + dz * qz) * inv_det;
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
+        const float res = dist > eps ? dist : MAX_T;
+        if (res < best_t) {
+          best_t = res;
+          best_i = base + i;
+          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        }
+      }
+      if (ANY && best_i != -1) { fin = true; break; }
+      if (sp == 0) { fin = true; break; }
+      --sp;
+      cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+    }
+    if (fin) {
+      const bool hit = best_i != -1;
+      if (hit) {
+        if (!ANY) hrec[j] = make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u);
+        if (!(ANY && FUSED)) atomicOr(flags + (j >> 5), 1u << (j & 31u));
+        if (COUNT) nhit += 1;
+      } else if (FUSED) {
+        const float4 tpv = R.t[j];
+        const V3 e = env_color(env, theta, v3(dx, dy, dz));
+        add_color(color, npix, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y, e.z * tpv.z, 1.0f,
+                  &ctr->err);
+      }
+      have = false;
+    }
+  }
+  if (COUNT) {
+    atomicAdd(&ctr->stat[ANY ? 2 : 0], (unsigned long long)nfetch);
+    atomicAdd(&ctr->stat[ANY ? 3 : 1], (unsigned long long)ntest);
+    atomicAdd(&ctr->stat[ANY ? 7 : 6], (unsigned long long)nhit);
+  }
+}
+
 // =====================================================================
 // Stable compaction of trace / shadow outcomes.
 //   MODE 0: closest-hit flags -> hit list (+ miss queue when MISSQ)
@@ -386,7 +528,9 @@ constexpr int SHADE_THREADS = 128;
 // main (:407-483).  Tiles of SHADE_THREADS hits are claimed in order; bounce
 // and shadow rays are written at their stable ranks found by a block scan plus
 // decoupled look-back, so slot order equals the serial order of the reference.
-__global__ void __launch_bounds__(SHADE_THREADS) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+// 8 resident blocks per SM (<= 64 registers): more shading warps in flight to
+// cover the attribute/texel/env gathers; a few registers spill to L1.
+__global__ void __launch_bounds__(SHADE_THREADS, 8) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                           const uint32_t* __restrict__ hit_list,
                                                           const uint4* __restrict__ hrec, RayQ Rin, RayQ Rout,
                                                           RayQ S, uint32_t capacity, float4* __restrict__ color,
@@ -591,6 +735,7 @@ __global__ void k_math(int fn, const float* __restrict__ x, const float* __restr
     case 5: r = exp2_(a); break;
     case 6: r = log2_(a); break;
     case 7: r = pow_(a, b); break;
+    case 8: r = snorm16_decode(__float_as_int(a)); break;
     default: r = __int_as_float(0x7fc00000);
   }
   out[i] = r;
@@ -608,7 +753,7 @@ uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) 
 // more blocks than there can be work items.
 void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade) {
   int t = 0, c = 0, s = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace<false, true, false>, TRACE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_shade, SHADE_THREADS, 0);
   const unsigned warps = (capacity + 31u) / 32u;
@@ -625,6 +770,21 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
   const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
+  if (L.trace_mode == TRACE_PERSISTENT) {
+    const unsigned words = (L.capacity + 31u) / 32u + 1u;
+    if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
+#define PK_TRACED(A, F, C) \
+  k_trace_dyn<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
+    if (!any_hit) {
+      if (fused) { if (count) PK_TRACED(false, true, true); else PK_TRACED(false, true, false); }
+      else { if (count) PK_TRACED(false, false, true); else PK_TRACED(false, false, false); }
+    } else {
+      if (fused) { if (count) PK_TRACED(true, true, true); else PK_TRACED(true, true, false); }
+      else { if (count) PK_TRACED(true, false, true); else PK_TRACED(true, false, false); }
+    }
+#undef PK_TRACED
+    return;
+  }
 #define PK_TRACE(A, F, C) \
   k_trace<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
   if (!any_hit) {

@@ -7,6 +7,10 @@
 
 namespace pk {
 
+// Traversal scheduling: fixed 32-ray chunks per warp, or persistent lanes with
+// batched refill.  Both visit every ray's nodes in the reference order.
+enum TraceMode : int { TRACE_CHUNKED = 0, TRACE_PERSISTENT = 1 };
+
 // Everything a launch needs that is fixed for a configured context.
 struct LaunchCtx {
   cudaStream_t stream;
@@ -22,6 +26,7 @@ struct LaunchCtx {
   uint32_t capacity;       // ray / hit / shadow queue capacity (batch rounded up to 128)
   uint32_t miss_capacity;  // 2 * capacity
   unsigned trace_blocks, compact_blocks, shade_blocks;
+  int trace_mode;
 };
 
 void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads);
@@ -50,7 +55,7 @@ void launch_math(cudaStream_t s, int fn, const float* x, const float* y, float* 
 // Convert the reference 20-byte BFS nodes + leaf-ordered triangles + 16-byte
 // vertices into the traversal format (inner records, v0/e1/e2 triangles).
 int convert_bvh(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4* tri4, uint32_t n_tris,
-                const float4* verts4, uint32_t n_verts, float4* inner, float4* tris, int* root_code,
+                const float4* verts4, uint32_t n_verts, float4* inner, int4* inner32, float4* tris, int* root_code,
                 uint32_t* err);
 // Row S: per-vertex attribute quantisation (scene.js:456-470).
 void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,

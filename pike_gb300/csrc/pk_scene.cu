@@ -130,6 +130,27 @@ __global__ void k_inner_records(const int32_t* __restrict__ nodes5, uint32_t n, 
                                             child_code(nodes5, rank, (uint32_t)l + 1, n_tris, err), 0, 0);
 }
 
+// 32-byte records: the children's reference masks and child codes.
+__global__ void k_inner_records32(const int32_t* __restrict__ nodes5, uint32_t n, const uint32_t* __restrict__ rank,
+                                  const float4* __restrict__ inner64, int4* __restrict__ inner32) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t* nd = nodes5 + 5 * (size_t)i;
+  if (nd[1] > -1) return;
+  const uint32_t r = rank[i];
+  const int4 codes = reinterpret_cast<const int4*>(inner64 + 4 * (size_t)r)[3];  // validated child codes
+  const int32_t l = nd[0];
+  int4 q0 = make_int4(0, 0, 0, 0), q1 = make_int4(0, 0, codes.x, codes.y);
+  if (l >= 1 && (uint32_t)l > i && (uint32_t)l + 1 < n) {
+    const int32_t* a = nodes5 + 5 * (size_t)l;
+    const int32_t* b = nodes5 + 5 * (size_t)(l + 1);
+    q0 = make_int4(a[2], a[3], a[4], b[2]);
+    q1 = make_int4(b[3], b[4], codes.x, codes.y);
+  }
+  inner32[2 * (size_t)r] = q0;
+  inner32[2 * (size_t)r + 1] = q1;
+}
+
 __global__ void k_tri_edges(const int4* __restrict__ tri4, uint32_t n, const float4* __restrict__ verts4,
                             uint32_t n_verts, float4* __restrict__ tris, uint32_t* err) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -152,12 +173,13 @@ __global__ void k_tri_edges(const int4* __restrict__ tri4, uint32_t n, const flo
 }
 
 int convert_bvh(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4* tri4, uint32_t n_tris,
-                const float4* verts4, uint32_t n_verts, float4* inner, float4* tris, int* root_code,
+                const float4* verts4, uint32_t n_verts, float4* inner, int4* inner32, float4* tris, int* root_code,
                 uint32_t* err) {
   DevBuf<uint32_t> flag(n_nodes), rank(n_nodes);
   k_inner_flags<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, flag.p);
   scan_exclusive_u32(s, flag.p, rank.p, n_nodes, nullptr);
   k_inner_records<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, rank.p, n_tris, inner, root_code, err);
+  k_inner_records32<<<(n_nodes + 255) / 256, 256, 0, s>>>(nodes5, n_nodes, rank.p, inner, inner32);
   if (n_tris) k_tri_edges<<<(n_tris + 255) / 256, 256, 0, s>>>(tri4, n_tris, verts4, n_verts, tris, err);
   return cudaStreamSynchronize(s) == cudaSuccess ? 0 : 1;
 }

@@ -23,9 +23,52 @@ __device__ __forceinline__ float box_hit(float xa, float xb, float ya, float yb,
   return (tmax >= tmin && tmax > 0.0f) ? tmin : MAX_T;
 }
 
+// unpack2x16snorm component: max(s / 32767, -1).  For integer s in
+// [-32768, 32767] the product with RN(1/32767) corrected by two FMAs equals the
+// IEEE quotient for every input (the tests check all 65536), so this is the
+// same value the reference decode and the 64-byte records hold.
+__device__ __forceinline__ float snorm16_decode(int s) {
+  const float sf = (float)s;
+  const float r = 0x1.0002p-15f;
+  const float q0 = sf * r;
+  const float e = __fmaf_rn(-q0, 32767.0f, sf);
+  return fmax_(__fmaf_rn(e, r, q0), -1.0f);
+}
+__device__ __forceinline__ float snorm_lo(int m) { return snorm16_decode((int)(int16_t)(uint16_t)((uint32_t)m & 0xffffu)); }
+__device__ __forceinline__ float snorm_hi(int m) { return snorm16_decode((int)(int16_t)(uint16_t)((uint32_t)m >> 16)); }
+
+// One inner-node step: both children's entry distances and child codes.
+// 32-byte records keep the reference's snorm16 boxes {Lx, Ly, Lz, Rx}{Ry, Rz,
+// codeL, codeR}; 64-byte records (the default: fewer instructions per step,
+// which matters more than bytes here) hold the same boxes decoded.
+__device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, float ox, float oy, float oz, float ix,
+                                               float iy, float iz, float& lh, float& rh, int& cl, int& cr);
+
 constexpr int TRACE_THREADS = 128;
 constexpr int STACK_SMEM = 32;   // per-thread entries kept in shared memory
 constexpr int STACK_LOCAL = 32;  // overflow entries in local memory (total depth 64)
+
+__device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, float ox, float oy, float oz, float ix,
+                                               float iy, float iz, float& lh, float& rh, int& cl, int& cr) {
+  if (sc.inner32) {
+    const int4* rec = sc.inner32 + 2 * (size_t)cur;
+    const int4 q0 = __ldg(rec), q1 = __ldg(rec + 1);
+    lh = box_hit(snorm_lo(q0.x), snorm_hi(q0.x), snorm_lo(q0.y), snorm_hi(q0.y), snorm_lo(q0.z), snorm_hi(q0.z), ox,
+                 oy, oz, ix, iy, iz);
+    rh = box_hit(snorm_lo(q0.w), snorm_hi(q0.w), snorm_lo(q1.x), snorm_hi(q1.x), snorm_lo(q1.y), snorm_hi(q1.y), ox,
+                 oy, oz, ix, iy, iz);
+    cl = q1.z;
+    cr = q1.w;
+  } else {
+    const float4* rec = sc.inner + 4 * (size_t)cur;
+    const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
+    const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
+    lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
+    rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+    cl = ch.x;
+    cr = ch.y;
+  }
+}
 
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
@@ -44,15 +87,13 @@ __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy,
   for (;;) {
     if (cur >= 0) {
       if (COUNT) nfetch += 3;
-      const float4* rec = sc.inner + 4 * (size_t)cur;
-      const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
-      const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
-      const float lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
-      const float rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+      float lh, rh;
+      int cl, cr;
+      inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
       const bool lok = lh < best_t, rok = rh < best_t;
       if (lok && rok) {
         int nearc, farc;
-        if (lh > rh) { nearc = ch.y; farc = ch.x; } else { nearc = ch.x; farc = ch.y; }
+        if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
         if (sp < STACK_SMEM) sstack[sp][tid] = farc;
         else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
         else { atomicOr(err, ERR_STACK); break; }
@@ -60,8 +101,8 @@ __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy,
         cur = nearc;
         continue;
       }
-      if (lok) { cur = ch.x; continue; }
-      if (rok) { cur = ch.y; continue; }
+      if (lok) { cur = cl; continue; }
+      if (rok) { cur = cr; continue; }
     } else {
       if (COUNT) nfetch += 1;
       const uint32_t word = (uint32_t)cur & 0x7fffffffu;

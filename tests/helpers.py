@@ -26,13 +26,15 @@ class Pair:
     """A synthetic scene set up on the GPU and in the oracle, sharing the same inputs."""
 
     def __init__(self, src, oracle, ctx: Context | None = None, gpu_bvh: bool = True, gpu_env: bool = True,
-                 batch: int | None = None, threads: int | None = None, camera: dict | None = None):
+                 batch: int | None = None, threads: int | None = None, camera: dict | None = None,
+                 trace_mode: int = _lib.PK_TRACE_PERSISTENT):
         self.src = src
         self.P = oracle.Prepared(src, threads=threads, batch=batch)
         self.ctx = ctx or Context(0)
         c = self.ctx
         self.batch = batch or src.width * src.height
         c.call("pk_configure", src.width, src.height, self.batch)
+        c.call("pk_set_trace_mode", trace_mode)
         pos, nrm = np.ascontiguousarray(src.pos), np.ascontiguousarray(src.normal)
         tan, uv = np.ascontiguousarray(src.tangent), np.ascontiguousarray(src.uv)
         tris = np.ascontiguousarray(src.tris, np.int32)

@@ -36,9 +36,11 @@ def test_fused_small_scene_matches_oracle(oracle, pk_built):
     assert c["samples"] == src.spp and c["err"] == 0
 
 
-def test_fused_sphere_matches_oracle(oracle, pk_built):
+@pytest.mark.parametrize("mode", [_lib.PK_TRACE_PERSISTENT, _lib.PK_TRACE_CHUNKED,
+                                  _lib.PK_TRACE_CHUNKED | _lib.PK_TRACE_COMPACT_RECORDS])
+def test_fused_sphere_matches_oracle(oracle, pk_built, mode):
     src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
-    pair = Pair(src, oracle)
+    pair = Pair(src, oracle, trace_mode=mode)
     fused_frames(pair, 3, 8)
     oracle_frames(pair, 3, 8)
     assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "accumulated radiance")
@@ -60,6 +62,8 @@ def test_fused_equals_pass_path(oracle, pk_built):
     a = Pair(src, oracle)
     fused_frames(a, 2, 8)
     fused = a.image("accum")
+    # the pass path below runs with the other traversal schedule: results must not depend on it
+    a.ctx.call("pk_set_trace_mode", _lib.PK_TRACE_CHUNKED)
     c = a.ctx
     c.call("pk_write_accum", ptr(np.zeros_like(fused)))
     for f in range(2):

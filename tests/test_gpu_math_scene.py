@@ -52,6 +52,19 @@ def test_math_binary_bit_exact(ctx, oracle, name):
     assert_bits_equal(got[~nan], want[~nan], name)
 
 
+def test_snorm16_decode_all_values(ctx, oracle):
+    """The traversal decodes the reference's snorm16 node boxes with a
+    reciprocal product and two FMAs; it must equal max(s / 32767, -1) with IEEE
+    division for every one of the 65536 values."""
+    s = np.arange(-32768, 32768, dtype=np.int32).view(np.float32)
+    want = oracle.math_fn("snorm16", s)
+    got = np.zeros_like(s)
+    ctx.call("pk_math_eval", 8, ptr(s), None, ptr(got), s.size)
+    assert_bits_equal(got, want, "snorm16 decode")
+    ieee = np.maximum(np.arange(-32768, 32768, dtype=np.float32) / np.float32(32767.0), np.float32(-1.0))
+    assert_bits_equal(want, ieee, "oracle snorm16 vs numpy IEEE division")
+
+
 def test_scene_flatten_matches_oracle(ctx, oracle):
     src = synth.displaced_sphere_scene(subdivisions=4, width=64, height=64)
     pos_o, attrs_o = oracle.flatten(src)

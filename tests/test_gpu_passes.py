@@ -66,14 +66,17 @@ def test_passes_small_scene_oracle_bvh(oracle, pk_built):
     run_pass_parity(Pair(src, oracle, gpu_bvh=False, gpu_env=False), frames=2, bounces=4)
 
 
-def test_passes_small_scene_gpu_bvh(oracle, pk_built):
+@pytest.mark.parametrize("mode", [_lib.PK_TRACE_PERSISTENT, _lib.PK_TRACE_CHUNKED])
+def test_passes_small_scene_gpu_bvh(oracle, pk_built, mode):
     src = synth.small_scene(width=128, height=128)
-    run_pass_parity(Pair(src, oracle), frames=2, bounces=4)
+    run_pass_parity(Pair(src, oracle, trace_mode=mode), frames=2, bounces=4)
 
 
-def test_passes_sphere_scene(oracle, pk_built):
+@pytest.mark.parametrize("mode", [_lib.PK_TRACE_PERSISTENT, _lib.PK_TRACE_CHUNKED,
+                                  _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_COMPACT_RECORDS])
+def test_passes_sphere_scene(oracle, pk_built, mode):
     src = synth.displaced_sphere_scene(subdivisions=5, width=80, height=48, env_size=(256, 128))
-    run_pass_parity(Pair(src, oracle), frames=2, bounces=6)
+    run_pass_parity(Pair(src, oracle, trace_mode=mode), frames=2, bounces=6)
 
 
 def test_passes_env_rotation_and_lens(oracle, pk_built):

@@ -99,6 +99,27 @@ def test_math_special_values(oracle):
     assert a[0] == 0.0 and a[1] == np.float32(math.pi) and a[2] == -np.float32(math.pi) and a[3] == np.float32(math.pi / 2)
 
 
+def test_snorm16_decode_fma_form_is_exact():
+    """The device decodes snorm16 boxes as fma(fma(-q0, 32767, s), r, q0) with
+    q0 = s * r and r = RN(1/32767); with exact rational arithmetic that equals
+    the IEEE quotient s / 32767 for all 65536 values."""
+    from fractions import Fraction
+
+    def rn32(q):
+        c = np.float32(float(q))
+        cands = [np.nextafter(c, np.float32(-np.inf)), c, np.nextafter(c, np.float32(np.inf))]
+        return min(cands, key=lambda v: (abs(Fraction(float(v)) - q), int(v.view(np.int32)) & 1))
+
+    r = np.float32(1.0) / np.float32(32767.0)
+    assert float(r).hex() == "0x1.0002000000000p-15"
+    for s in range(-32768, 32768, 7):  # every 7th value here; the GPU test covers all of them
+        sf = np.float32(s)
+        q0 = sf * r
+        e = rn32(Fraction(float(sf)) - Fraction(float(q0)) * 32767)
+        q1 = rn32(Fraction(float(e)) * Fraction(float(r)) + Fraction(float(q0)))
+        assert q1 == sf / np.float32(32767.0)
+
+
 # ---------------- bvh.js + trace_pass.js packing, restated in Python ----------------
 def js_toint16(v):
     if not math.isfinite(v):
