@@ -182,6 +182,14 @@ int pk_cast_rays(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t
 int pk_cast_rays_noalloc(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
                          uint32_t* hits4, uint32_t* hit_index, uint32_t* n_hits);
 
+/* Autofocus: Raycaster.cast (render/raycaster.js:13-131) of one ray in the
+ * normalised frame, in double precision against the unquantised triangles
+ * (Möller-Trumbore, epsilon 1e-12; 1e6 when nothing is hit), and the focal
+ * depth 1 - 1/t that PikeRenderer.focusCamera derives from it (pike.js:88-90).
+ * Needs the normaliser of pk_bvh_build.  focal_depth_out may be NULL. */
+int pk_focus_distance(pk_ctx* ctx, const double origin[3], const double dir[3], double* t_out,
+                      double* focal_depth_out);
+
 /* ---- readback ---------------------------------------------------------- */
 int pk_sync(pk_ctx* ctx);
 /* samples, num_hits, num_misses, num_rays, num_shadow, device error bits,

@@ -340,6 +340,75 @@ static inline PackedBVH pack_bvh(const BVHBuild& b, const double* pos3, size_t n
   return p;
 }
 
+// ---- raycaster.js: the CPU autofocus cast (double precision) -------------------
+// Raycaster.cast / traverse / closestNode / rayBoxIntersect / rayTriangleIntersect
+// (raycaster.js:13-131) on the built tree with exact double bounds.
+struct Raycaster {
+  const BVHBuild& b;
+  const double* pos3;
+  const int32_t* tri4;
+  double center[3], s;
+  double o[3], d[3];
+  static constexpr double MAXT = 1e6;
+  void norm(const double* v, double* out) const { for (int i = 0; i < 3; i++) out[i] = (v[i] - center[i]) * s; }
+  double box(const Box& bb) const {
+    double mn[3], mx[3], inv[3];
+    norm(bb.mn, mn);
+    norm(bb.mx, mx);
+    for (int i = 0; i < 3; i++) inv[i] = 1.0 / d[i];
+    const double tx1 = (mn[0] - o[0]) * inv[0], tx2 = (mx[0] - o[0]) * inv[0];
+    const double ty1 = (mn[1] - o[1]) * inv[1], ty2 = (mx[1] - o[1]) * inv[1];
+    const double tz1 = (mn[2] - o[2]) * inv[2], tz2 = (mx[2] - o[2]) * inv[2];
+    double tmin = js_min(tx1, tx2), tmax = js_max(tx1, tx2);
+    tmin = js_max(tmin, js_min(ty1, ty2));
+    tmax = js_min(tmax, js_max(ty1, ty2));
+    tmin = js_max(tmin, js_min(tz1, tz2));
+    tmax = js_min(tmax, js_max(tz1, tz2));
+    return (tmax >= tmin && tmax >= 0) ? tmin : MAXT;
+  }
+  double tri(int32_t id) const {
+    const double eps = 0.000000000001;
+    double v0[3], v1[3], v2[3];
+    norm(pos3 + 3 * (size_t)tri4[4 * (size_t)id + 0], v0);
+    norm(pos3 + 3 * (size_t)tri4[4 * (size_t)id + 1], v1);
+    norm(pos3 + 3 * (size_t)tri4[4 * (size_t)id + 2], v2);
+    double e1[3], e2[3], tv[3];
+    for (int i = 0; i < 3; i++) { e1[i] = v1[i] - v0[i]; e2[i] = v2[i] - v0[i]; tv[i] = o[i] - v0[i]; }
+    // Vec3.cross: y = -(a0*b2 - a2*b0); Vec.dot sums from 0 left to right
+    const double p[3] = {d[1] * e2[2] - d[2] * e2[1], -(d[0] * e2[2] - d[2] * e2[0]), d[0] * e2[1] - d[1] * e2[0]};
+    const double det = 0.0 + e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
+    if (det > -eps && det < eps) return MAXT;
+    const double inv = 1.0 / det;
+    const double u = (0.0 + tv[0] * p[0] + tv[1] * p[1] + tv[2] * p[2]) * inv;
+    if (u < 0 || u > 1) return MAXT;
+    const double q[3] = {tv[1] * e1[2] - tv[2] * e1[1], -(tv[0] * e1[2] - tv[2] * e1[0]), tv[0] * e1[1] - tv[1] * e1[0]};
+    const double v = (0.0 + d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * inv;
+    if (v < 0 || u + v > 1) return MAXT;
+    const double t = (0.0 + e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * inv;
+    return t > eps ? t : MAXT;
+  }
+  double traverse(int node, double closest) const {
+    const BuiltNode& n = b.nodes[node];
+    if (n.leaf) {
+      double res = MAXT;
+      for (int32_t id : n.leaf_tris) { const double x = tri(id); if (x < res) res = x; }
+      return res;
+    }
+    const double tl = box(b.nodes[n.left].bounds), tr = box(b.nodes[n.right].bounds);
+    const int l = tl < MAXT ? n.left : -1, r = tr < MAXT ? n.right : -1;
+    int ord[2];
+    double ot[2];
+    if (tl < tr) { ord[0] = l; ot[0] = tl; ord[1] = r; ot[1] = tr; } else { ord[0] = r; ot[0] = tr; ord[1] = l; ot[1] = tl; }
+    for (int i = 0; i < 2; i++) {
+      if (ord[i] >= 0 && ot[i] < closest) {
+        const double res = traverse(ord[i], closest);
+        closest = js_min(res, closest);
+      }
+    }
+    return closest;
+  }
+};
+
 // ---- Row E: env_sampler.js tables ----------------------------------------
 struct EnvTables {
   uint32_t w = 0, h = 0;

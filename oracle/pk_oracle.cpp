@@ -51,13 +51,15 @@ int or_materials(const double* mats9, size_t n_mats, int32_t* index_out4, uint8_
   return 0;
 }
 
-struct OrBVH { BVHBuild build; PackedBVH packed; };
+struct OrBVH { BVHBuild build; PackedBVH packed; std::vector<double> pos; std::vector<int32_t> tri4; };
 
 void* or_bvh_build(const double* pos3, size_t n_verts, const int32_t* tri4, size_t n_tris) {
   try {
     OrBVH* b = new OrBVH();
     b->build = build_bvh(pos3, tri4, n_tris);
     b->packed = pack_bvh(b->build, pos3, n_verts, tri4);
+    b->pos.assign(pos3, pos3 + 3 * n_verts);
+    b->tri4.assign(tri4, tri4 + 4 * n_tris);
     return b;
   } catch (std::exception& e) {
     g_err = e.what();
@@ -85,6 +87,17 @@ void or_bvh_copy(void* h, int32_t* nodes5, int32_t* tri4, float* verts4, double*
     norm10[7 + i] = b->packed.root_max[i];
   }
   norm10[3] = b->packed.scale;
+}
+
+// Raycaster.cast of n rays (6 doubles each: origin, dir in the normalised frame).
+void or_bvh_cast(void* h, const double* rays6, size_t n, double* t_out) {
+  OrBVH* b = (OrBVH*)h;
+  Raycaster rc{b->build, b->pos.data(), b->tri4.data(), {b->packed.center[0], b->packed.center[1], b->packed.center[2]},
+               b->packed.scale, {0, 0, 0}, {0, 0, 0}};
+  for (size_t i = 0; i < n; i++) {
+    for (int k = 0; k < 3; k++) { rc.o[k] = rays6[6 * i + k]; rc.d[k] = rays6[6 * i + 3 + k]; }
+    t_out[i] = rc.traverse(0, Raycaster::MAXT);
+  }
 }
 
 void* or_env_build(const uint8_t* rgbe, uint32_t w, uint32_t h) {

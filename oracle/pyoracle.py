@@ -103,9 +103,21 @@ class BVH:
         self.verts = np.zeros((pos.shape[0], 4), np.float32)
         norm = np.zeros(10, np.float64)
         L.or_bvh_copy(C.c_void_p(h), _p(self.nodes), _p(self.tris), _p(self.verts), _p(norm))
-        L.or_bvh_free(C.c_void_p(h))
+        self._h = h
         self.center, self.scale = norm[:3].copy(), float(norm[3])
         self.root_min, self.root_max = norm[4:7].copy(), norm[7:10].copy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().or_bvh_free(C.c_void_p(self._h))
+            self._h = None
+
+    def cast(self, rays6: np.ndarray) -> np.ndarray:
+        """Raycaster.cast (raycaster.js:128-131) of rays {origin, dir} in the normalised frame."""
+        rays6 = np.ascontiguousarray(rays6, np.float64)
+        out = np.zeros(rays6.shape[0], np.float64)
+        lib().or_bvh_cast(C.c_void_p(self._h), _p(rays6), C.c_size_t(rays6.shape[0]), _p(out))
+        return out
 
 
 class Env:

@@ -81,6 +81,7 @@ def load(path: str = LIB_PATH):
         "pk_cast_rays": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
         "pk_cast_rays_noalloc": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
         "pk_set_trace_mode": [_P, C.c_int],
+        "pk_focus_distance": [_P, _P, _P, C.POINTER(C.c_double), C.POINTER(C.c_double)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

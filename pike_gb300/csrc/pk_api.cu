@@ -271,6 +271,7 @@ int pk_bvh_upload(pk_ctx* c, const int32_t* nodes5, uint32_t n_nodes, const int3
   return guarded(c, [&]() {
     if (!nodes5 || !n_nodes || !verts4 || !n_verts) return fail(c, PK_ERR_ARG, "empty BVH");
     upload(c->nodes5, nodes5, 5 * (size_t)n_nodes, c->stream);
+    c->node_box_d.release();
     upload(c->tri4_leaf, tri4_leaf, n_leaf_tris, c->stream);
     upload(c->verts4, verts4, n_verts, c->stream);
     c->n_nodes = n_nodes;
@@ -290,6 +291,7 @@ int pk_bvh_build(pk_ctx* c, int mode) {
     if (build_bvh_sweep(c->stream, c->pos.p, c->n_verts, c->tri4.p, c->n_tris, out, why))
       return fail(c, PK_ERR_ARG, "pk_bvh_build: " + why);
     c->nodes5 = std::move(out.nodes5);
+    c->node_box_d = std::move(out.node_box);
     c->tri4_leaf = std::move(out.tri4_leaf);
     c->verts4 = std::move(out.verts4);
     c->n_nodes = out.n_nodes;
@@ -339,10 +341,18 @@ static int env_set(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const
 int pk_env_build(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h) {
   return guarded(c, [&]() {
     if (!rgbe || !w || !h) return fail(c, PK_ERR_ARG, "empty environment");
-    EnvHostTables t;
+    if ((uint64_t)w * h >= (1ull << 31)) return fail(c, PK_ERR_ARG, "environment too large");
+    upload(c->rgbe, rgbe, (size_t)w * h, c->stream);
     std::string why;
-    if (build_env_tables(rgbe, w, h, t, why)) return fail(c, PK_ERR_ARG, "pk_env_build: " + why);
-    return env_set(c, rgbe, w, h, t.bins2.data(), (uint32_t)(t.bins2.size() / 2), t.coords2.data(), t.pdf.data());
+    uint32_t nb = 0;
+    if (build_env_tables_gpu(c->stream, c->rgbe.p, w, h, c->bins, nb, c->coords, c->pdf, why)) {
+      c->env_ready = false;
+      return fail(c, PK_ERR_ARG, "pk_env_build: " + why);
+    }
+    c->env_w = w; c->env_h = h; c->env_nb = nb;
+    c->env_ready = true;
+    c->invalidate_graph();
+    return PK_OK;
   });
 }
 

@@ -629,6 +629,9 @@ int build_bvh_sweep(cudaStream_t s, const double* pos3, uint32_t n_verts, const 
   k_norm_verts<<<blocks(n_verts), 256, 0, s>>>(pos3, n_verts, center[0], center[1], center[2], longest, out.verts4.p);
   out.tri4_leaf.alloc(T);
   k_gather_tris<<<blocks(T), 256, 0, s>>>(tri4, leaf_ids.p, T, out.tri4_leaf.p);
+  out.node_box.alloc(6 * (size_t)n_nodes);
+  check(cudaMemcpyAsync(out.node_box.p, node_box.p, (size_t)n_nodes * sizeof(Box6), cudaMemcpyDeviceToDevice, s),
+        "memcpy");
   check(cudaGetLastError(), "bvh pack");
   check(cudaStreamSynchronize(s), "sync");
   out.n_nodes = n_nodes;

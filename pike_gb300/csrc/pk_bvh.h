@@ -12,6 +12,7 @@ struct BvhOut {
   DevBuf<int32_t> nodes5;   // BFS nodes, 5 words each (BVHNodeStruct)
   DevBuf<int4> tri4_leaf;   // leaf-ordered {i0, i1, i2, matId}
   DevBuf<float4> verts4;    // normalised positions (xyz, 0)
+  DevBuf<double> node_box;  // exact double bounds per BFS node {min xyz, max xyz} (raycaster.js uses them)
   uint32_t n_nodes = 0, n_leaf_tris = 0, depth = 0, largest_leaf = 0;
   double norm[4] = {0, 0, 0, 0};  // centre xyz, scale = 2 / longest
 };

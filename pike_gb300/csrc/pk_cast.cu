@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "../../include/pike.h"
@@ -215,6 +216,160 @@ extern "C" int pk_cast_rays_noalloc(pk_ctx* c, const float* ray_o4, const float*
     check(cudaMemcpyAsync(&err, s.tickets + 2, 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "sync");
     if (err) { c->err = "pk_cast_rays_noalloc: device error flags"; return PK_ERR_DEVICE; }
+    return PK_OK;
+  } catch (CudaError& e) {
+    c->err = e.what();
+    return PK_ERR_CUDA;
+  }
+}
+
+// ---- autofocus distance --------------------------------------------------------
+// Raycaster.cast (render/raycaster.js:13-131): one ray traversed in double
+// precision over the exact (unquantised) node bounds and normalised triangles,
+// Möller-Trumbore with epsilon 1e-12, MAX_T = 1e6.  The recursion is kept as
+// an explicit stack: closestNode orders the two children by entry distance,
+// and each is entered only if its distance is below the closest hit found so
+// far when its turn comes.  Math.min / Math.max propagate NaN, so a slab with
+// 0 * inf culls the box exactly as the reference does.
+namespace pk {
+namespace {
+
+__device__ __forceinline__ double jmin(double a, double b) {
+  return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000ll) : (a < b ? a : (b < a ? b : (signbit(a) ? a : b)));
+}
+__device__ __forceinline__ double jmax(double a, double b) {
+  return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000ll) : (a > b ? a : (b > a ? b : (signbit(a) ? b : a)));
+}
+
+struct FocusScene {
+  const double* pos3;
+  const int32_t* nodes5;
+  const double* box6;
+  const int4* tri4_leaf;
+  double cx, cy, cz, s;
+};
+
+__device__ __forceinline__ double focus_box(const FocusScene& f, int node, const double* o, const double* inv) {
+  const double* b = f.box6 + 6 * (size_t)node;
+  const double c[3] = {f.cx, f.cy, f.cz};
+  double t1[3], t2[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double mn = (b[a] - c[a]) * f.s, mx = (b[3 + a] - c[a]) * f.s;
+    t1[a] = (mn - o[a]) * inv[a];
+    t2[a] = (mx - o[a]) * inv[a];
+  }
+  double tmin = jmin(t1[0], t2[0]), tmax = jmax(t1[0], t2[0]);
+  tmin = jmax(tmin, jmin(t1[1], t2[1]));
+  tmax = jmin(tmax, jmax(t1[1], t2[1]));
+  tmin = jmax(tmin, jmin(t1[2], t2[2]));
+  tmax = jmin(tmax, jmax(t1[2], t2[2]));
+  return (tmax >= tmin && tmax >= 0.0) ? tmin : 1000000.0;
+}
+
+__device__ __forceinline__ double focus_tri(const FocusScene& f, const int4 t4, const double* o, const double* d) {
+  const double eps = 0.000000000001;
+  double v[3][3];
+  const int ids[3] = {t4.x, t4.y, t4.z};
+  const double c[3] = {f.cx, f.cy, f.cz};
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int a = 0; a < 3; a++) v[k][a] = (f.pos3[3 * (size_t)ids[k] + a] - c[a]) * f.s;
+  double e1[3], e2[3], tv[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) { e1[a] = v[1][a] - v[0][a]; e2[a] = v[2][a] - v[0][a]; tv[a] = o[a] - v[0][a]; }
+  const double p[3] = {d[1] * e2[2] - d[2] * e2[1], -(d[0] * e2[2] - d[2] * e2[0]), d[0] * e2[1] - d[1] * e2[0]};
+  const double det = 0.0 + e1[0] * p[0] + e1[1] * p[1] + e1[2] * p[2];
+  if (det > -eps && det < eps) return 1000000.0;
+  const double inv = 1.0 / det;
+  const double u = (0.0 + tv[0] * p[0] + tv[1] * p[1] + tv[2] * p[2]) * inv;
+  if (u < 0.0 || u > 1.0) return 1000000.0;
+  const double q[3] = {tv[1] * e1[2] - tv[2] * e1[1], -(tv[0] * e1[2] - tv[2] * e1[0]), tv[0] * e1[1] - tv[1] * e1[0]};
+  const double vv = (0.0 + d[0] * q[0] + d[1] * q[1] + d[2] * q[2]) * inv;
+  if (vv < 0.0 || u + vv > 1.0) return 1000000.0;
+  const double t = (0.0 + e2[0] * q[0] + e2[1] * q[1] + e2[2] * q[2]) * inv;
+  return t > eps ? t : 1000000.0;
+}
+
+constexpr int FOCUS_STACK = 96;
+
+__global__ void k_focus(FocusScene f, const double* __restrict__ rays6, uint32_t n, double* __restrict__ t_out,
+                        uint32_t* __restrict__ err) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const double o[3] = {rays6[6 * r], rays6[6 * r + 1], rays6[6 * r + 2]};
+  const double d[3] = {rays6[6 * r + 3], rays6[6 * r + 4], rays6[6 * r + 5]};
+  const double inv[3] = {1.0 / d[0], 1.0 / d[1], 1.0 / d[2]};
+  int stack_node[FOCUS_STACK];
+  double stack_t[FOCUS_STACK];
+  int sp = 0;
+  double closest = 1000000.0;
+  // the root is entered unconditionally (cast -> traverse(root, MAX_T))
+  stack_node[sp] = 0;
+  stack_t[sp] = -__longlong_as_double(0x7ff0000000000000ll);
+  sp++;
+  bool first = true;
+  while (sp > 0) {
+    --sp;
+    const int node = stack_node[sp];
+    if (!first && !(stack_t[sp] < closest)) continue;
+    first = false;
+    const int32_t* nd = f.nodes5 + 5 * (size_t)node;
+    if (nd[1] > -1) {  // leaf: processLeaf returns the leaf's own minimum
+      const int size = nd[1] >> 24, base = nd[1] & 0x00ffffff;
+      double res = 1000000.0;
+      for (int i = 0; i < size; i++) {
+        const double x = focus_tri(f, f.tri4_leaf[base + i], o, d);
+        if (x < res) res = x;
+      }
+      closest = jmin(res, closest);
+      continue;
+    }
+    const int l = nd[0], rr = nd[0] + 1;
+    const double tl = focus_box(f, l, o, inv), tr = focus_box(f, rr, o, inv);
+    // closestNode: a child whose box is missed is dropped; the nearer one goes first
+    const int ln = tl < 1000000.0 ? l : -1, rn = tr < 1000000.0 ? rr : -1;
+    int o0, o1;
+    double t0, t1;
+    if (tl < tr) { o0 = ln; t0 = tl; o1 = rn; t1 = tr; } else { o0 = rn; t0 = tr; o1 = ln; t1 = tl; }
+    if (sp + 2 > FOCUS_STACK) { atomicOr(err, 1u); break; }
+    if (o1 >= 0) { stack_node[sp] = o1; stack_t[sp] = t1; sp++; }
+    if (o0 >= 0) { stack_node[sp] = o0; stack_t[sp] = t0; sp++; }
+  }
+  t_out[r] = closest;
+}
+
+}  // namespace
+}  // namespace pk
+
+extern "C" int pk_focus_distance(pk_ctx* c, const double origin[3], const double dir[3], double* t_out,
+                                 double* focal_depth_out) {
+  if (!c) return PK_ERR_ARG;
+  try {
+    check(cudaSetDevice(c->device), "cudaSetDevice");
+    if (!c->bvh_ready || !c->node_box_d.p || c->norm[3] == 0.0) {
+      c->err = "pk_focus_distance: needs a BVH built by pk_bvh_build (its exact node bounds)";
+      return PK_ERR_STATE;
+    }
+    if (!origin || !dir || !t_out) { c->err = "pk_focus_distance: null argument"; return PK_ERR_ARG; }
+    const double ray[6] = {origin[0], origin[1], origin[2], dir[0], dir[1], dir[2]};
+    DevBuf<double> dray(6), dt(1);
+    DevBuf<uint32_t> err(1);
+    check(cudaMemsetAsync(err.p, 0, 4, c->stream), "memset");
+    check(cudaMemcpyAsync(dray.p, ray, sizeof ray, cudaMemcpyHostToDevice, c->stream), "H2D");
+    const FocusScene f{c->pos.p, c->nodes5.p, c->node_box_d.p, reinterpret_cast<const int4*>(c->tri4_leaf.p),
+                       c->norm[0], c->norm[1], c->norm[2], c->norm[3]};
+    k_focus<<<1, 32, 0, c->stream>>>(f, dray.p, 1, dt.p, err.p);
+    check(cudaGetLastError(), "k_focus");
+    double t = 0.0;
+    uint32_t e = 0;
+    check(cudaMemcpyAsync(&t, dt.p, 8, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaMemcpyAsync(&e, err.p, 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
+    if (e) { c->err = "pk_focus_distance: traversal stack overflow"; return PK_ERR_DEVICE; }
+    *t_out = t;
+    if (focal_depth_out) *focal_depth_out = 1.0 - 1.0 / t;  // PikeRenderer.focusCamera (pike.js:88-90)
     return PK_OK;
   } catch (CudaError& e) {
     c->err = e.what();

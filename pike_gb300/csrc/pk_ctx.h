@@ -78,6 +78,7 @@ struct pk_ctx {
   DevBuf<int4> tri4_leaf;
   DevBuf<float4> verts4, inner, tris;
   DevBuf<int4> inner32;
+  DevBuf<double> node_box_d;  // exact double node bounds (pk_bvh_build only)
   bool compact_nodes = false;  // traverse 32-byte records (same boxes as the 64-byte ones)
   int root = 0;
   bool bvh_ready = false;

@@ -1,4 +1,4 @@
-// pk_host_tables.h -- small host-side tables built once at scene load.
+// pk_host_tables.h -- the material table, built on the host once per scene (as the reference does).
 #pragma once
 #include <cstdint>
 #include <string>
@@ -13,13 +13,5 @@ namespace pk {
 // mats9: base r,g,b,a, roughness, metallic, emissive r,g,b per material.
 void build_material_layers(const double* mats9, uint32_t n_mats, std::vector<int32_t>& index4,
                            std::vector<uint8_t>& layers_rgba8);
-
-// EnvironmentGenerator tables (env_sampler.js:43-157).
-struct EnvHostTables {
-  std::vector<int32_t> bins2;
-  std::vector<int32_t> coords2;
-  std::vector<float> pdf;
-};
-int build_env_tables(const uint8_t* rgbe, uint32_t w, uint32_t h, EnvHostTables& out, std::string& why);
 
 }  // namespace pk

@@ -53,4 +53,8 @@ void scan_exclusive_u32(cudaStream_t s, const uint32_t* in, uint32_t* out, uint3
 void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64_t* keys_tmp, uint32_t* vals_tmp,
                           uint32_t n, int bits);
 
+// EnvironmentGenerator tables on the GPU (pk_env.cu).
+int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
+                         uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why);
+
 }  // namespace pk

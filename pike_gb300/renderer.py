@@ -75,6 +75,22 @@ class PikeRenderer:
         self.postProcessPass.generateCommands(enc)
         self.device.queue.submit([enc.finish()])
 
+    def focusCamera(self) -> float:
+        """pike.js:88-90: focalDepth = 1 - 1/t of the camera ray's closest hit
+        (Raycaster.cast, double precision; see pk_focus_distance)."""
+        import ctypes as C
+        o = (C.c_double * 3)(*self.camera["pos"])
+        d = (C.c_double * 3)(*self.camera["dir"])
+        t, fd = C.c_double(0.0), C.c_double(0.0)
+        self.device.ctx.call("pk_focus_distance", o, d, C.byref(t), C.byref(fd))
+        self.camera["focalDepth"] = fd.value
+        return fd.value
+
+    def savePNG(self, path: str) -> None:
+        """The tonemapped frame (PostProcessPass output) as an 8-bit PNG."""
+        from .image import write_png
+        write_png(path, self.image()[1][..., :3])
+
     def counters(self) -> dict:
         return read_counters(self.device.ctx)
 

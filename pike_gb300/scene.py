@@ -63,6 +63,12 @@ class EnvironmentGenerator:
         self.height, self.width = self.img.shape[:2]
         self.device = None
 
+    @classmethod
+    def fromFile(cls, path: str) -> "EnvironmentGenerator":
+        """An RGBE PNG (what the reference loads) or a Radiance .hdr file."""
+        from .envmap import load_env
+        return cls(load_env(path))
+
     def upload(self, device):
         device.ctx.call("pk_env_build", ptr(self.img), self.width, self.height)
         self.device = device

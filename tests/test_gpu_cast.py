@@ -62,3 +62,26 @@ def test_cast_rays_empty_and_tiny(oracle, pk_built):
         ref = pair.P.r.trace_rays(np.concatenate([o, d], axis=1))
         assert np.array_equal(hits[:, 1], ref[:, 1])
         assert np.array_equal(idx, np.flatnonzero(ref[:, 1] != 0xFFFFFFFF).astype(np.uint32))
+
+
+def test_focus_distance_matches_raycaster(oracle, pk_built):
+    """pk_focus_distance (double-precision autofocus cast) equals the oracle's
+    Raycaster.cast restatement bit for bit, and focalDepth = 1 - 1/t."""
+    src = synth.displaced_sphere_scene(subdivisions=5, width=16, height=16, env_size=(64, 32))
+    pair = Pair(src, oracle)
+    rng = np.random.default_rng(9)
+    rays = np.zeros((64, 6))
+    rays[:, :3] = rng.uniform(-0.9, 0.9, (64, 3))
+    v = rng.normal(size=(64, 3))
+    rays[:, 3:] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    st = src.camera_state()
+    rays[0] = [*st["pos"], *st["dir"]]
+    want = pair.P.bvh.cast(rays)
+    for i in range(rays.shape[0]):
+        o = (C.c_double * 3)(*rays[i, :3])
+        d = (C.c_double * 3)(*rays[i, 3:])
+        t, fd = C.c_double(0.0), C.c_double(0.0)
+        pair.ctx.call("pk_focus_distance", o, d, C.byref(t), C.byref(fd))
+        assert np.float64(t.value).view(np.uint64) == np.float64(want[i]).view(np.uint64), i
+        assert fd.value == 1.0 - 1.0 / t.value
+    assert (want < 1e6).any() and (want == 1e6).any()

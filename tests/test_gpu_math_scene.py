@@ -92,10 +92,21 @@ def test_materials_match_oracle(ctx, oracle):
     assert np.array_equal(layers, layers_o)
 
 
-@pytest.mark.parametrize("size", [(64, 32), (2048, 1024)])
+@pytest.mark.parametrize("size", [(64, 32), (2048, 1024), "constant", "banded"])
 def test_env_tables_match_oracle(ctx, oracle, size):
-    w, h = size
-    rgbe = synth.rgbe_encode(synth.hdr_env(1234, w, h))
+    """GPU env tables (radiance, stable descending sort, sequential bin walk,
+    pdf) equal env_sampler.js's, including environments full of equal texels."""
+    if size == "constant":
+        w, h = 64, 32
+        rgbe = np.zeros((h, w, 4), np.uint8)
+        rgbe[...] = (255, 255, 255, 128)
+    elif size == "banded":
+        w, h = 300, 150
+        rgbe = synth.rgbe_encode(synth.hdr_env(77, w, h, sun=500.0))
+        rgbe[::3] = rgbe[0, 0]
+    else:
+        w, h = size
+        rgbe = synth.rgbe_encode(synth.hdr_env(1234, w, h))
     env = oracle.Env(rgbe)
     ctx.call("pk_env_build", ptr(rgbe), w, h)
     ww, hh, nb = (np.zeros(1, np.uint32) for _ in range(3))
