@@ -85,6 +85,13 @@ int pk_configure(pk_ctx* ctx, uint32_t width, uint32_t height, uint32_t batch_si
 int pk_scene_flatten(pk_ctx* ctx, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
                      uint32_t n_verts, const int32_t* tri4, uint32_t n_tris, double scale,
                      const double translate[3]);
+/* The same for props whose transforms rotate (scene.js:83-93): the host has
+ * applied the glTF node matrices and the prop's rotate/scale/translate.
+ * pos3 are final positions (used as is), nrm3/tan4 the rotated normal and
+ * tangent (tan4.w unused), and bn3/bt4 the normal and signed tangent before
+ * the prop's rotations, from which scene.js:160 builds the bitangent. */
+int pk_scene_flatten_tbn(pk_ctx* ctx, const double* pos3, const double* nrm3, const double* tan4, const double* bn3,
+                         const double* bt4, const double* uv2, uint32_t n_verts, const int32_t* tri4, uint32_t n_tris);
 /* Upload already-flattened scene tables (scene.indices / scene.attributes). */
 int pk_scene_upload(pk_ctx* ctx, const int32_t* tri4, uint32_t n_tris, const double* pos3, const uint32_t* attr4,
                     uint32_t n_verts);
@@ -98,7 +105,13 @@ int pk_materials_set(pk_ctx* ctx, const double* mats9, uint32_t n_mats);
  * (MaterialIndexStruct, structs.js:251-260) and 1x1 rgba8 atlas layers. */
 int pk_materials_upload(pk_ctx* ctx, const int32_t* mat4, uint32_t n_mats, const uint8_t* layers_rgba8,
                         uint32_t n_layers);
-/* n_layers, then mat4 (n_mats*4) and layers (n_layers*4 bytes); either pointer may be NULL. */
+/* Textured atlas (TexturePacker.getPixels, texture_packer.js:121-136): n_layers
+ * rgba8 layers of res x res texels, row-major, sampled by the shading pass with
+ * textureSampleLevel's linear filter and repeat addressing (shade_hit.wgsl:
+ * 184-197).  Replaces the layers of pk_materials_set/upload; material indices
+ * stay as uploaded. */
+int pk_atlas_upload(pk_ctx* ctx, const uint8_t* layers, uint32_t res, uint32_t n_layers);
+/* n_layers, then mat4 (n_mats*4) and layers (n_layers*4 bytes, 1x1 layers only); either pointer may be NULL. */
 int pk_materials_download(pk_ctx* ctx, uint32_t* n_mats, uint32_t* n_layers, int32_t* mat4, uint8_t* layers_rgba8);
 
 /* ---- BVH (rows BVH and Q) ----------------------------------------------

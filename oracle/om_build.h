@@ -73,11 +73,15 @@ static inline uint32_t quantize_vec2_to_int(double a, double b) {
   return (uint32_t)(uint16_t)s0 | ((uint32_t)(uint16_t)s1 << 16);
 }
 
-// One vertex of scene.js:458-470 with a transform {scale, translate} and no
-// rotations (rotations use Math.sin/cos, which no test of the reference pins).
+// One vertex of scene.js:458-470 with a transform {scale, translate}.  The
+// bitangent is built from bn/bt4, the normal and signed tangent before the
+// prop's rotations (scene.js:160); without rotations they are nrm and tan4.
 struct FlatVertex { double pos[3]; uint32_t tangent, bitangent, normal, uv; };
 static inline FlatVertex flatten_vertex(const double* pos, const double* nrm, const double* tan4,
-                                        const double* uv, double scale_, const double* translate) {
+                                        const double* uv, double scale_, const double* translate,
+                                        const double* bn = nullptr, const double* bt4 = nullptr) {
+  if (!bn) bn = nrm;
+  if (!bt4) bt4 = tan4;
   FlatVertex fv;
   for (int i = 0; i < 3; i++) fv.pos[i] = pos[i] * scale_ + translate[i];
   double normal[3], tangent[3];
@@ -85,10 +89,10 @@ static inline FlatVertex flatten_vertex(const double* pos, const double* nrm, co
   for (int i = 0; i < 3; i++) tangent[i] = tan4[i] * 1.0 + 0.0;
   // Vec3.cross(normalAt, tangentAt): y = -(a0*b2 - a2*b0)
   double c[3];
-  c[0] = nrm[1] * tan4[2] - nrm[2] * tan4[1];
-  c[1] = -(nrm[0] * tan4[2] - nrm[2] * tan4[0]);
-  c[2] = nrm[0] * tan4[1] - nrm[1] * tan4[0];
-  double w = tan4[3];
+  c[0] = bn[1] * bt4[2] - bn[2] * bt4[1];
+  c[1] = -(bn[0] * bt4[2] - bn[2] * bt4[0]);
+  c[2] = bn[0] * bt4[1] - bn[1] * bt4[0];
+  double w = bt4[3];
   double sgn = (w != 0.0 && w == w) ? w : 1.0;  // signedTangent[3] || 1
   for (int i = 0; i < 3; i++) c[i] = c[i] * sgn;
   double bt[3], tn[3], nn[3];

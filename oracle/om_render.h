@@ -82,7 +82,8 @@ struct Renderer {
   std::vector<float> verts4;
   std::vector<uint32_t> attrs4;
   std::vector<int32_t> mat4;
-  std::vector<uint8_t> layers;   // rgba8, 1x1 per layer
+  std::vector<uint8_t> layers;   // rgba8, atlas_res x atlas_res per layer
+  int32_t atlas_res = 1;
   // env
   uint32_t env_w = 0, env_h = 0;
   std::vector<uint8_t> env_rgbe;
@@ -294,11 +295,33 @@ struct Renderer {
     float metallic, opacity, alpha;
   };
   struct Sample { V3 wi; float pdf; };
-  // textureSampleLevel on a 1x1 rgba8unorm layer: every tap is the one texel.
-  void texel(int32_t layer, float* c) const {
-    const int32_t nl = (int32_t)(layers.size() / 4);
-    int32_t l = layer < 0 ? 0 : (layer >= nl ? nl - 1 : layer);
-    for (int i = 0; i < 4; i++) c[i] = (float)layers[4 * (size_t)l + i] / 255.0f;
+  // textureSampleLevel(atlas, linear sampler with repeat addressing, uv, layer, 0)
+  // on rgba8unorm layers (shade_hit.wgsl:184-197; sampler: shade_hit_pass.js:83-90).
+  // A 1x1 layer returns its texel.  Larger layers filter bilinearly: texel
+  // space x = u*R - 0.5, i0 = floor(x), fx = x - i0, indices wrap, and
+  // mix(mix(t00, t10, fx), mix(t01, t11, fx), fy) with mix(a,b,t) = a(1-t) + bt.
+  void texel_at(int32_t l, int32_t i, int32_t j, float* c) const {
+    const int32_t R = atlas_res;
+    i = ((i % R) + R) % R;
+    j = ((j % R) + R) % R;
+    const uint8_t* p = &layers[4 * (((size_t)l * R + (size_t)j) * R + (size_t)i)];
+    for (int k = 0; k < 4; k++) c[k] = (float)p[k] / 255.0f;
+  }
+  void texel(int32_t layer, float u, float v, float* c) const {
+    const int32_t R = atlas_res;
+    const int32_t nl = (int32_t)(layers.size() / (4 * (size_t)R * R));
+    const int32_t l = layer < 0 ? 0 : (layer >= nl ? nl - 1 : layer);
+    if (R == 1) { texel_at(l, 0, 0, c); return; }
+    const float x = u * (float)R - 0.5f, y = v * (float)R - 0.5f;
+    const float x0 = std::floor(x), y0 = std::floor(y);
+    const float fx = x - x0, fy = y - y0;
+    const int32_t i0 = f2i(x0), j0 = f2i(y0);
+    float t00[4], t10[4], t01[4], t11[4];
+    texel_at(l, i0, j0, t00);
+    texel_at(l, i0 + 1, j0, t10);
+    texel_at(l, i0, j0 + 1, t01);
+    texel_at(l, i0 + 1, j0 + 1, t11);
+    for (int k = 0; k < 4; k++) c[k] = mix1(mix1(t00[k], t10[k], fx), mix1(t01[k], t11[k], fx), fy);
   }
   static void onb(V3 n, V3* b1, V3* b2) {
     float sign = n.z > 0.0f ? 1.0f : -1.0f;
@@ -327,23 +350,24 @@ struct Renderer {
     V3 T = normalize(matvec(tg[0], tg[1], tg[2], bary));
     V3 Bt = normalize(matvec(bt[0], bt[1], bt[2], bary));
     V3 N = normalize(matvec(nm[0], nm[1], nm[2], bary));
-    (void)uvx; (void)uvy;  // uv = uvs * bary is only used to address 1x1 layers
+    const float tu = uvx[0] * bary.x + uvx[1] * bary.y + uvx[2] * bary.z;  // uvs * bary (mat3x2 * vec3)
+    const float tv = uvy[0] * bary.x + uvy[1] * bary.y + uvy[2] * bary.z;
     const int32_t* mat = &mat4[4 * (size_t)tri[3]];
     float nrm[4], dif[4], mr[4], em[4];
-    texel(mat[2], nrm);
+    texel(mat[2], tu, tv, nrm);
     V3 map_normal = mul(sub(v3(nrm[0], nrm[1], nrm[2]), v3(0.5f, 0.5f, 0.0f)), v3(2.0f, 2.0f, 1.0f));
     si.normal = normalize(matvec(T, Bt, N, map_normal));
     si.origin = add(ro, scale(rd, hit.t - 1e-7f * 40.0f));
     si.n = si.normal;
     onb(si.normal, &si.b1, &si.b2);
     si.wo = vecmat(neg(rd), si.b1, si.b2, si.n);
-    texel(mat[0], dif);
+    texel(mat[0], tu, tv, dif);
     si.base = v3(dif[0], dif[1], dif[2]);
     si.opacity = dif[3];
-    texel(mat[1], mr);
+    texel(mat[1], tu, tv, mr);
     si.metallic = mr[2];
     si.alpha = mr[1] * mr[1];
-    texel(mat[3], em);
+    texel(mat[3], tu, tv, em);
     si.emission = v3(em[0], em[1], em[2]);
     si.spec = v3(mix1(1.0f, si.base.x, si.metallic), mix1(1.0f, si.base.y, si.metallic), mix1(1.0f, si.base.z, si.metallic));
     return si;

@@ -38,6 +38,22 @@ int or_flatten(const double* pos3, const double* nrm3, const double* tan4, const
   return 0;
 }
 
+// pk_scene_flatten_tbn: final positions, rotated normal/tangent, bitangent sources.
+int or_flatten_tbn(const double* pos3, const double* nrm3, const double* tan4, const double* bn3, const double* bt4,
+                   const double* uv2, size_t n, double* pos_out3, uint32_t* attr_out4) {
+  const double zero[3] = {0.0, 0.0, 0.0};
+  for (size_t i = 0; i < n; i++) {
+    FlatVertex fv = flatten_vertex(pos3 + 3 * i, nrm3 + 3 * i, tan4 + 4 * i, uv2 + 2 * i, 1.0, zero, bn3 + 3 * i,
+                                   bt4 + 4 * i);
+    for (int k = 0; k < 3; k++) pos_out3[3 * i + k] = fv.pos[k];
+    attr_out4[4 * i + 0] = fv.tangent;
+    attr_out4[4 * i + 1] = fv.bitangent;
+    attr_out4[4 * i + 2] = fv.normal;
+    attr_out4[4 * i + 3] = fv.uv;
+  }
+  return 0;
+}
+
 // Row M: materials {r,g,b,a, roughness, metallic, er,eg,eb} -> index table + 1x1 layers.
 int or_materials(const double* mats9, size_t n_mats, int32_t* index_out4, uint8_t* layers_out,
                  size_t max_layers, size_t* n_layers_out) {
@@ -139,6 +155,14 @@ int or_set_scene(void* p, const int32_t* nodes5, size_t n_nodes, const int32_t* 
   r->attrs4.assign(attrs4, attrs4 + 4 * n_verts);
   r->mat4.assign(mat4, mat4 + 4 * n_mats);
   r->layers.assign(layers, layers + 4 * n_layers);
+  r->atlas_res = 1;
+  return 0;
+}
+// Replace the 1x1 layers with res x res rgba8 atlas layers.
+int or_set_atlas(void* p, const uint8_t* layers, uint32_t res, size_t n_layers) {
+  Renderer* r = (Renderer*)p;
+  r->layers.assign(layers, layers + 4 * (size_t)res * res * n_layers);
+  r->atlas_res = (int32_t)res;
   return 0;
 }
 int or_set_env(void* p, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32_t* bins2, size_t nb,

@@ -72,6 +72,16 @@ def flatten(src, scale: float = 1.0, translate=(0.0, 0.0, 0.0)):
     return pos_out, attrs
 
 
+def flatten_tbn(pos, nrm, tan4, bn, bt4, uv):
+    """pk_scene_flatten_tbn restated: (pos f64 (V,3), attrs u32 (V,4))."""
+    arrs = [np.ascontiguousarray(a, np.float64) for a in (pos, nrm, tan4, bn, bt4, uv)]
+    n = arrs[0].shape[0]
+    pos_out = np.zeros((n, 3), np.float64)
+    attrs = np.zeros((n, 4), np.uint32)
+    lib().or_flatten_tbn(*[_p(a) for a in arrs], C.c_size_t(n), _p(pos_out), _p(attrs))
+    return pos_out, attrs
+
+
 def materials(mats9: np.ndarray):
     """Row M: returns (index table i32 (M,4), layers u8 (L,4))."""
     L = lib()
@@ -172,6 +182,12 @@ class Renderer:
         n, t, v, a, m, l = self._keep
         lib().or_set_scene(self.p, _p(n), C.c_size_t(n.shape[0]), _p(t), C.c_size_t(t.shape[0]), _p(v),
                            C.c_size_t(v.shape[0]), _p(a), _p(m), C.c_size_t(m.shape[0]), _p(l), C.c_size_t(l.shape[0]))
+
+    def set_atlas(self, layers: np.ndarray):
+        """(n, res, res, 4) uint8 atlas layers in place of the 1x1 colour layers."""
+        self._atlas = np.ascontiguousarray(layers, np.uint8)
+        n, res = self._atlas.shape[0], self._atlas.shape[1]
+        lib().or_set_atlas(self.p, _p(self._atlas), C.c_uint32(res), C.c_size_t(n))
 
     def set_env(self, env: Env):
         lib().or_set_env(self.p, _p(env.rgbe), C.c_uint32(env.w), C.c_uint32(env.h), _p(env.bins),

@@ -59,9 +59,10 @@ def load(path: str = LIB_PATH):
         "pk_create": [C.POINTER(_P), C.c_int], "pk_destroy": [_P], "pk_version": [],
         "pk_configure": [_P, u32, u32, u32],
         "pk_scene_flatten": [_P, _P, _P, _P, _P, u32, _P, u32, f64, _P],
+        "pk_scene_flatten_tbn": [_P, _P, _P, _P, _P, _P, _P, u32, _P, u32],
         "pk_scene_upload": [_P, _P, u32, _P, _P, u32], "pk_scene_download": [_P, _P, _P],
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
-        "pk_materials_download": [_P, _P, _P, _P, _P],
+        "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],
         "pk_bvh_info": [_P, _P, _P, _P], "pk_bvh_download": [_P, _P, _P, _P],
         "pk_env_build": [_P, _P, u32, u32], "pk_env_upload": [_P, _P, u32, u32, _P, u32, _P, _P],

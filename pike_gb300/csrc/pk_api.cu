@@ -150,22 +150,27 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
 }
 
 // ---------------- scene ----------------
-int pk_scene_flatten(pk_ctx* c, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
-                     uint32_t n_verts, const int32_t* tri4, uint32_t n_tris, double scale, const double translate[3]) {
+namespace {
+int flatten_impl(pk_ctx* c, const double* pos3, const double* nrm3, const double* tan4, const double* bn3,
+                 const double* bt4, const double* uv2, uint32_t n_verts, const int32_t* tri4, uint32_t n_tris,
+                 double scale, const double translate[3]) {
   return guarded(c, [&]() {
     if (!pos3 || !nrm3 || !tan4 || !uv2 || !tri4 || !n_verts || !n_tris) return fail(c, PK_ERR_ARG, "empty scene");
     for (uint32_t t = 0; t < n_tris; t++)
       for (int k = 0; k < 3; k++)
         if (tri4[4 * t + k] < 0 || (uint32_t)tri4[4 * t + k] >= n_verts) return fail(c, PK_ERR_ARG, "vertex index out of range");
-    DevBuf<double> p, n, t, u;
+    DevBuf<double> p, n, t, u, bn, bt;
     upload(p, pos3, 3 * (size_t)n_verts, c->stream);
     upload(n, nrm3, 3 * (size_t)n_verts, c->stream);
     upload(t, tan4, 4 * (size_t)n_verts, c->stream);
     upload(u, uv2, 2 * (size_t)n_verts, c->stream);
+    if (bn3) upload(bn, bn3, 3 * (size_t)n_verts, c->stream);
+    if (bt4) upload(bt, bt4, 4 * (size_t)n_verts, c->stream);
     c->pos.alloc(3 * (size_t)n_verts);
     c->attrs.alloc(n_verts);
     const double tr[3] = {translate ? translate[0] : 0.0, translate ? translate[1] : 0.0, translate ? translate[2] : 0.0};
-    launch_flatten(c->stream, p.p, n.p, t.p, u.p, n_verts, scale, tr[0], tr[1], tr[2], c->pos.p, c->attrs.p);
+    launch_flatten(c->stream, p.p, n.p, t.p, bn3 ? bn.p : n.p, bt4 ? bt.p : t.p, u.p, n_verts, scale, tr[0], tr[1],
+                   tr[2], c->pos.p, c->attrs.p);
     check(cudaGetLastError(), "k_flatten");
     upload(c->tri4, tri4, n_tris, c->stream);
     check(cudaStreamSynchronize(c->stream), "sync");
@@ -175,6 +180,19 @@ int pk_scene_flatten(pk_ctx* c, const double* pos3, const double* nrm3, const do
     c->invalidate_graph();
     return PK_OK;
   });
+}
+}  // namespace
+
+int pk_scene_flatten(pk_ctx* c, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
+                     uint32_t n_verts, const int32_t* tri4, uint32_t n_tris, double scale, const double translate[3]) {
+  return flatten_impl(c, pos3, nrm3, tan4, nullptr, nullptr, uv2, n_verts, tri4, n_tris, scale, translate);
+}
+
+int pk_scene_flatten_tbn(pk_ctx* c, const double* pos3, const double* nrm3, const double* tan4, const double* bn3,
+                         const double* bt4, const double* uv2, uint32_t n_verts, const int32_t* tri4, uint32_t n_tris) {
+  if (c && (!bn3 || !bt4)) return fail(c, PK_ERR_ARG, "bitangent sources missing");
+  const double zero[3] = {0.0, 0.0, 0.0};
+  return flatten_impl(c, pos3, nrm3, tan4, bn3, bt4, uv2, n_verts, tri4, n_tris, 1.0, zero);
 }
 
 int pk_scene_upload(pk_ctx* c, const int32_t* tri4, uint32_t n_tris, const double* pos3, const uint32_t* attr4,
@@ -217,6 +235,7 @@ int pk_materials_set(pk_ctx* c, const double* mats9, uint32_t n_mats) {
     check(cudaStreamSynchronize(c->stream), "sync");
     c->n_mats = n_mats;
     c->n_layers = (uint32_t)(layers.size() / 4);
+    c->atlas_res = 1;
     c->invalidate_graph();
     return PK_OK;
   });
@@ -230,6 +249,20 @@ int pk_materials_upload(pk_ctx* c, const int32_t* mat4, uint32_t n_mats, const u
     check(cudaStreamSynchronize(c->stream), "sync");
     c->n_mats = n_mats;
     c->n_layers = n_layers;
+    c->atlas_res = 1;
+    c->invalidate_graph();
+    return PK_OK;
+  });
+}
+
+int pk_atlas_upload(pk_ctx* c, const uint8_t* layers, uint32_t res, uint32_t n_layers) {
+  return guarded(c, [&]() {
+    if (!layers || !res || !n_layers || res > 16384) return fail(c, PK_ERR_ARG, "bad atlas");
+    if ((uint64_t)res * res * n_layers >= (1ull << 32)) return fail(c, PK_ERR_ARG, "atlas too large");
+    upload(c->layers, layers, (size_t)res * res * n_layers, c->stream);
+    check(cudaStreamSynchronize(c->stream), "sync");
+    c->n_layers = n_layers;
+    c->atlas_res = res;
     c->invalidate_graph();
     return PK_OK;
   });
@@ -240,7 +273,8 @@ int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32
     if (n_mats) *n_mats = c->n_mats;
     if (n_layers) *n_layers = c->n_layers;
     if (mat4 && c->n_mats) check(cudaMemcpyAsync(mat4, c->mat4.p, c->mat4.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
-    if (layers && c->n_layers) check(cudaMemcpyAsync(layers, c->layers.p, c->layers.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (layers && c->n_layers && c->atlas_res == 1)
+      check(cudaMemcpyAsync(layers, c->layers.p, c->layers.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
     check(cudaStreamSynchronize(c->stream), "sync");
     return PK_OK;
   });

@@ -68,7 +68,7 @@ struct pk_ctx {
   DevBuf<double> pos;
   DevBuf<uint4> attrs;
   DevBuf<int4> tri4;
-  uint32_t n_mats = 0, n_layers = 0;
+  uint32_t n_mats = 0, n_layers = 0, atlas_res = 1;
   DevBuf<int4> mat4;
   DevBuf<uchar4> layers;
   // bvh
@@ -112,7 +112,7 @@ struct pk_ctx {
     L.ctr = ctr.p;
     L.cam = cam.p;
     L.scene = pk::SceneDev{inner.p, compact_nodes ? inner32.p : nullptr, tris.p, tri4_leaf.p, attrs.p, mat4.p,
-                           layers.p, (int)n_layers, root,
+                           layers.p, (int)n_layers, (int)atlas_res, root,
                        n_leaf_tris, n_verts, n_mats};
     L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
     L.color = color.p;

@@ -64,8 +64,9 @@ struct SceneDev {
   const int4* tri4;        // leaf-ordered {i0, i1, i2, matId}
   const uint4* attrs;      // per-vertex {tangent, bitangent, normal (snorm8x4), uv (snorm16x2)}
   const int4* mat4;        // per-material atlas layers {diff, metRough, norm, emit}
-  const uchar4* layers;    // 1x1 rgba8 atlas layers
+  const uchar4* layers;    // rgba8 atlas layers, atlas_res x atlas_res each
   int n_layers;
+  int atlas_res;
   int root;                // child code of the root
   uint32_t n_tris;         // leaf-ordered triangles
   uint32_t n_verts;        // vertex attributes

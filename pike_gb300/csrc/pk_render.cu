@@ -380,10 +380,28 @@ struct Sample {
   V3 wi;
   float pdf;
 };
-__device__ __forceinline__ float4 texel(const SceneDev& sc, int layer) {
-  const int l = layer < 0 ? 0 : (layer >= sc.n_layers ? sc.n_layers - 1 : layer);
-  const uchar4 t = sc.layers[l];
+__device__ __forceinline__ float4 texel_at(const SceneDev& sc, int l, int i, int j) {
+  const int R = sc.atlas_res;
+  i = ((i % R) + R) % R;
+  j = ((j % R) + R) % R;
+  const uchar4 t = __ldg(sc.layers + ((size_t)l * R + (size_t)j) * R + (size_t)i);
   return make_float4((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f, (float)t.w / 255.0f);
+}
+// textureSampleLevel(atlas, linear + repeat sampler, uv, layer, 0) on rgba8unorm
+// layers (shade_hit.wgsl:184-197): a 1x1 layer returns its texel; larger ones
+// filter bilinearly around x = u*R - 0.5 with mix(a, b, t) = a(1-t) + bt.
+__device__ __forceinline__ float4 texel(const SceneDev& sc, int layer, float u, float v) {
+  const int l = layer < 0 ? 0 : (layer >= sc.n_layers ? sc.n_layers - 1 : layer);
+  const int R = sc.atlas_res;
+  if (R == 1) return texel_at(sc, l, 0, 0);
+  const float x = u * (float)R - 0.5f, y = v * (float)R - 0.5f;
+  const float x0 = floorf(x), y0 = floorf(y);
+  const float fx = x - x0, fy = y - y0;
+  const int i0 = f2i(x0), j0 = f2i(y0);
+  const float4 a = texel_at(sc, l, i0, j0), b = texel_at(sc, l, i0 + 1, j0);
+  const float4 c = texel_at(sc, l, i0, j0 + 1), d = texel_at(sc, l, i0 + 1, j0 + 1);
+  return make_float4(mix1(mix1(a.x, b.x, fx), mix1(c.x, d.x, fx), fy), mix1(mix1(a.y, b.y, fx), mix1(c.y, d.y, fx), fy),
+                     mix1(mix1(a.z, b.z, fx), mix1(c.z, d.z, fx), fy), mix1(mix1(a.w, b.w, fx), mix1(c.w, d.w, fx), fy));
 }
 __device__ __forceinline__ void unpack_snorm8x3(uint32_t w, V3& o) {
   o.x = snorm8((int)(int8_t)(w & 0xffu));
@@ -414,20 +432,25 @@ __device__ __forceinline__ SI surface(const SceneDev& sc, V3 ro, V3 rd, float t,
   const V3 T = normalize(matvec(t0, t1, t2, bary));
   const V3 B = normalize(matvec(q0, q1, q2, bary));
   const V3 N = normalize(matvec(n0, n1, n2, bary));
+  // uvs * bary (mat3x2 * vec3)
+  const float tu = snorm16((int)(int16_t)(a0.w & 0xffffu)) * bary.x + snorm16((int)(int16_t)(a1.w & 0xffffu)) * bary.y +
+                   snorm16((int)(int16_t)(a2.w & 0xffffu)) * bary.z;
+  const float tv = snorm16((int)(int16_t)(a0.w >> 16)) * bary.x + snorm16((int)(int16_t)(a1.w >> 16)) * bary.y +
+                   snorm16((int)(int16_t)(a2.w >> 16)) * bary.z;
   const int4 mat = __ldg(sc.mat4 + tri.w);
-  const float4 nm = texel(sc, mat.z);
+  const float4 nm = texel(sc, mat.z, tu, tv);
   const V3 map_normal = mul(sub(v3(nm.x, nm.y, nm.z), v3(0.5f, 0.5f, 0.0f)), v3(2.0f, 2.0f, 1.0f));
   si.n = normalize(matvec(T, B, N, map_normal));
   si.origin = add(ro, scale(rd, t - SHADE_EPS * 40.0f));
   onb(si.n, si.b1, si.b2);
   si.wo = vecmat(neg(rd), si.b1, si.b2, si.n);
-  const float4 dif = texel(sc, mat.x);
+  const float4 dif = texel(sc, mat.x, tu, tv);
   si.base = v3(dif.x, dif.y, dif.z);
   si.opacity = dif.w;
-  const float4 mr = texel(sc, mat.y);
+  const float4 mr = texel(sc, mat.y, tu, tv);
   si.metallic = mr.z;
   si.alpha = mr.y * mr.y;
-  const float4 em = texel(sc, mat.w);
+  const float4 em = texel(sc, mat.w, tu, tv);
   si.emission = v3(em.x, em.y, em.z);
   si.spec = v3(mix1(1.0f, si.base.x, si.metallic), mix1(1.0f, si.base.y, si.metallic),
                mix1(1.0f, si.base.z, si.metallic));

@@ -58,7 +58,8 @@ int convert_bvh(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const i
                 const float4* verts4, uint32_t n_verts, float4* inner, int4* inner32, float4* tris, int* root_code,
                 uint32_t* err);
 // Row S: per-vertex attribute quantisation (scene.js:456-470).
-void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
-                    uint32_t n, double scale, double tx, double ty, double tz, double* pos_out3, uint4* attrs);
+void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* bn3,
+                    const double* bt4, const double* uv2, uint32_t n, double scale, double tx, double ty, double tz,
+                    double* pos_out3, uint4* attrs);
 
 }  // namespace pk

@@ -38,14 +38,21 @@ __device__ __forceinline__ uint32_t quantize2(double a, double b) {
   return (uint32_t)(uint16_t)s0 | ((uint32_t)(uint16_t)s1 << 16);
 }
 
+// bn3/bt4 are the normal and signed tangent the bitangent is built from:
+// scene.js:160 takes them before the prop's rotations, so a caller that rotates
+// on the host passes both forms (pk_scene_flatten_tbn); otherwise they alias
+// nrm3/tan4.
 __global__ void k_flatten(const double* __restrict__ pos3, const double* __restrict__ nrm3,
-                          const double* __restrict__ tan4, const double* __restrict__ uv2, uint32_t n, double scl,
+                          const double* __restrict__ tan4, const double* __restrict__ bn3,
+                          const double* __restrict__ bt4, const double* __restrict__ uv2, uint32_t n, double scl,
                           double tx, double ty, double tz, double* __restrict__ pos_out3, uint4* __restrict__ attrs) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* p = pos3 + 3 * (size_t)i;
   const double* nr = nrm3 + 3 * (size_t)i;
   const double* tg = tan4 + 4 * (size_t)i;
+  const double* bn = bn3 + 3 * (size_t)i;
+  const double* bt = bt4 + 4 * (size_t)i;
   pos_out3[3 * (size_t)i + 0] = p[0] * scl + tx;
   pos_out3[3 * (size_t)i + 1] = p[1] * scl + ty;
   pos_out3[3 * (size_t)i + 2] = p[2] * scl + tz;
@@ -53,20 +60,21 @@ __global__ void k_flatten(const double* __restrict__ pos3, const double* __restr
   const double nx = nr[0] * 1.0 + 0.0, ny = nr[1] * 1.0 + 0.0, nz = nr[2] * 1.0 + 0.0;
   const double ux = tg[0] * 1.0 + 0.0, uy = tg[1] * 1.0 + 0.0, uz = tg[2] * 1.0 + 0.0;
   // bitangent = normalize(cross(normalAt, tangentAt) * (w || 1)); cross.y = -(a0*b2 - a2*b0)
-  double cx = nr[1] * tg[2] - nr[2] * tg[1];
-  double cy = -(nr[0] * tg[2] - nr[2] * tg[0]);
-  double cz = nr[0] * tg[1] - nr[1] * tg[0];
-  const double w = tg[3];
+  double cx = bn[1] * bt[2] - bn[2] * bt[1];
+  double cy = -(bn[0] * bt[2] - bn[2] * bt[0]);
+  double cz = bn[0] * bt[1] - bn[1] * bt[0];
+  const double w = bt[3];
   const double sg = (w != 0.0 && w == w) ? w : 1.0;
   cx = cx * sg; cy = cy * sg; cz = cz * sg;
   const double* uv = uv2 + 2 * (size_t)i;
   attrs[i] = make_uint4(quantize3(ux, uy, uz), quantize3(cx, cy, cz), quantize3(nx, ny, nz), quantize2(uv[0], uv[1]));
 }
 
-void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* uv2,
-                    uint32_t n, double scale, double tx, double ty, double tz, double* pos_out3, uint4* attrs) {
+void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, const double* tan4, const double* bn3,
+                    const double* bt4, const double* uv2, uint32_t n, double scale, double tx, double ty, double tz,
+                    double* pos_out3, uint4* attrs) {
   if (n == 0) return;
-  k_flatten<<<(n + 255) / 256, 256, 0, s>>>(pos3, nrm3, tan4, uv2, n, scale, tx, ty, tz, pos_out3, attrs);
+  k_flatten<<<(n + 255) / 256, 256, 0, s>>>(pos3, nrm3, tan4, bn3, bt4, uv2, n, scale, tx, ty, tz, pos_out3, attrs);
 }
 
 // ---- serialised BVH -> traversal format --------------------------------
