@@ -54,6 +54,8 @@ class AtlasImage:
 
     def __init__(self, pixels: np.ndarray, src: str):
         px = np.asarray(pixels, np.uint8)
+        if px.ndim == 3 and px.shape[2] == 1:
+            px = px[..., 0]
         if px.ndim == 2:
             px = np.stack([px, px, px, np.full_like(px, 255)], -1)
         elif px.shape[2] == 3:

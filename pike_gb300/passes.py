@@ -181,8 +181,7 @@ class ShadeHitPass:
     @staticmethod
     def create(device, cameraPass, tracePass, scene, envGenerator) -> "ShadeHitPass":
         inst = ShadeHitPass(device, cameraPass, tracePass, scene, envGenerator)
-        mats = np.ascontiguousarray(scene.materials, np.float64)
-        device.ctx.call("pk_materials_set", ptr(mats), mats.shape[0])
+        scene.uploadMaterials(device)
         if envGenerator is not None:
             envGenerator.upload(device)
         return inst

@@ -103,3 +103,12 @@ def assert_bits_equal(got: np.ndarray, want: np.ndarray, what: str):
     if bad.size:
         i = tuple(bad[0])
         raise AssertionError(f"{what}: {bad.shape[0]} words differ; first at {i}: got {g[i]:#x} want {w[i]:#x}")
+
+
+def assert_bits_equal_nan(got: np.ndarray, want: np.ndarray, what: str):
+    """Bit equality where NaNs sit in the same places; their payloads may differ
+    (x86 produces a negative quiet NaN where the GPU produces 0x7fffffff)."""
+    g, w = np.ascontiguousarray(got, np.float32), np.ascontiguousarray(want, np.float32)
+    gn, wn = np.isnan(g), np.isnan(w)
+    assert np.array_equal(gn, wn), f"{what}: NaNs differ in {int(np.count_nonzero(gn != wn))} places"
+    assert_bits_equal(np.where(gn, np.float32(0), g), np.where(wn, np.float32(0), w), what)
