@@ -53,8 +53,9 @@ def parse():
     ap.add_argument("--subdivisions", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked"],
+    ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
+    ap.add_argument("--no-forms", action="store_true", help="skip the 8-wide BVH (form 1) measurement")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
                     help="inner-node record size (identical results): decoded float boxes (64) or snorm16 (32)")
     return ap.parse_args()
@@ -292,6 +293,93 @@ def read_timing(ctx):
     return {k: {"ms": float(t[i]), "launches": int(t[8 + i])} for i, k in enumerate(kinds)}
 
 
+def hit_agreement(ctx, mode_a: int, mode_b: int, bounces: int = 2):
+    """Per-ray closest-hit agreement of two traversal modes on the pass path
+    (camera rays, then bounce rays shaded from mode_b's hits): rays whose
+    {t, slot, barycentrics} differ, out of all rays traced."""
+    import numpy as np
+    from pike_gb300 import _lib
+    from pike_gb300._lib import ptr
+
+    def counters():
+        c = np.zeros(8, np.uint32)
+        ctx.call("pk_read_counters", ptr(c))
+        return c
+
+    def hit_rows(mode):
+        ctx.call("pk_set_trace_mode", mode)
+        ctx.call("pk_clear_hits_misses")
+        ctx.call("pk_trace")
+        k = int(counters()[1])
+        out = np.zeros((k, 16), np.uint32)
+        if k:
+            ctx.call("pk_read_hits", 0, k, ptr(out))
+        keys = np.ascontiguousarray(out[:, 4:16]).view(np.dtype((np.void, 48))).ravel()
+        return keys, out[:, :3]
+
+    ctx.call("pk_set_render_state", 0, 0.0)
+    for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
+        ctx.call("pk_" + name)
+    total = differ = 0
+    for _ in range(bounces):
+        total += int(counters()[3])
+        ka, va = hit_rows(mode_a)
+        kb, vb = hit_rows(mode_b)
+        common, ia, ib = np.intersect1d(ka, kb, assume_unique=True, return_indices=True)
+        differ += (ka.size - common.size) + (kb.size - common.size) + int((va[ia] != vb[ib]).any(axis=1).sum())
+        for name in ("shade_hit", "trace_shadow", "shade_miss"):
+            ctx.call("pk_" + name)
+    return total, differ
+
+
+def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
+    """Form (1): the 8-wide compressed BVH traced through the same frame
+    pipeline; throughput, work per ray and closest-hit agreement with the
+    drop-in traversal."""
+    from pike_gb300 import _lib
+    wide_mode = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    ctx.call("pk_set_trace_mode", wide_mode)
+    build_ms = ctx.timer_stop()
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", max(args.warmup, 1), B)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_counting", 1)
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", 1, B)
+    ctx.call("pk_sync")
+    counts = read_stats(ctx)
+    ctx.call("pk_set_counting", 0)
+    ctx.call("pk_set_timing", 1)
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", 4, B)
+    ctx.call("pk_sync")
+    kt = read_timing(ctx)
+    ctx.call("pk_set_timing", 0)
+    steps = max(1, min(args.steps, 32))
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    ctx.call("pk_render_frames", steps, B)
+    ms = ctx.timer_stop()
+    rays = read_stats(ctx)["rays_traced"]
+    total, differ = hit_agreement(ctx, plain_mode, wide_mode)
+    ctx.call("pk_set_trace_mode", plain_mode)
+    tr = kt["trace"]
+    R = max(counts["closest_rays"], 1)
+    return {"value": rays / (ms / 1000.0) / 1e6, "unit": UNIT, "steps": steps, "ms_per_step": ms / steps,
+            "closest_hit_launch_ms": tr["ms"] / max(tr["launches"], 1), "wide_build_ms": build_ms,
+            "wide_nodes_per_ray": counts["closest_fetch"] / R, "tri_tests_per_ray": counts["closest_tests"] / R,
+            "shadow_wide_nodes_per_ray": counts["shadow_fetch"] / max(counts["shadow_rays"], 1),
+            "node_bytes": 96,
+            "closest_hit_agreement": {"rays": total, "differ": differ, "fraction_equal": 1.0 - differ / max(total, 1),
+                                      "note": "camera + first bounce rays, pass path; differing rays are the "
+                                              "drop-in's truncated-box misses and t ties (the wide result "
+                                              "equals brute force, tests/test_gpu_wide.py)"}}
+
+
 def gpu_arm(args):
     import ctypes as C
 
@@ -300,7 +388,9 @@ def gpu_arm(args):
     src = make_scene(args)
     ctx, bvh_ms = setup_context(src, local)
     from pike_gb300 import _lib
-    mode = _lib.PK_TRACE_PERSISTENT if args.trace_mode == "persistent" else _lib.PK_TRACE_CHUNKED
+    mode = _lib.PK_TRACE_CHUNKED if args.trace_mode == "chunked" else _lib.PK_TRACE_PERSISTENT
+    if args.trace_mode == "wide":
+        mode |= _lib.PK_TRACE_WIDE
     if args.node_records == 32:
         mode |= _lib.PK_TRACE_COMPACT_RECORDS
     ctx.call("pk_set_trace_mode", mode)
@@ -372,13 +462,17 @@ def gpu_arm(args):
     e2e_value = D.sum(float(e2e_rays)) / (e2e_ms_max / 1000.0) / 1e6
     img.free()
     ctx.call("pk_sync")
+    forms = None
+    if rank == 0 and args.trace_mode != "wide" and not args.no_forms:
+        forms = {"wide_bvh": wide_form(ctx, args, B, first_sample, mode)}
 
     if rank == 0:
         peak, peak_kind = load_peak_hbm()
         tr = kt["trace"]
         trace_ms = tr["ms"] / max(tr["launches"], 1)
         R, H = counts["closest_rays"], counts["closest_hits"]
-        alg_bytes_frame = (20 * counts["closest_fetch"] + 52 * counts["closest_tests"] + 48 * R + 64 * H
+        node_bytes = 96 if args.trace_mode == "wide" else 20
+        alg_bytes_frame = (node_bytes * counts["closest_fetch"] + 52 * counts["closest_tests"] + 48 * R + 64 * H
                            + 48 * (R - H))
         alg_bytes_launch = alg_bytes_frame / B
         achieved = alg_bytes_launch / (trace_ms / 1000.0) / 1e9
@@ -399,13 +493,15 @@ def gpu_arm(args):
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes_launch,
                          "launch_ms": trace_ms,
-                         "bytes_model": "20*node_fetch + 52*tri_test + 48*ray + 64*hit + 48*miss"},
+                         "bytes_model": f"{node_bytes}*node_fetch + 52*tri_test + 48*ray + 64*hit + 48*miss"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": src.width * src.height * 4, "steps": e2e_steps},
             "gpu_launches": launches_per_frame * args.steps,
             "clocks": clk,
             "counts_per_frame": counts,
         }
+        if forms:
+            line["forms"] = forms
         if world == 1 and not args.no_cpu_baseline:
             res = cpu_run(src, B, args.cpu_seconds, os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": res["mrays"], "unit": UNIT, "cores": os.cpu_count() or 1,

@@ -128,6 +128,10 @@ int pk_bvh_upload(pk_ctx* ctx, const int32_t* nodes5, uint32_t n_nodes, const in
                   uint32_t n_leaf_tris, const float* verts4, uint32_t n_verts);
 /* n_nodes, n_leaf_tris, and the normaliser {center x,y,z, scale} (only set by pk_bvh_build). */
 int pk_bvh_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* n_leaf_tris, double norm4[4]);
+/* Size (8-wide nodes, levels) and records (24 floats per node, the layout of
+ * pk_wide.h) of the wide BVH; PK_ERR_STATE before PK_TRACE_WIDE was set. */
+int pk_wide_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* depth);
+int pk_wide_download(pk_ctx* ctx, float* nodes24);
 int pk_bvh_download(pk_ctx* ctx, int32_t* nodes5, int32_t* tri4_leaf, float* verts4);
 
 /* ---- environment (row E) --------------------------------------------------
@@ -257,6 +261,14 @@ int pk_read_display_async(pk_ctx* ctx, uint8_t* out8);
 #define PK_TRACE_CHUNKED 0
 #define PK_TRACE_PERSISTENT 1
 #define PK_TRACE_COMPACT_RECORDS 2
+/* OR PK_TRACE_WIDE to trace an 8-wide BVH with 8-bit child boxes, collapsed
+ * from the binary BVH on first use (no reference counterpart: the precision
+ * form beside the drop-in).  Its closest hit is the minimum of (t, triangle
+ * slot) over every triangle the reference's test accepts, with the same t, u,
+ * v bits; the drop-in traversal keeps the reference's first-found order and
+ * its inward-truncated snorm16 boxes, so the two differ only on rays where
+ * those boxes lose a hit or two triangles tie on t. */
+#define PK_TRACE_WIDE 4
 int pk_set_trace_mode(pk_ctx* ctx, int mode);
 /* Elementwise evaluation of the library's built-in definitions on the GPU
  * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */

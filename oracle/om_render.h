@@ -197,6 +197,27 @@ struct Renderer {
     return dist > eps ? dist : MAX_T;
   }
   struct TravResult { float t; int32_t index; uint32_t bary; uint32_t fetch, tests, max_stack; };
+  // Order-independent answer: every triangle tested, closest = min (t, slot),
+  // any = some triangle accepted.  Used in place of intersect() when
+  // `canonical` is set (the reference of the 8-wide traversal).
+  bool canonical = false;
+  template <bool ANY>
+  TravResult brute(V3 o, V3 d) const {
+    const float eps = ANY ? 1e-7f : 1e-8f;
+    TravResult r{MAX_T, -1, 0u, 0u, 0u, 0u};
+    const size_t nt = tri4.size() / 4;
+    for (size_t k = 0; k < nt; k++) {
+      uint32_t bary = 0u;
+      const float res = tri_hit(o, d, &tri4[4 * k], eps, &bary);
+      if (res < r.t) {
+        r.t = res;
+        r.index = (int32_t)k;
+        r.bary = bary;
+        if (ANY) break;
+      }
+    }
+    return r;
+  }
   template <bool ANY>
   TravResult intersect(V3 o, V3 d, std::vector<int32_t>& stack) const {
     const float eps = ANY ? 1e-7f : 1e-8f;
@@ -248,7 +269,8 @@ struct Renderer {
       std::vector<int32_t> stack;
       for (size_t j = b; j < e; j++) {
         const DeferredRay& r = ray_buffer[j];
-        res[j] = intersect<false>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), stack);
+        res[j] = canonical ? brute<false>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]))
+                           : intersect<false>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), stack);
       }
     });
     for (uint32_t j = 0; j < n; j++) {
@@ -273,7 +295,8 @@ struct Renderer {
       std::vector<int32_t> stack;
       for (size_t j = b; j < e; j++) {
         const DeferredRay& r = ray_buffer[off + j];
-        res[j] = intersect<true>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), stack);
+        res[j] = canonical ? brute<true>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]))
+                           : intersect<true>(v3(r.o[0], r.o[1], r.o[2]), v3(r.d[0], r.d[1], r.d[2]), stack);
       }
     });
     for (uint32_t j = 0; j < n; j++) {

@@ -275,6 +275,27 @@ void or_trace_rays(void* p, const float* rays8, size_t n, int any_hit, uint32_t*
   });
 }
 
+// Brute-force ray queries over every leaf-ordered triangle with the
+// reference's triangle test: closest = minimum of (t, slot), any = whether
+// some triangle is accepted.  out4 = {t bits, slot, bary, 0} (any: t and slot
+// of the lowest accepted slot).  The canonical answer an order-independent
+// traversal must reproduce.
+void or_brute_rays(void* p, const float* rays8, size_t n, int any_hit, uint32_t* out4) {
+  Renderer* r = (Renderer*)p;
+  parallel_for(n, r->nthreads, [&](size_t b, size_t e, int) {
+    for (size_t i = b; i < e; i++) {
+      const float* q = rays8 + 8 * i;
+      const V3 o = v3(q[0], q[1], q[2]), d = v3(q[4], q[5], q[6]);
+      const Renderer::TravResult t = any_hit ? r->brute<true>(o, d) : r->brute<false>(o, d);
+      out4[4 * i + 0] = f2u(t.t);
+      out4[4 * i + 1] = (uint32_t)t.index;
+      out4[4 * i + 2] = t.bary;
+      out4[4 * i + 3] = 0u;
+    }
+  });
+}
+void or_set_canonical(void* p, int on) { ((Renderer*)p)->canonical = on != 0; }
+
 // Elementwise math probes for parity of the built-in definitions:
 // fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y), 8 snorm16 decode.
 void or_math(int fn, const float* x, const float* y, float* out, size_t n) {

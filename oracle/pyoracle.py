@@ -265,6 +265,17 @@ class Renderer:
         lib().or_trace_rays(self.p, _p(rays8), C.c_size_t(rays8.shape[0]), C.c_int(1 if any_hit else 0), _p(out))
         return out
 
+    def set_canonical(self, on: bool = True):
+        """Trace by testing every triangle (min (t, slot)): the 8-wide traversal's answer."""
+        lib().or_set_canonical(self.p, C.c_int(1 if on else 0))
+
+    def brute_rays(self, rays8: np.ndarray, any_hit: bool = False) -> np.ndarray:
+        """Every triangle tested: closest = min (t, slot); the order-independent answer."""
+        rays8 = np.ascontiguousarray(rays8, np.float32)
+        out = np.zeros((rays8.shape[0], 4), np.uint32)
+        lib().or_brute_rays(self.p, _p(rays8), C.c_size_t(rays8.shape[0]), C.c_int(1 if any_hit else 0), _p(out))
+        return out
+
 
 MATH_FN = {"sin": 0, "cos": 1, "tan": 2, "atan2": 3, "acos": 4, "exp2": 5, "log2": 6, "pow": 7, "snorm16": 8}
 

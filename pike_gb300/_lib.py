@@ -19,7 +19,7 @@ HEADER = os.path.join(HERE, "..", "include", "pike.h")
 PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED = range(6)
 PK_BVH_SWEEP = 0
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
-PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS = 0, 1, 2
+PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE = 0, 1, 2, 4
 
 
 class PikeError(RuntimeError):
@@ -63,6 +63,7 @@ def load(path: str = LIB_PATH):
         "pk_scene_upload": [_P, _P, u32, _P, _P, u32], "pk_scene_download": [_P, _P, _P],
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
         "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
+        "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],
         "pk_bvh_info": [_P, _P, _P, _P], "pk_bvh_download": [_P, _P, _P, _P],
         "pk_env_build": [_P, _P, u32, u32], "pk_env_upload": [_P, _P, u32, u32, _P, u32, _P, _P],

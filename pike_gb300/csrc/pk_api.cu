@@ -13,6 +13,7 @@
 #include "../../include/pike.h"
 #include "pk_bvh.h"
 #include "pk_ctx.h"
+#include "pk_wide.h"
 #include "pk_host_tables.h"
 #include "pk_internal.cuh"
 #include "pk_render.h"
@@ -117,7 +118,7 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
     c->npix = width * height;
     c->ct = compact_tiles(c->cap);
     c->st = shade_tiles(c->cap);
-    kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade);
+    kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade, &c->g_trace_wide);
     for (int i = 0; i < 3; i++) {
       c->rq[0][i].alloc(c->cap);
       c->rq[1][i].alloc(c->cap);
@@ -281,7 +282,30 @@ int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32
 }
 
 // ---------------- BVH ----------------
+// The 8-wide compressed BVH from the binary nodes and triangle records.
+static int build_wide(pk_ctx* c) {
+  std::vector<int32_t> nodes(5 * (size_t)c->n_nodes);
+  std::vector<float> tris(12 * (size_t)c->n_leaf_tris);
+  check(cudaMemcpyAsync(nodes.data(), c->nodes5.p, nodes.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  if (c->n_leaf_tris)
+    check(cudaMemcpyAsync(tris.data(), c->tris.p, tris.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  check(cudaStreamSynchronize(c->stream), "sync");
+  WideHost w;
+  std::string why;
+  if (build_wide_bvh(nodes.data(), c->n_nodes, tris.data(), c->n_leaf_tris, w, why))
+    return fail(c, PK_ERR_ARG, "wide BVH: " + why);
+  upload(c->wide, reinterpret_cast<const float4*>(w.nodes.data()), 6 * (size_t)w.n_nodes, c->stream);
+  check(cudaStreamSynchronize(c->stream), "sync");
+  c->wide_nodes = w.n_nodes;
+  c->wide_depth = w.max_depth;
+  c->wide_ready = true;
+  c->invalidate_graph();
+  return PK_OK;
+}
+
 static int finish_bvh(pk_ctx* c) {
+  c->wide_ready = false;
+  c->wide.release();
   c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->inner32.alloc(2 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
@@ -296,8 +320,30 @@ static int finish_bvh(pk_ctx* c) {
   check(cudaMemcpy(&herr, err.p, 4, cudaMemcpyDeviceToHost), "D2H");
   if (herr) return fail(c, PK_ERR_ARG, "malformed BVH (child index, leaf size >= 128 or vertex index out of range)");
   c->bvh_ready = true;
+  if (c->trace_mode & TRACE_WIDE) {
+    const int rc = build_wide(c);
+    if (rc != PK_OK) return rc;
+  }
   c->invalidate_graph();
   return PK_OK;
+}
+
+int pk_wide_info(pk_ctx* c, uint32_t* n_nodes, uint32_t* depth) {
+  return guarded(c, [&]() {
+    if (!c->wide_ready) return fail(c, PK_ERR_STATE, "no wide BVH: set PK_TRACE_WIDE after building a BVH");
+    if (n_nodes) *n_nodes = c->wide_nodes;
+    if (depth) *depth = c->wide_depth;
+    return PK_OK;
+  });
+}
+
+int pk_wide_download(pk_ctx* c, float* nodes24) {
+  return guarded(c, [&]() {
+    if (!c->wide_ready) return fail(c, PK_ERR_STATE, "no wide BVH");
+    if (!nodes24) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaMemcpy(nodes24, c->wide.p, c->wide.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    return PK_OK;
+  });
 }
 
 int pk_bvh_upload(pk_ctx* c, const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4_leaf, uint32_t n_leaf_tris,
@@ -815,8 +861,13 @@ int pk_set_trace_mode(pk_ctx* c, int mode) {
   return guarded(c, [&]() {
     c->invalidate_graph();
     const int sched = mode & 1;
-    if (mode & ~(1 | PK_TRACE_COMPACT_RECORDS)) return fail(c, PK_ERR_ARG, "unknown trace mode");
-    c->trace_mode = sched;
+    if (mode & ~(1 | PK_TRACE_COMPACT_RECORDS | PK_TRACE_WIDE)) return fail(c, PK_ERR_ARG, "unknown trace mode");
+    if ((mode & PK_TRACE_WIDE) && !c->wide_ready) {
+      if (!c->bvh_ready) return fail(c, PK_ERR_STATE, "PK_TRACE_WIDE needs a BVH");
+      const int rc = build_wide(c);
+      if (rc != PK_OK) return rc;
+    }
+    c->trace_mode = sched | (mode & PK_TRACE_WIDE ? TRACE_WIDE : 0);
     c->compact_nodes = (mode & PK_TRACE_COMPACT_RECORDS) != 0;
     return PK_OK;
   });

@@ -37,7 +37,7 @@ struct pk_ctx {
   // configuration
   uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;
   uint32_t ct = 0, st = 0;  // look-back tiles per compaction / shade launch
-  unsigned g_trace = 1, g_compact = 1, g_shade = 1;  // persistent grid sizes
+  unsigned g_trace = 1, g_compact = 1, g_shade = 1, g_trace_wide = 1;  // persistent grid sizes
   int trace_mode = pk::TRACE_PERSISTENT;
   // CUDA graph of one pk_render_frame (replayed per frame); rebuilt when any
   // pointer or launch parameter captured in it changes.
@@ -80,6 +80,9 @@ struct pk_ctx {
   DevBuf<int4> inner32;
   DevBuf<double> node_box_d;  // exact double node bounds (pk_bvh_build only)
   bool compact_nodes = false;  // traverse 32-byte records (same boxes as the 64-byte ones)
+  DevBuf<float4> wide;         // 8-wide compressed BVH (built on first use of PK_TRACE_WIDE)
+  uint32_t wide_nodes = 0, wide_depth = 0;
+  bool wide_ready = false;
   int root = 0;
   bool bvh_ready = false;
   // env
@@ -113,7 +116,7 @@ struct pk_ctx {
     L.cam = cam.p;
     L.scene = pk::SceneDev{inner.p, compact_nodes ? inner32.p : nullptr, tris.p, tri4_leaf.p, attrs.p, mat4.p,
                            layers.p, (int)n_layers, (int)atlas_res, root,
-                       n_leaf_tris, n_verts, n_mats};
+                       n_leaf_tris, n_verts, n_mats, wide_ready ? wide.p : nullptr};
     L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
     L.color = color.p;
     L.accum = accum.p;
@@ -123,6 +126,7 @@ struct pk_ctx {
     L.capacity = cap;
     L.miss_capacity = 2 * cap;
     L.trace_blocks = g_trace;
+    L.trace_blocks_wide = g_trace_wide;
     L.compact_blocks = g_compact;
     L.shade_blocks = g_shade;
     L.trace_mode = trace_mode;

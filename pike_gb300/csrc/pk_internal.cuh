@@ -71,6 +71,7 @@ struct SceneDev {
   uint32_t n_tris;         // leaf-ordered triangles
   uint32_t n_verts;        // vertex attributes
   uint32_t n_mats;         // material index entries
+  const float4* wide;      // 6 float4 per 8-wide node (pk_wide.h); null unless built
 };
 
 struct EnvDev {

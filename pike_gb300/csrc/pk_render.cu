@@ -12,6 +12,7 @@
 #include "pk_internal.cuh"
 #include "pk_render.h"
 #include "pk_traverse.cuh"
+#include "pk_traverse_wide.cuh"
 
 namespace pk {
 
@@ -261,6 +262,154 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
       if (sp == 0) { fin = true; break; }
       --sp;
       cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+    }
+    if (fin) {
+      const bool hit = best_i != -1;
+      if (hit) {
+        if (!ANY) hrec[j] = make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u);
+        if (!(ANY && FUSED)) atomicOr(flags + (j >> 5), 1u << (j & 31u));
+        if (COUNT) nhit += 1;
+      } else if (FUSED) {
+        const float4 tpv = R.t[j];
+        const V3 e = env_color(env, theta, v3(dx, dy, dz));
+        add_color(color, npix, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y, e.z * tpv.z, 1.0f,
+                  &ctr->err);
+      }
+      have = false;
+    }
+  }
+  if (COUNT) {
+    atomicAdd(&ctr->stat[ANY ? 2 : 0], (unsigned long long)nfetch);
+    atomicAdd(&ctr->stat[ANY ? 3 : 1], (unsigned long long)ntest);
+    atomicAdd(&ctr->stat[ANY ? 7 : 6], (unsigned long long)nhit);
+  }
+}
+
+// Pops the next stack entry whose entry distance does not exceed the current
+// best hit (with the traversal's slack); false when none is left.
+__device__ __forceinline__ bool wide_pop(int (*sstack)[TRACE_THREADS], float (*sdist)[TRACE_THREADS], const int* lstack,
+                                         const float* ldist, int tid, int& sp, float best_t, int& cur) {
+  const float lim = best_t + best_t * WIDE_SLACK;
+  while (sp > 0) {
+    --sp;
+    const bool sm = sp < WIDE_STACK_SMEM;
+    const float dd = sm ? sdist[sp][tid] : ldist[sp - WIDE_STACK_SMEM];
+    if (dd <= lim) {
+      cur = sm ? sstack[sp][tid] : lstack[sp - WIDE_STACK_SMEM];
+      return true;
+    }
+  }
+  return false;
+}
+
+// =====================================================================
+// Persistent traversal of the 8-wide compressed BVH: the lane scheduling and
+// outputs of k_trace_dyn; closest hit = min (t, slot) over accepted
+// triangles, any hit = the first accepted triangle.
+// =====================================================================
+template <bool ANY, bool FUSED, bool COUNT>
+__global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+                                                               const uint32_t* __restrict__ countp, RayQ R,
+                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
+                                                               float4* __restrict__ color, uint32_t npix,
+                                                               uint32_t* __restrict__ ticket) {
+  __shared__ int sstack[WIDE_STACK_SMEM][TRACE_THREADS];
+  __shared__ float sdist[WIDE_STACK_SMEM][TRACE_THREADS];
+  int lstack[WIDE_STACK_LOCAL];
+  float ldist[WIDE_STACK_LOCAL];
+  const uint32_t n = *countp;
+  const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x;
+  const uint32_t ltmask = (1u << lane) - 1u;
+  const float theta = ctr->env_theta;
+  const float eps = ANY ? 1e-7f : 1e-8f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&ctr->rays_traced, (unsigned long long)n);
+    if (COUNT) atomicAdd(&ctr->stat[ANY ? 5 : 4], (unsigned long long)n);
+  }
+  uint32_t nfetch = 0, ntest = 0, nhit = 0;
+  uint32_t j = 0;
+  bool have = false, exhausted = false;
+  float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, ix = 0.f, iy = 0.f, iz = 0.f;
+  float best_t = MAX_T;
+  int best_i = -1;
+  uint32_t best_b = 0u;
+  int sp = 0, cur = 0;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
+    const uint32_t busy = __ballot_sync(0xffffffffu, have);
+    if (idle && (__popc(idle) >= REFILL_MIN || busy == 0u)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(ticket, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!have && !exhausted) {
+        j = base + (uint32_t)__popc(idle & ltmask);
+        if (j < n) {
+          const float4 o = R.o[j], d = R.d[j];
+          ox = o.x; oy = o.y; oz = o.z;
+          dx = d.x; dy = d.y; dz = d.z;
+          ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz);
+          best_t = MAX_T; best_i = -1; best_b = 0u;
+          sp = 0;
+          cur = 0;  // wide root
+          have = true;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) break;
+    if (!have) continue;
+    bool fin = false;
+    // wide nodes: descend into the nearest hit child, push the others with
+    // their entry distances; pops skip entries that start beyond the best hit
+    while (cur >= 0) {
+      if (COUNT) nfetch += 1;
+      float d[8];
+      int c[8];
+      wide_children(sc.wide, cur, ox, oy, oz, ix, iy, iz, best_t, d, c);
+      // descend into the nearest hit child; push the other hit children (their
+      // codes differ from the nearest one's)
+      float dn = __int_as_float(0x7f800000);
+      int cn = 0;
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if (d[k] < dn) { dn = d[k]; cn = c[k]; }
+      if (!(dn < __int_as_float(0x7f800000))) {
+        if (!wide_pop(sstack, sdist, lstack, ldist, tid, sp, best_t, cur)) { fin = true; break; }
+        continue;
+      }
+      bool over = false;
+#pragma unroll
+      for (int k = 7; k >= 0; k--) {
+        if (d[k] < __int_as_float(0x7f800000) && c[k] != cn) {
+          if (sp < WIDE_STACK_SMEM) { sstack[sp][tid] = c[k]; sdist[sp][tid] = d[k]; }
+          else if (sp < WIDE_STACK_SMEM + WIDE_STACK_LOCAL) { lstack[sp - WIDE_STACK_SMEM] = c[k]; ldist[sp - WIDE_STACK_SMEM] = d[k]; }
+          else over = true;
+          ++sp;
+        }
+      }
+      if (over) { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
+      cur = cn;
+    }
+    // leaves
+    while (!fin && cur < 0) {
+      const uint32_t word = (uint32_t)cur & 0x7fffffffu;
+      const int size = (int)(word >> 24);
+      const int base = (int)(word & 0x00ffffffu);
+      for (int i = 0; i < size; i++) {
+        if (COUNT) ntest += 1;
+        float res, u, v;
+        if (!tri_test(sc.tris, base + i, ox, oy, oz, dx, dy, dz, eps, res, u, v)) continue;
+        if (res < best_t || (res == best_t && base + i < best_i)) {
+          best_t = res;
+          best_i = base + i;
+          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        }
+      }
+      if (ANY && best_i != -1) { fin = true; break; }
+      if (!wide_pop(sstack, sdist, lstack, ldist, tid, sp, best_t, cur)) { fin = true; break; }
     }
     if (fin) {
       const bool hit = best_i != -1;
@@ -774,15 +923,19 @@ uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) 
 
 // Persistent grids: enough resident blocks to fill every multiprocessor, never
 // more blocks than there can be work items.
-void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade) {
-  int t = 0, c = 0, s = 0;
+void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade,
+                  unsigned* trace_wide) {
+  int t = 0, c = 0, s = 0, w = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false>, TRACE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w, k_trace_wide<false, true, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_shade, SHADE_THREADS, 0);
   const unsigned warps = (capacity + 31u) / 32u;
   *trace = std::max(1u, std::min((unsigned)(sms * std::max(t, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
   *compact = std::max(1u, std::min((unsigned)(sms * std::max(c, 1)), compact_tiles(capacity)));
   *shade = std::max(1u, std::min((unsigned)(sms * std::max(s, 1)), shade_tiles(capacity)));
+  *trace_wide =
+      std::max(1u, std::min((unsigned)(sms * std::max(w, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
 }
 
 void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
@@ -793,6 +946,22 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
   const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
+  if (L.trace_mode & TRACE_WIDE) {
+    const dim3 grid(L.trace_blocks_wide);
+    const unsigned words = (L.capacity + 31u) / 32u + 1u;
+    if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
+#define PK_TRACEW(A, F, C) \
+  k_trace_wide<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
+    if (!any_hit) {
+      if (fused) { if (count) PK_TRACEW(false, true, true); else PK_TRACEW(false, true, false); }
+      else { if (count) PK_TRACEW(false, false, true); else PK_TRACEW(false, false, false); }
+    } else {
+      if (fused) { if (count) PK_TRACEW(true, true, true); else PK_TRACEW(true, true, false); }
+      else { if (count) PK_TRACEW(true, false, true); else PK_TRACEW(true, false, false); }
+    }
+#undef PK_TRACEW
+    return;
+  }
   if (L.trace_mode == TRACE_PERSISTENT) {
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);

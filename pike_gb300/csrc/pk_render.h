@@ -9,7 +9,7 @@ namespace pk {
 
 // Traversal scheduling: fixed 32-ray chunks per warp, or persistent lanes with
 // batched refill.  Both visit every ray's nodes in the reference order.
-enum TraceMode : int { TRACE_CHUNKED = 0, TRACE_PERSISTENT = 1 };
+enum TraceMode : int { TRACE_CHUNKED = 0, TRACE_PERSISTENT = 1, TRACE_WIDE = 4 };
 
 // Everything a launch needs that is fixed for a configured context.
 struct LaunchCtx {
@@ -25,7 +25,7 @@ struct LaunchCtx {
   uint32_t npix;
   uint32_t capacity;       // ray / hit / shadow queue capacity (batch rounded up to 128)
   uint32_t miss_capacity;  // 2 * capacity
-  unsigned trace_blocks, compact_blocks, shade_blocks;
+  unsigned trace_blocks, compact_blocks, shade_blocks, trace_blocks_wide;
   int trace_mode;
 };
 
@@ -41,7 +41,8 @@ void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, Ra
 void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,
                   uint32_t* ticket, unsigned long long* tiles);
 // Grid sizes for a queue capacity on a GPU with `sms` multiprocessors.
-void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade);
+void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade,
+                  unsigned* trace_wide);
 // Tile counts the look-back kernels need for a given queue capacity.
 uint32_t compact_tiles(uint32_t capacity);
 uint32_t shade_tiles(uint32_t capacity);

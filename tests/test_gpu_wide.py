@@ -1,0 +1,149 @@
+"""The 8-wide compressed BVH (PK_TRACE_WIDE): closest hits equal the minimum
+of (t, triangle slot) over every triangle the reference's test accepts, any
+hits equal "some triangle accepted", so whole frames match the oracle run
+with brute-force traversal bit for bit; against the drop-in traversal they
+differ only where its inward-truncated boxes lose a hit or triangles tie."""
+import numpy as np
+import pytest
+
+from pike_gb300 import _lib, synth
+from pike_gb300._lib import ptr
+
+from helpers import Pair, assert_bits_equal
+
+pytestmark = pytest.mark.gpu
+
+WIDE = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE
+
+
+def wide_pair(oracle, src, **kw) -> Pair:
+    pair = Pair(src, oracle, **kw)
+    pair.ctx.call("pk_set_trace_mode", WIDE)
+    pair.P.r.set_canonical(True)
+    return pair
+
+
+def wide_nodes(ctx):
+    n, depth = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
+    ctx.call("pk_wide_info", ptr(n), ptr(depth))
+    nodes = np.zeros((int(n[0]), 24), np.float32)
+    ctx.call("pk_wide_download", ptr(nodes))
+    return nodes, int(depth[0])
+
+
+def test_wide_structure(oracle, pk_built):
+    """Every leaf-ordered triangle is reachable from exactly one valid slot;
+    child nodes come after their parent; decoded child boxes lie inside the
+    parent's own slot box."""
+    src = synth.displaced_sphere_scene(subdivisions=5, width=16, height=16, env_size=(64, 32))
+    pair = wide_pair(oracle, src)
+    nodes, depth = wide_nodes(pair.ctx)
+    words = nodes.view(np.uint32)
+    n_tris = src.tris.shape[0]
+    seen = np.zeros(n_tris, np.int64)
+    referenced = np.zeros(nodes.shape[0], np.int64)
+    for i in range(nodes.shape[0]):
+        valid = words[i, 3] >> 24
+        codes = words[i, 4:12].view(np.int32)
+        for k in range(8):
+            if not (valid >> k) & 1:
+                continue
+            c = int(codes[k])
+            if c >= 0:
+                assert c > i
+                referenced[c] += 1
+            else:
+                w = c & 0x7FFFFFFF
+                size, base = w >> 24, w & 0xFFFFFF
+                seen[base:base + size] += 1
+    assert (seen == 1).all()
+    assert referenced[0] == 0 and (referenced[1:] == 1).all()
+    assert 2 <= depth <= 16
+
+
+@pytest.mark.parametrize("make", [
+    lambda: synth.small_scene(width=64, height=48),
+    lambda: synth.displaced_sphere_scene(subdivisions=4, width=64, height=40, env_size=(128, 64)),
+])
+def test_wide_frames_match_bruteforce_oracle(oracle, pk_built, make):
+    src = make()
+    pair = wide_pair(oracle, src, threads=16)
+    pair.ctx.call("pk_set_render_state", 0, 0.0)
+    pair.ctx.call("pk_render_frames", 2, 4)
+    pair.ctx.call("pk_sync")
+    P = pair.P.r
+    P.set_render_state(0)
+    for _ in range(2):
+        P.tick(4)
+    assert_bits_equal(pair.image("accum"), P.accum(), "wide traversal vs brute-force oracle")
+    assert pair.counters()["err"] == 0
+
+
+def test_wide_pass_hits_match_bruteforce(oracle, pk_built):
+    """Camera and two bounces of rays through the pass path: every closest hit
+    (slot, t, barycentrics) equals the brute-force answer."""
+    src = synth.displaced_sphere_scene(subdivisions=6, width=120, height=80, env_size=(128, 64))
+    pair = wide_pair(oracle, src, threads=16)
+    c, P = pair.ctx, pair.P.r
+    pair.set_render_state(0)
+    for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
+        c.call("pk_" + name)
+    for bounce in range(3):
+        n = pair.counters()["num_rays"]
+        rays = pair.rays(_lib.PK_QUEUE_RAYS, 0, n)
+        c.call("pk_trace")
+        hits = pair.hits(pair.counters()["num_hits"])
+        want = P.brute_rays(np.ascontiguousarray(rays[:, :8]))
+        hit = want[:, 1] != 0xFFFFFFFF
+        assert hits.shape[0] == int(hit.sum()), f"bounce {bounce}: hit count"
+        # the hit list is in ray order; hit records carry {t, slot, bary}
+        assert np.array_equal(hits[:, 1], want[hit, 1]), f"bounce {bounce}: slots"
+        assert np.array_equal(hits[:, 0], want[hit, 0]), f"bounce {bounce}: t"
+        assert np.array_equal(hits[:, 2], want[hit, 2]), f"bounce {bounce}: barycentrics"
+        for name in ("shade_hit", "trace_shadow", "shade_miss"):
+            c.call("pk_" + name)
+
+
+def per_ray(hits: np.ndarray, rays: np.ndarray) -> np.ndarray:
+    """Hit records -> (n, 3) {t, slot, bary} per queue ray (slot 0xffffffff: miss).
+    Records carry their ray, whose 12 words identify it in the queue."""
+    index = {rays[i].tobytes(): i for i in range(rays.shape[0])}
+    out = np.zeros((rays.shape[0], 3), np.uint32)
+    out[:, 1] = 0xFFFFFFFF
+    for h in hits:
+        out[index[h[4:16].view(np.float32).tobytes()]] = h[:3]
+    return out
+
+
+def test_wide_vs_dropin_agreement(oracle, pk_built):
+    """Closest hits of the drop-in traversal agree with the wide one except on
+    rays where the drop-in's inward-truncated boxes lose a hit or a tie on t
+    resolves differently; on every differing ray the wide answer equals brute
+    force, and such rays are rare."""
+    src = synth.displaced_sphere_scene(subdivisions=7, width=320, height=180, env_size=(256, 128))
+    pair = Pair(src, oracle)
+    c = pair.ctx
+    pair.set_render_state(0)
+    for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
+        c.call("pk_" + name)
+    total = differ = 0
+    for bounce in range(3):
+        n = pair.counters()["num_rays"]
+        rays = pair.rays(_lib.PK_QUEUE_RAYS, 0, n)
+        res = []
+        for mode in (_lib.PK_TRACE_PERSISTENT, WIDE):
+            c.call("pk_set_trace_mode", mode)
+            c.call("pk_clear_hits_misses")
+            c.call("pk_trace")
+            res.append(per_ray(pair.hits(pair.counters()["num_hits"]), rays))
+        plain, wide = res
+        bad = np.flatnonzero((plain != wide).any(axis=1))
+        total += n
+        differ += bad.size
+        if bad.size:
+            want = pair.P.r.brute_rays(np.ascontiguousarray(rays[bad, :8]))
+            assert np.array_equal(wide[bad], want[:, :3]), f"bounce {bounce}: wide differs from brute force"
+        for name in ("shade_hit", "trace_shadow", "shade_miss"):
+            c.call("pk_" + name)
+    assert total > 100_000
+    assert differ <= total // 10_000, f"{differ} of {total} rays differ"
