@@ -274,6 +274,40 @@ int pk_set_trace_mode(pk_ctx* ctx, int mode);
  * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */
 int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);
 
+/* ---- form (3): differentiable rendering (no reference counterpart) -------
+ * A path tracer over the loaded scene and BVH with continuous parameters and
+ * its path-replay adjoint.  Paths are cosine-sampled, so they depend on the
+ * seed only; the image is a smooth function of the parameters and
+ * pk_diff_backward returns its exact derivative for those paths (what central
+ * differences with common random numbers measure).  All array pointers are
+ * DEVICE pointers owned by the caller (e.g. torch tensors); the calls block
+ * until the work on the library's stream is done, so the caller must finish
+ * its own writes to the inputs first.  Resolution comes from pk_configure. */
+typedef struct pk_diff_camera {
+  float origin[3];
+  float forward[3];  /* unit view direction */
+  float right[3];    /* scaled by tan(fov/2) * width/height */
+  float up[3];       /* scaled by tan(fov/2) */
+} pk_diff_camera;
+typedef struct pk_diff_params {
+  const float* albedo3;    /* n_mats x 3 */
+  const float* roughness;  /* n_mats, alpha = roughness^2 */
+  const float* metallic;   /* n_mats */
+  uint32_t n_mats;         /* >= the scene's material count, <= 4096 */
+  const float* env_rgb;    /* env_h x env_w x 3 equirect radiance */
+  uint32_t env_w, env_h;
+  uint32_t spp, depth;     /* depth = rays per path, 1..8 */
+  uint32_t seed;
+} pk_diff_params;
+/* image4: width x height x 4 floats (rgb, 0). */
+int pk_diff_render(pk_ctx* ctx, const pk_diff_camera* cam, const pk_diff_params* params, float* image4);
+/* d_image4: dLoss/dimage (width x height x 4); the gradients are ADDED to
+ * g_albedo3 (n_mats x 3), g_roughness (n_mats) and g_env_rgb (env_h x env_w x 3). */
+int pk_diff_backward(pk_ctx* ctx, const pk_diff_camera* cam, const pk_diff_params* params, const float* d_image4,
+                     double* g_albedo3, double* g_roughness, double* g_env_rgb);
+/* Rays traced by the last pk_diff_render / pk_diff_backward call. */
+int pk_diff_rays(pk_ctx* ctx, unsigned long long* rays);
+
 #ifdef __cplusplus
 }
 #endif

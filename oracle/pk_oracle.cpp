@@ -15,6 +15,7 @@
 
 #include "om_build.h"
 #include "om_render.h"
+#include "om_diff.h"
 
 using namespace om;
 
@@ -295,6 +296,38 @@ void or_brute_rays(void* p, const float* rays8, size_t n, int any_hit, uint32_t*
   });
 }
 void or_set_canonical(void* p, int on) { ((Renderer*)p)->canonical = on != 0; }
+
+// Differentiable path tracer (pk_diff.cu) in binary64: image and gradient.
+static DiffScene diff_scene(void* p, const float* cam12, const double* albedo, const double* rough,
+                            const double* metal, uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h,
+                            uint32_t spp, uint32_t depth, uint32_t seed, uint32_t W, uint32_t H) {
+  DiffScene S;
+  S.r = (Renderer*)p;
+  for (int k = 0; k < 3; k++) {
+    S.cam.o[k] = cam12[k];
+    S.cam.f[k] = cam12[3 + k];
+    S.cam.r[k] = cam12[6 + k];
+    S.cam.u[k] = cam12[9 + k];
+  }
+  S.W = W; S.H = H;
+  S.albedo = albedo; S.rough = rough; S.metal = metal; S.n_mats = n_mats;
+  S.env = env; S.env_w = (int)env_w; S.env_h = (int)env_h;
+  S.spp = (int)spp; S.depth = (int)depth; S.seed = seed;
+  return S;
+}
+uint64_t or_diff_render(void* p, const float* cam12, const double* albedo, const double* rough, const double* metal,
+                        uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h, uint32_t spp,
+                        uint32_t depth, uint32_t seed, uint32_t W, uint32_t H, double* image3) {
+  const DiffScene S = diff_scene(p, cam12, albedo, rough, metal, n_mats, env, env_w, env_h, spp, depth, seed, W, H);
+  return diff_render(S, image3, ((Renderer*)p)->nthreads);
+}
+void or_diff_grad(void* p, const float* cam12, const double* albedo, const double* rough, const double* metal,
+                  uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h, uint32_t spp, uint32_t depth,
+                  uint32_t seed, uint32_t W, uint32_t H, const double* dimage3, double* g_albedo, double* g_rough,
+                  double* g_env) {
+  const DiffScene S = diff_scene(p, cam12, albedo, rough, metal, n_mats, env, env_w, env_h, spp, depth, seed, W, H);
+  diff_gradient(S, dimage3, g_albedo, g_rough, g_env, ((Renderer*)p)->nthreads);
+}
 
 // Elementwise math probes for parity of the built-in definitions:
 // fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y), 8 snorm16 decode.

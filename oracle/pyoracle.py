@@ -265,6 +265,33 @@ class Renderer:
         lib().or_trace_rays(self.p, _p(rays8), C.c_size_t(rays8.shape[0]), C.c_int(1 if any_hit else 0), _p(out))
         return out
 
+    def _diff_args(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H):
+        self._dkeep = [np.ascontiguousarray(cam12, np.float32), np.ascontiguousarray(albedo, np.float64),
+                       np.ascontiguousarray(rough, np.float64), np.ascontiguousarray(metal, np.float64),
+                       np.ascontiguousarray(env, np.float64)]
+        c, a, r, m, e = self._dkeep
+        return [self.p, _p(c), _p(a), _p(r), _p(m), C.c_uint32(r.shape[0]), _p(e), C.c_uint32(e.shape[1]),
+                C.c_uint32(e.shape[0]), C.c_uint32(spp), C.c_uint32(depth), C.c_uint32(seed), C.c_uint32(W),
+                C.c_uint32(H)]
+
+    def diff_render(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H):
+        """FP64 oracle of pk_diff_render: (H, W, 3) image and the rays traced."""
+        img = np.zeros((H, W, 3), np.float64)
+        L = lib()
+        L.or_diff_render.restype = C.c_uint64
+        rays = L.or_diff_render(*self._diff_args(cam12, albedo, rough, metal, env, spp, depth, seed, W, H), _p(img))
+        return img, int(rays)
+
+    def diff_grad(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H, dimage):
+        """FP64 oracle of pk_diff_backward for dLoss/dimage = dimage (H, W, 3)."""
+        d = np.ascontiguousarray(dimage, np.float64)
+        ga = np.zeros((np.asarray(albedo).shape[0], 3))
+        gr = np.zeros(np.asarray(rough).shape[0])
+        ge = np.zeros(np.asarray(env).shape)
+        lib().or_diff_grad(*self._diff_args(cam12, albedo, rough, metal, env, spp, depth, seed, W, H), _p(d), _p(ga),
+                           _p(gr), _p(ge))
+        return ga, gr, ge
+
     def set_canonical(self, on: bool = True):
         """Trace by testing every triangle (min (t, slot)): the 8-wide traversal's answer."""
         lib().or_set_canonical(self.p, C.c_int(1 if on else 0))

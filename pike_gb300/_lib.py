@@ -64,6 +64,8 @@ def load(path: str = LIB_PATH):
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
         "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
         "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P],
+        "pk_diff_render": [_P, _P, _P, _P], "pk_diff_backward": [_P, _P, _P, _P, _P, _P, _P],
+        "pk_diff_rays": [_P, _P],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],
         "pk_bvh_info": [_P, _P, _P, _P], "pk_bvh_download": [_P, _P, _P, _P],
         "pk_env_build": [_P, _P, u32, u32], "pk_env_upload": [_P, _P, u32, u32, _P, u32, _P, _P],

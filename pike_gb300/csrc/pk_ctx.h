@@ -100,6 +100,7 @@ struct pk_ctx {
   float kind_ms[pk::N_KINDS] = {0};
   float kind_n[pk::N_KINDS] = {0};
   unsigned long long frames = 0;
+  unsigned long long diff_rays = 0;  // rays of the last differentiable render / adjoint
 
   RayQ R(int i) { return RayQ{rq[i][0].p, rq[i][1].p, rq[i][2].p}; }
   RayQ S() { return RayQ{sq[0].p, sq[1].p, sq[2].p}; }

@@ -1,0 +1,182 @@
+"""Form (3): differentiable rendering through the path-replay adjoint
+(pk_diff_render / pk_diff_backward), exposed as a torch.autograd.Function.
+
+``DiffScene`` owns a library context with the scene, its GPU-built BVH and a
+pinhole camera; ``render(scene, albedo, roughness, env)`` returns the
+(H, W, 4) image as a differentiable function of
+
+* ``albedo``    (n_mats, 3) float32 CUDA tensor,
+* ``roughness`` (n_mats,)   float32 CUDA tensor (alpha = roughness^2),
+* ``env``       (env_h, env_w, 3) float32 CUDA tensor, equirect radiance.
+
+Metallic values are fixed per material (the scene's).  Backward replays every
+path from its seed and returns dLoss/dparams accumulated in FP64 on the
+device (cast to the parameters' dtype).  The host side of a JavaScript
+binding would wrap the same two C calls with the same contract (forward
+returns the image, backward maps dL/dimage to parameter gradients).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from ._lib import Context, ptr
+
+
+class DiffCamera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
+                ("up", C.c_float * 3)]
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("albedo3", C.c_void_p), ("roughness", C.c_void_p), ("metallic", C.c_void_p), ("n_mats", C.c_uint32),
+                ("env_rgb", C.c_void_p), ("env_w", C.c_uint32), ("env_h", C.c_uint32), ("spp", C.c_uint32),
+                ("depth", C.c_uint32), ("seed", C.c_uint32)]
+
+
+def pinhole(state: dict, width: int, height: int) -> np.ndarray:
+    """Camera origin, forward, right, up (12 float32) of a CameraState dict in
+    the BVH's normalised frame: right and up scaled by tan(fov/2) (right also
+    by the aspect ratio), the basis of camera.wgsl:58-73 without lens effects."""
+    o = np.asarray(state["pos"], np.float64)
+    f = np.asarray(state["dir"], np.float64)
+    f = f / np.linalg.norm(f)
+    tf = math.tan(float(state["fov"]) * 0.5)
+    r = np.cross(f, [0.0, 1.0, 0.0])
+    r = r / np.linalg.norm(r)
+    u = np.cross(r, f)
+    u = u / np.linalg.norm(u)
+    return np.concatenate([o, f, r * tf * (width / height), u * tf]).astype(np.float32)
+
+
+class DiffScene:
+    def __init__(self, src, width: int, height: int, spp: int = 16, depth: int = 4, device: int = 0,
+                 camera: dict | None = None):
+        import torch
+        self.src = src
+        self.W, self.H, self.spp, self.depth = int(width), int(height), int(spp), int(depth)
+        ctx = Context(device)
+        self.ctx = ctx
+        ctx.call("pk_configure", self.W, self.H, self.W * self.H)
+        tr = np.zeros(3)
+        ctx.call("pk_scene_flatten", ptr(np.ascontiguousarray(src.pos)), ptr(np.ascontiguousarray(src.normal)),
+                 ptr(np.ascontiguousarray(src.tangent)), ptr(np.ascontiguousarray(src.uv)), src.pos.shape[0],
+                 ptr(np.ascontiguousarray(src.tris, np.int32)), src.tris.shape[0], 1.0, ptr(tr))
+        mats = np.ascontiguousarray(src.materials, np.float64)
+        ctx.call("pk_materials_set", ptr(mats), mats.shape[0])
+        from . import _lib
+        ctx.call("pk_bvh_build", _lib.PK_BVH_SWEEP)
+        self.n_mats = mats.shape[0]
+        self.device = torch.device("cuda", device)
+        self.metallic = torch.tensor(mats[:, 5], dtype=torch.float32, device=self.device)
+        self.cam12 = pinhole(camera or src.camera_state(), self.W, self.H)
+        c = self.cam12
+        self.camera = DiffCamera((C.c_float * 3)(*c[0:3]), (C.c_float * 3)(*c[3:6]), (C.c_float * 3)(*c[6:9]),
+                                 (C.c_float * 3)(*c[9:12]))
+
+    def source_params(self, env_size=(256, 128), sun: float = 100.0, sigma: float = 1.0, seed: int = 7):
+        """The scene's own albedo/roughness and a seeded env map, as CUDA tensors."""
+        import torch
+        from . import synth
+        m = self.src.materials
+        env = synth.hdr_env(synth.SEED_BASE + seed, env_size[0], env_size[1], sigma=sigma, sun=sun)
+        t = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float32, device=self.device)
+        return t(m[:, 0:3]), t(m[:, 4]), t(env)
+
+    def _params(self, albedo, rough, env, seed: int) -> DiffParams:
+        assert albedo.is_contiguous() and rough.is_contiguous() and env.is_contiguous()
+        assert albedo.shape == (self.n_mats, 3) and rough.shape == (self.n_mats,) and env.dim() == 3
+        return DiffParams(albedo.data_ptr(), rough.data_ptr(), self.metallic.data_ptr(), self.n_mats, env.data_ptr(),
+                          env.shape[1], env.shape[0], self.spp, self.depth, int(seed))
+
+    def render(self, albedo, rough, env, seed: int = 0):
+        import torch
+        img = torch.empty((self.H, self.W, 4), dtype=torch.float32, device=self.device)
+        p = self._params(albedo, rough, env, seed)
+        torch.cuda.synchronize(self.device)
+        self.ctx.call("pk_diff_render", C.byref(self.camera), C.byref(p), C.c_void_p(img.data_ptr()))
+        return img
+
+    def backward(self, albedo, rough, env, dimage, seed: int = 0):
+        import torch
+        ga = torch.zeros((self.n_mats, 3), dtype=torch.float64, device=self.device)
+        gr = torch.zeros((self.n_mats,), dtype=torch.float64, device=self.device)
+        ge = torch.zeros(tuple(env.shape), dtype=torch.float64, device=self.device)
+        d = dimage.contiguous().to(torch.float32)
+        p = self._params(albedo, rough, env, seed)
+        torch.cuda.synchronize(self.device)
+        self.ctx.call("pk_diff_backward", C.byref(self.camera), C.byref(p), C.c_void_p(d.data_ptr()),
+                      C.c_void_p(ga.data_ptr()), C.c_void_p(gr.data_ptr()), C.c_void_p(ge.data_ptr()))
+        return ga, gr, ge
+
+    def rays(self) -> int:
+        n = C.c_ulonglong(0)
+        self.ctx.call("pk_diff_rays", C.byref(n))
+        return int(n.value)
+
+
+def _function():
+    import torch
+
+    class PikeRender(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, albedo, rough, env, scene, seed):
+            ctx.scene, ctx.seed = scene, seed
+            ctx.save_for_backward(albedo, rough, env)
+            return scene.render(albedo.detach().contiguous(), rough.detach().contiguous(), env.detach().contiguous(),
+                                seed)
+
+        @staticmethod
+        def backward(ctx, grad_image):
+            albedo, rough, env = ctx.saved_tensors
+            ga, gr, ge = ctx.scene.backward(albedo.detach().contiguous(), rough.detach().contiguous(),
+                                            env.detach().contiguous(), grad_image, ctx.seed)
+            return ga.to(albedo.dtype), gr.to(rough.dtype), ge.to(env.dtype), None, None
+
+    return PikeRender
+
+
+_FN = None
+
+
+def render(scene: DiffScene, albedo, rough, env, seed: int = 0):
+    """Differentiable image (H, W, 4) of the scene for these parameters."""
+    global _FN
+    if _FN is None:
+        _FN = _function()
+    return _FN.apply(albedo, rough, env, scene, seed)
+
+
+def l2_loss(image, target):
+    return ((image[..., :3] - target[..., :3]) ** 2).mean()
+
+
+def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 200, lr: float = 0.02,
+                   n_free: int | None = None, seed_per_step: bool = True):
+    """Adam on (albedo, roughness, env) towards the target image; materials at
+    index >= n_free stay fixed.  Returns the parameters and the loss history."""
+    import torch
+    a = albedo.clone().requires_grad_(True)
+    r = rough.clone().requires_grad_(True)
+    e = env.clone().requires_grad_(True)
+    opt = torch.optim.Adam([a, r, e], lr=lr)
+    keep = None
+    if n_free is not None and n_free < a.shape[0]:
+        keep = (a.detach()[n_free:].clone(), r.detach()[n_free:].clone())
+    hist = []
+    for k in range(steps):
+        opt.zero_grad()
+        loss = l2_loss(render(scene, a, r, e, seed=k if seed_per_step else 0), target)
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            a.clamp_(0.0, 1.0)
+            r.clamp_(0.05, 1.0)
+            e.clamp_(min=0.0)
+            if keep is not None:
+                a[n_free:] = keep[0]
+                r[n_free:] = keep[1]
+        hist.append(float(loss.item()))
+    return a.detach(), r.detach(), e.detach(), hist
