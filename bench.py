@@ -380,6 +380,97 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
                                               "equals brute force, tests/test_gpu_wide.py)"}}
 
 
+def adjoint_form(args, local: int):
+    """Form (3), the differentiation workload: the 1.31M-triangle scene at
+    512x512, 16 spp, depth 4; parameters = 256 group albedos (RGB), 256
+    roughness values and a 256x128 RGB environment.  Forward and adjoint
+    throughput (rays/s, full gradients/s), 32 central differences (h = 1e-3,
+    common random numbers) against the adjoint, and Adam inverse rendering."""
+    import numpy as np
+    import torch
+    from pike_gb300 import synth
+    from pike_gb300.diff import DiffScene, inverse_render, l2_loss, render
+    src = synth.displaced_sphere_scene(subdivisions=args.subdivisions, width=512, height=512, env_size=(64, 32))
+    scene = DiffScene(src, 512, 512, spp=16, depth=4, device=local)
+    albedo, rough, env = scene.source_params(env_size=(256, 128), sun=20.0)
+    n_free = src.materials.shape[0] - 1
+    target = scene.render(albedo, rough, env, seed=12345)
+    a0 = torch.full_like(albedo, 0.5)
+    a0[n_free:] = albedo[n_free:]
+    r0 = torch.full_like(rough, 0.5)
+    r0[n_free:] = rough[n_free:]
+    e0 = torch.full_like(env, float(env.mean()))
+    for _ in range(2):  # warm-up
+        img = scene.render(a0, r0, e0, seed=0)
+        d = 2.0 * (img - target) / (3 * 512 * 512)
+        scene.backward(a0, r0, e0, d, seed=0)
+    reps = 5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fwd_rays = 0
+    for k in range(reps):
+        img = scene.render(a0, r0, e0, seed=k)
+        fwd_rays += scene.rays()
+    fwd_s = time.perf_counter() - t0
+    d = 2.0 * (img - target) / (3 * 512 * 512)
+    d[..., 3] = 0
+    t0 = time.perf_counter()
+    adj_rays = 0
+    for k in range(reps):
+        ga, gr, ge = scene.backward(a0, r0, e0, d, seed=reps - 1)
+        adj_rays += scene.rays()
+    adj_s = time.perf_counter() - t0
+    # central differences at 32 random parameters
+    rng = np.random.default_rng(2024)
+    img = scene.render(a0, r0, e0, seed=7)
+    d = 2.0 * (img - target) / (3 * 512 * 512)
+    d[..., 3] = 0
+    ga, gr, ge = scene.backward(a0, r0, e0, d, seed=7)
+    grads, base = {"albedo": ga, "rough": gr, "env": ge}, {"albedo": a0, "rough": r0, "env": e0}
+    picks = [("albedo", (int(rng.integers(0, n_free)), int(rng.integers(0, 3)))) for _ in range(12)]
+    picks += [("rough", (int(rng.integers(0, n_free)),)) for _ in range(10)]
+    seen = torch.nonzero(ge.abs().sum(-1) > 0).cpu().numpy()
+    picks += [("env", (int(seen[k, 0]), int(seen[k, 1]), int(rng.integers(0, 3))))
+              for k in rng.choice(seen.shape[0], 10, replace=False)]
+    worst, within = 0.0, 0
+    scale = {k: float(v.abs().max()) for k, v in grads.items()}
+    for name, idx in picks:
+        vals = []
+        for sgn in (1.0, -1.0):
+            p = {k: v.clone() for k, v in base.items()}
+            p[name][idx] += sgn * 1e-3
+            vals.append(float(l2_loss(scene.render(p["albedo"], p["rough"], p["env"], seed=7).double(),
+                                      target.double())))
+        fd = (vals[0] - vals[1]) / 2e-3
+        g = float(grads[name][idx])
+        rel = abs(g - fd) / max(abs(fd), 1e-3 * scale[name])
+        worst = max(worst, rel)
+        within += rel <= 0.01
+    # inverse rendering on the common-random-numbers objective (the target's own
+    # seed: deterministic, minimum at the hidden parameters)
+    steps = 200
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a, r, e, hist = inverse_render(scene, target, a0, r0, e0, steps=steps, lr=0.02, n_free=n_free,
+                                   seed_per_step=False, seed=12345)
+    torch.cuda.synchronize()
+    opt_s = time.perf_counter() - t0
+    eval_loss = lambda A, R, E: float(l2_loss(scene.render(A, R, E, seed=12345), target))
+    return {"workload": "icosphere8+openbox 512x512, 16 spp, depth 4; 256 albedos (RGB), 256 roughness, "
+                        "256x128 RGB env (98,304 env values)",
+            "forward": {"value": fwd_rays / fwd_s / 1e6, "unit": "Mrays/s", "ms": 1000 * fwd_s / reps},
+            "adjoint": {"value": adj_rays / adj_s / 1e6, "unit": "Mrays/s", "ms": 1000 * adj_s / reps,
+                        "grads_per_s": reps / adj_s},
+            "adjoint_vs_forward_rays": (adj_rays / adj_s) / (fwd_rays / fwd_s),
+            "finite_differences": {"params": len(picks), "h": 1e-3, "within_1pct": int(within),
+                                   "worst_rel_err": worst},
+            "inverse_rendering": {"steps": steps, "seconds": opt_s, "objective": "L2 to the target, same seed", "loss_first": hist[0], "loss_last": hist[-1],
+                                  "loss_eval_seed_start": eval_loss(a0, r0, e0),
+                                  "loss_eval_seed_end": eval_loss(a, r, e),
+                                  "albedo_mae_start": float((a0[:n_free] - albedo[:n_free]).abs().mean()),
+                                  "albedo_mae_end": float((a[:n_free] - albedo[:n_free]).abs().mean())}}
+
+
 def gpu_arm(args):
     import ctypes as C
 
@@ -465,6 +556,7 @@ def gpu_arm(args):
     forms = None
     if rank == 0 and args.trace_mode != "wide" and not args.no_forms:
         forms = {"wide_bvh": wide_form(ctx, args, B, first_sample, mode)}
+        forms["adjoint"] = adjoint_form(args, local)
 
     if rank == 0:
         peak, peak_kind = load_peak_hbm()

@@ -308,6 +308,42 @@ int pk_diff_backward(pk_ctx* ctx, const pk_diff_camera* cam, const pk_diff_param
 /* Rays traced by the last pk_diff_render / pk_diff_backward call. */
 int pk_diff_rays(pk_ctx* ctx, unsigned long long* rays);
 
+/* ---- form (2): batched rendering (no reference counterpart) -------------
+ * Many render requests over up to 8 resident scenes in one persistent launch:
+ * lanes draw paths (request, sample, pixel) from a shared queue and advance
+ * one bounce per step with the drop-in's shading (shade_hit.wgsl), so a batch
+ * of uneven requests keeps the GPU full.  A frame of the batch (every request
+ * at its spp) is captured once as a CUDA graph and replayed per frame.  The
+ * scene contexts must stay alive and unchanged while the batch exists.
+ * Images are statistically, not bitwise, equal to the drop-in's: the RNG seed
+ * of a hit uses the bounce index where the reference uses the hit-queue slot. */
+typedef struct pk_batch pk_batch;
+typedef struct pk_batch_request {
+  uint32_t scene;            /* index into the scenes of pk_batch_create */
+  uint32_t width, height;
+  uint32_t spp;              /* samples per frame */
+  uint32_t depth;            /* bounces, 1..16 */
+  pk_camera_state camera;    /* invocation_offset ignored */
+} pk_batch_request;
+int pk_batch_create(pk_batch** out, pk_ctx* const* scenes, uint32_t n_scenes);
+int pk_batch_destroy(pk_batch* batch);
+const char* pk_batch_last_error(pk_batch* batch);
+int pk_batch_set_requests(pk_batch* batch, const pk_batch_request* requests, uint32_t n);
+/* Threads per block (64/128/256), shared-memory traversal stack entries
+ * (16/32) and queue chunk (a warp claims chunk*32 paths per atomic, 1..64). */
+int pk_batch_set_config(pk_batch* batch, int block, int stack, int chunk);
+int pk_batch_get_config(pk_batch* batch, int* block, int* stack, int* chunk);
+/* Times every supported configuration on the first sample_paths paths of the
+ * batch (0 = all), keeps the fastest, and clears the accumulation. */
+int pk_batch_autotune(pk_batch* batch, uint64_t sample_paths, float* best_ms);
+/* Renders `frames` frames of every request (graph replay); device time of the
+ * call in pk_batch_info. */
+int pk_batch_render(pk_batch* batch, uint32_t frames);
+int pk_batch_reset(pk_batch* batch);
+/* Mean radiance (width x height x 4 floats) of request `req` over the frames rendered. */
+int pk_batch_read(pk_batch* batch, uint32_t req, float* rgba_mean);
+int pk_batch_info(pk_batch* batch, uint64_t* total_paths, uint32_t* frames, float* last_ms);
+
 #ifdef __cplusplus
 }
 #endif

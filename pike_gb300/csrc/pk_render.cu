@@ -21,17 +21,11 @@ constexpr float SHADE_EPS = 1e-7f;
 // =====================================================================
 // camera.wgsl:75-93 main + createPrimaryRay (:58-73)
 // =====================================================================
-__global__ void __launch_bounds__(128) k_camera(const CamState* __restrict__ camp, Counters* __restrict__ ctr,
-                                                RayQ R, uint32_t n_threads, uint32_t capacity) {
-  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= n_threads) return;
-  const CamState cam = *camp;
-  const uint32_t W = cam.dims_mask >> 16, H = cam.dims_mask & 0xffffu;
-  const uint32_t idx = gid + cam.invocation_offset;
-  const uint32_t px = idx % W, py = idx / W;
-  if (px >= W || py >= H) return;
+// camera.wgsl:54-76 createPrimaryRay for pixel (px, py) of a W x H image.
+__device__ __forceinline__ void camera_ray(const CamState& cam, uint32_t px, uint32_t py, uint32_t W, uint32_t H,
+                                           int32_t samples, V3& org, V3& dir) {
   Hash h;
-  h.seed = (px * 1973u + py * 9277u + (uint32_t)ctr->samples * 26699u) | 1u;
+  h.seed = (px * 1973u + py * 9277u + (uint32_t)samples * 26699u) | 1u;
   h.seed = h.next();
   const float fx = (float)px, fy = (float)py, rx = (float)W, ry = (float)H;
   const float k = cam.distortion;
@@ -54,8 +48,21 @@ __global__ void __launch_bounds__(128) k_camera(const CamState* __restrict__ cam
   const float pw = pow_(h.rand(), cam.bokeh);
   const V3 dof = scale(scale(add(scale(bx, cos_(theta)), scale(by, sin_(theta))), cam.aperture), pw);
   const V3 screen = add(add(add(scale(bx, ux), scale(by, uy)), ed), eo);
-  const V3 dir = normalize(sub(add(screen, scale(dof, cam.focal_depth)), add(eo, dof)));
-  const V3 org = add(dof, eo);
+  dir = normalize(sub(add(screen, scale(dof, cam.focal_depth)), add(eo, dof)));
+  org = add(dof, eo);
+}
+
+__global__ void __launch_bounds__(128) k_camera(const CamState* __restrict__ camp, Counters* __restrict__ ctr,
+                                                RayQ R, uint32_t n_threads, uint32_t capacity) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= n_threads) return;
+  const CamState cam = *camp;
+  const uint32_t W = cam.dims_mask >> 16, H = cam.dims_mask & 0xffffu;
+  const uint32_t idx = gid + cam.invocation_offset;
+  const uint32_t px = idx % W, py = idx / W;
+  if (px >= W || py >= H) return;
+  V3 org, dir;
+  camera_ray(cam, px, py, W, H, ctr->samples, org, dir);
   if (gid < capacity) {
     R.o[gid] = make_float4(org.x, org.y, org.z, 0.0f);
     R.d[gid] = make_float4(dir.x, dir.y, dir.z, 0.0f);
@@ -702,6 +709,85 @@ constexpr int SHADE_THREADS = 128;
 // decoupled look-back, so slot order equals the serial order of the reference.
 // 8 resident blocks per SM (<= 64 registers): more shading warps in flight to
 // cover the attribute/texel/env gathers; a few registers spill to L1.
+// shade_hit.wgsl:407-483 for one hit: the hit record of slot `r` (its
+// position in the hit list, which seeds the RNG) on ray (o4, d4, t4).
+// Returns whether the surface emits (emission contribution in em); eb/es with
+// the bounce and shadow rays as in the reference.
+__device__ __forceinline__ bool shade_one(const SceneDev& sc, const EnvDev& env, float theta, int32_t samples,
+                                          uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr, V3& em, bool& eb,
+                                          float4& bo, float4& bd, float4& bt, bool& es, float4& so, float4& sd,
+                                          float4& st) {
+  bool emitted = false;
+  em = v3(0.0f, 0.0f, 0.0f);
+  const V3 ro = v3(o4.x, o4.y, o4.z), rd = v3(d4.x, d4.y, d4.z);
+  const float ht = __uint_as_float(hr.x);
+  const uint32_t mask = __float_as_uint(t4.w);
+  const uint32_t color_idx = mask & 0x0fffffffu;
+  const uint32_t ray_type = mask & 0xf0000000u;
+  Hash h;
+  h.seed = (r * 1973u + color_idx * 9277u + (uint32_t)samples * 26699u) | 1u;
+  h.seed = h.next();
+  const SI si = surface(sc, ro, rd, ht, (int)hr.y, hr.z);
+  if (h.rand() > si.opacity) {
+    const V3 ao = add(ro, scale(rd, ht + SHADE_EPS * 40.0f));
+    eb = true;
+    bo = make_float4(ao.x, ao.y, ao.z, 0.0f);
+    bd = d4;
+    bt = t4;
+  } else if (dot(si.emission, v3(1.0f, 1.0f, 1.0f)) > 0.0f) {
+    const float att = fmax_(dot(si.n, matvec(si.b1, si.b2, si.n, si.wo)), 0.0f);
+    em = v3(50.0f * si.emission.x * t4.x * att, 50.0f * si.emission.y * t4.y * att,
+            50.0f * si.emission.z * t4.z * att);
+    emitted = true;
+  } else if (ray_type != 0x10000000u) {
+    const V3 m = sample_ggx(h, si);
+    const float f = mix1(schlick(fmax_(dot(si.wo, m), 0.0f), 1.5f), 1.0f, si.metallic);
+    Sample bs;
+    V3 bsdf;
+    if (h.rand() > f) {
+      const float lr = sqrtf(h.rand());
+      const float lphi = c::TAU * h.rand();
+      const float x = lr * cos_(lphi);
+      const float y = lr * sin_(lphi);
+      const float z = sqrtf(fmax_(0.0f, 1.0f - x * x - y * y));
+      bs.wi = v3(x, y, z);
+      bs.pdf = lambert_pdf(bs.wi);
+      bsdf = eval_lambert(si, bs);
+    } else {
+      bs.wi = reflect(neg(si.wo), m);
+      bs.pdf = specular_pdf(si, m);
+      bsdf = eval_specular(si, bs);
+    }
+    if (bs.wi.z > 0.0f) {
+      const V3 dir = matvec(si.b1, si.b2, si.n, bs.wi);
+      const float weight = env.enabled ? power_heuristic(bs.pdf, env_pdf_dir(env, theta, dir)) : 1.0f;
+      eb = true;
+      bo = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
+      bd = make_float4(dir.x, dir.y, dir.z, 0.0f);
+      bt = make_float4(bsdf.x * t4.x * weight, bsdf.y * t4.y * weight, bsdf.z * t4.z * weight, t4.w);
+    }
+    if (env.enabled) {
+      const Sample es_ = sample_env(env, theta, h, si);
+      if (dot(es_.wi, m) > 0.0f && es_.wi.z > 0.0f) {
+        // createMaterialSampleRay (:339-348)
+        const float lw = power_heuristic(es_.pdf, lambert_pdf(es_.wi));
+        const V3 el = eval_lambert(si, es_);
+        V3 scv = scale(v3((1.0f - f) * el.x, (1.0f - f) * el.y, (1.0f - f) * el.z), lw);
+        const V3 hv = normalize(add(si.wo, es_.wi));
+        const float sw = power_heuristic(es_.pdf, specular_pdf(si, hv));
+        const V3 ev = eval_specular(si, es_);
+        scv = add(scv, scale(v3(f * ev.x, f * ev.y, f * ev.z), sw));
+        const V3 sdir = matvec(si.b1, si.b2, si.n, es_.wi);
+        es = true;
+        so = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
+        sd = make_float4(sdir.x, sdir.y, sdir.z, 0.0f);
+        st = make_float4(scv.x * t4.x, scv.y * t4.y, scv.z * t4.z, t4.w);
+      }
+    }
+  }
+  return emitted;
+}
+
 __global__ void __launch_bounds__(SHADE_THREADS, 8) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                           const uint32_t* __restrict__ hit_list,
                                                           const uint4* __restrict__ hrec, RayQ Rin, RayQ Rout,
@@ -737,71 +823,9 @@ __global__ void __launch_bounds__(SHADE_THREADS, 8) k_shade(SceneDev sc, EnvDev 
     }
     if (valid) {
       const float4 o4 = Rin.o[j], d4 = Rin.d[j], t4 = Rin.t[j];
-      const V3 ro = v3(o4.x, o4.y, o4.z), rd = v3(d4.x, d4.y, d4.z);
-      const float ht = __uint_as_float(hr.x);
-      const uint32_t mask = __float_as_uint(t4.w);
-      const uint32_t color_idx = mask & 0x0fffffffu;
-      const uint32_t ray_type = mask & 0xf0000000u;
-      Hash h;
-      h.seed = (r * 1973u + color_idx * 9277u + (uint32_t)samples * 26699u) | 1u;
-      h.seed = h.next();
-      const SI si = surface(sc, ro, rd, ht, (int)hr.y, hr.z);
-      if (h.rand() > si.opacity) {
-        const V3 ao = add(ro, scale(rd, ht + SHADE_EPS * 40.0f));
-        eb = true;
-        bo = make_float4(ao.x, ao.y, ao.z, 0.0f);
-        bd = d4;
-        bt = t4;
-      } else if (dot(si.emission, v3(1.0f, 1.0f, 1.0f)) > 0.0f) {
-        const float att = fmax_(dot(si.n, matvec(si.b1, si.b2, si.n, si.wo)), 0.0f);
-        add_color(color, npix, color_idx, 50.0f * si.emission.x * t4.x * att, 50.0f * si.emission.y * t4.y * att,
-                  50.0f * si.emission.z * t4.z * att, 1.0f, &ctr->err);
-      } else if (ray_type != 0x10000000u) {
-        const V3 m = sample_ggx(h, si);
-        const float f = mix1(schlick(fmax_(dot(si.wo, m), 0.0f), 1.5f), 1.0f, si.metallic);
-        Sample bs;
-        V3 bsdf;
-        if (h.rand() > f) {
-          const float lr = sqrtf(h.rand());
-          const float lphi = c::TAU * h.rand();
-          const float x = lr * cos_(lphi);
-          const float y = lr * sin_(lphi);
-          const float z = sqrtf(fmax_(0.0f, 1.0f - x * x - y * y));
-          bs.wi = v3(x, y, z);
-          bs.pdf = lambert_pdf(bs.wi);
-          bsdf = eval_lambert(si, bs);
-        } else {
-          bs.wi = reflect(neg(si.wo), m);
-          bs.pdf = specular_pdf(si, m);
-          bsdf = eval_specular(si, bs);
-        }
-        if (bs.wi.z > 0.0f) {
-          const V3 dir = matvec(si.b1, si.b2, si.n, bs.wi);
-          const float weight = env.enabled ? power_heuristic(bs.pdf, env_pdf_dir(env, theta, dir)) : 1.0f;
-          eb = true;
-          bo = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
-          bd = make_float4(dir.x, dir.y, dir.z, 0.0f);
-          bt = make_float4(bsdf.x * t4.x * weight, bsdf.y * t4.y * weight, bsdf.z * t4.z * weight, t4.w);
-        }
-        if (env.enabled) {
-          const Sample es_ = sample_env(env, theta, h, si);
-          if (dot(es_.wi, m) > 0.0f && es_.wi.z > 0.0f) {
-            // createMaterialSampleRay (:339-348)
-            const float lw = power_heuristic(es_.pdf, lambert_pdf(es_.wi));
-            const V3 el = eval_lambert(si, es_);
-            V3 scv = scale(v3((1.0f - f) * el.x, (1.0f - f) * el.y, (1.0f - f) * el.z), lw);
-            const V3 hv = normalize(add(si.wo, es_.wi));
-            const float sw = power_heuristic(es_.pdf, specular_pdf(si, hv));
-            const V3 ev = eval_specular(si, es_);
-            scv = add(scv, scale(v3(f * ev.x, f * ev.y, f * ev.z), sw));
-            const V3 sdir = matvec(si.b1, si.b2, si.n, es_.wi);
-            es = true;
-            so = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);
-            sd = make_float4(sdir.x, sdir.y, sdir.z, 0.0f);
-            st = make_float4(scv.x * t4.x, scv.y * t4.y, scv.z * t4.z, t4.w);
-          }
-        }
-      }
+      V3 em;
+      if (shade_one(sc, env, theta, samples, r, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd, st))
+        add_color(color, npix, __float_as_uint(t4.w) & 0x0fffffffu, em.x, em.y, em.z, 1.0f, &ctr->err);
     }
     uint32_t ea, es2, ta, tb;
     block_scan2<SHADE_THREADS / 32>(eb ? 1u : 0u, es ? 1u : 0u, ea, es2, ta, tb, s_warp);
@@ -923,6 +947,174 @@ uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) 
 
 // Persistent grids: enough resident blocks to fill every multiprocessor, never
 // more blocks than there can be work items.
+
+// =====================================================================
+// Form (2): one persistent launch renders many requests (camera, resolution,
+// spp, depth, resident scene).  A path is (request, sample, pixel); lanes
+// take path ids from a warp-local range that one lane refills with a single
+// atomicAdd of chunk * 32 ids, and every lane advances its own path one
+// bounce per iteration (trace, shade_hit, the shadow ray, env on a miss), so
+// lanes whose paths end early pick up new ones without waiting for the
+// warp.  Shading is the drop-in's (shade_one); the slot that seeds its RNG
+// is the bounce index, since no hit queue orders the paths here.
+// =====================================================================
+template <int BLOCK, int SSTACK>
+__global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ scenes, int nscenes,
+                                                 const BatchReq* __restrict__ reqs, int nreq,
+                                                 unsigned long long total, int chunk,
+                                                 unsigned long long* __restrict__ counter,
+                                                 const uint32_t* __restrict__ frame, float4* __restrict__ accum,
+                                                 unsigned long long n_accum, uint32_t* __restrict__ err) {
+  __shared__ int sstack[SSTACK][BLOCK];
+  __shared__ unsigned long long s_begin[BATCH_MAX_REQ + 1];
+  __shared__ BatchScene s_scene[BATCH_MAX_SCENES];
+  for (int i = threadIdx.x; i < nreq; i += BLOCK) s_begin[i] = reqs[i].path_begin;
+  if (threadIdx.x == 0) s_begin[nreq] = total;
+  for (int i = threadIdx.x; i < nscenes; i += BLOCK) s_scene[i] = scenes[i];
+  __syncthreads();
+  const uint32_t fr = *frame;
+  const int lane = threadIdx.x & 31;
+  const uint32_t ltmask = (1u << lane) - 1u;
+  unsigned long long wq_next = 0, wq_end = 0;  // warp-uniform
+  bool warp_done = false;
+  bool have = false;
+  int req = 0, bounce = 0;
+  uint32_t pix = 0;
+  int32_t samples = 0;
+  float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4, t4 = o4;
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xffffffffu, !have);
+    if (idle && !warp_done) {
+      if (wq_next >= wq_end) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk * 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) {
+          warp_done = true;
+        } else {
+          wq_next = base;
+          wq_end = min(base + (unsigned long long)chunk * 32ull, total);
+        }
+      }
+      if (!warp_done) {
+        const unsigned long long avail = wq_end - wq_next;
+        const uint32_t rank = __popc(idle & ltmask);
+        if (!have && rank < avail) {
+          const unsigned long long pid = wq_next + rank;
+          int lo = 0, hi = nreq - 1;  // last request with begin <= pid
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_begin[mid] <= pid) lo = mid; else hi = mid - 1;
+          }
+          req = lo;
+          const BatchReq& q = reqs[req];
+          const unsigned long long local = pid - s_begin[req];
+          const unsigned long long npix = (unsigned long long)q.W * q.H;
+          pix = (uint32_t)(local % npix);
+          samples = (int32_t)(fr * q.spp + (uint32_t)(local / npix));
+          V3 org, dir;
+          camera_ray(q.cam, pix % q.W, pix / q.W, q.W, q.H, samples, org, dir);
+          o4 = make_float4(org.x, org.y, org.z, 0.0f);
+          d4 = make_float4(dir.x, dir.y, dir.z, 0.0f);
+          t4 = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pix));
+          bounce = 0;
+          have = true;
+        }
+        wq_next += min((unsigned long long)__popc(idle), avail);
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) {
+      if (warp_done) break;
+      continue;
+    }
+    if (!have) continue;
+    const BatchReq& q = reqs[req];
+    const BatchScene& S = s_scene[q.scene];
+    const unsigned long long oi = q.out_offset + pix;
+    float t;
+    int idx;
+    uint32_t bary, nf = 0, nt = 0;
+    traverse<false, false, BLOCK, SSTACK>(S.sc, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, t, idx, bary, sstack, err, nf,
+                                          nt);
+    float cr = 0.0f, cg = 0.0f, cb = 0.0f;
+    bool next = false;
+    if (idx < 0) {
+      const V3 e = env_color(S.env, S.theta, v3(d4.x, d4.y, d4.z));
+      cr = e.x * t4.x; cg = e.y * t4.y; cb = e.z * t4.z;
+    } else {
+      bool eb = false, es = false;
+      float4 bo, bd, bt, so, sd, st;
+      V3 em;
+      const uint4 hr = make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u);
+      if (shade_one(S.sc, S.env, S.theta, samples, (uint32_t)bounce, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd,
+                    st)) {
+        cr = em.x; cg = em.y; cb = em.z;
+      }
+      if (es) {
+        float ts;
+        int is;
+        uint32_t bs;
+        traverse<true, false, BLOCK, SSTACK>(S.sc, so.x, so.y, so.z, sd.x, sd.y, sd.z, ts, is, bs, sstack, err, nf,
+                                             nt);
+        if (is < 0) {
+          const V3 e = env_color(S.env, S.theta, v3(sd.x, sd.y, sd.z));
+          cr += e.x * st.x; cg += e.y * st.y; cb += e.z * st.z;
+        }
+      }
+      if (eb && bounce + 1 < (int)q.depth) {
+        o4 = bo; d4 = bd; t4 = bt;
+        bounce++;
+        next = true;
+      }
+    }
+    if (cr != 0.0f || cg != 0.0f || cb != 0.0f) {
+      if (oi < n_accum) {
+        atomicAdd(&accum[oi].x, cr);
+        atomicAdd(&accum[oi].y, cg);
+        atomicAdd(&accum[oi].z, cb);
+      } else {
+        atomicOr(err, ERR_PIXEL);
+      }
+    }
+    have = next;
+  }
+}
+
+__global__ void k_batch_next_frame(uint32_t* frame) { *frame += 1u; }
+
+#define PK_BATCH_CONFIGS(X) X(64, 16) X(64, 32) X(128, 16) X(128, 32) X(256, 16) X(256, 32)
+
+bool batch_config_ok(const BatchConfig& c) {
+#define PK_B_OK(B, S) if (c.block == B && c.stack == S) return c.chunk >= 1 && c.chunk <= 64;
+  PK_BATCH_CONFIGS(PK_B_OK)
+#undef PK_B_OK
+  return false;
+}
+
+int batch_blocks_per_sm(const BatchConfig& c) {
+  int n = 0;
+#define PK_B_OCC(B, S) \
+  if (c.block == B && c.stack == S) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<B, S>, B, 0);
+  PK_BATCH_CONFIGS(PK_B_OCC)
+#undef PK_B_OCC
+  return n;
+}
+
+void launch_batch(cudaStream_t s, const BatchConfig& c, unsigned grid, const BatchScene* scenes, int nscenes,
+                  const BatchReq* reqs, int nreq, unsigned long long total, unsigned long long* counter,
+                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err) {
+#define PK_B_LAUNCH(B, S)                                                                                          \
+  if (c.block == B && c.stack == S) {                                                                              \
+    k_batch<B, S><<<grid, B, 0, s>>>(scenes, nscenes, reqs, nreq, total, c.chunk, counter, frame, accum, n_accum, \
+                                     err);                                                                         \
+    return;                                                                                                        \
+  }
+  PK_BATCH_CONFIGS(PK_B_LAUNCH)
+#undef PK_B_LAUNCH
+}
+
+void launch_batch_next_frame(cudaStream_t s, uint32_t* frame) { k_batch_next_frame<<<1, 1, 0, s>>>(frame); }
+
 void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade,
                   unsigned* trace_wide) {
   int t = 0, c = 0, s = 0, w = 0;

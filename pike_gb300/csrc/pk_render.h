@@ -63,4 +63,29 @@ void launch_flatten(cudaStream_t s, const double* pos3, const double* nrm3, cons
                     const double* bt4, const double* uv2, uint32_t n, double scale, double tx, double ty, double tz,
                     double* pos_out3, uint4* attrs);
 
+// ---- form (2): persistent multi-request batch (pk_batch.cu drives it) ----
+struct BatchScene {
+  SceneDev sc;
+  EnvDev env;
+  float theta;
+};
+struct BatchReq {
+  CamState cam;
+  uint32_t scene, W, H, spp, depth;
+  unsigned long long path_begin;  // first path id of this request
+  unsigned long long out_offset;  // first accumulation pixel of this request
+};
+constexpr int BATCH_MAX_SCENES = 8;
+constexpr int BATCH_MAX_REQ = 1024;
+struct BatchConfig {
+  int block, stack, chunk;  // threads per block, shared-memory stack entries, warp grab = chunk * 32 paths
+};
+// false for a configuration without a kernel instantiation
+bool batch_config_ok(const BatchConfig& c);
+int batch_blocks_per_sm(const BatchConfig& c);
+void launch_batch(cudaStream_t s, const BatchConfig& c, unsigned grid, const BatchScene* scenes, int nscenes,
+                  const BatchReq* reqs, int nreq, unsigned long long total, unsigned long long* counter,
+                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err);
+void launch_batch_next_frame(cudaStream_t s, uint32_t* frame);
+
 }  // namespace pk

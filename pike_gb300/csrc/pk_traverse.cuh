@@ -70,10 +70,12 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
   }
 }
 
-template <bool ANY, bool COUNT>
+// BLOCK threads per block share `sstack` (SSTACK entries per thread in shared
+// memory, STACK_LOCAL more in local memory).
+template <bool ANY, bool COUNT, int BLOCK = TRACE_THREADS, int SSTACK = STACK_SMEM>
 __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
                                          float dz, float& best_t, int& best_i, uint32_t& best_b,
-                                         int (*sstack)[TRACE_THREADS], uint32_t* err, uint32_t& nfetch,
+                                         int (*sstack)[BLOCK], uint32_t* err, uint32_t& nfetch,
                                          uint32_t& ntest) {
   const float eps = ANY ? 1e-7f : 1e-8f;
   const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
@@ -94,8 +96,8 @@ __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy,
       if (lok && rok) {
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
-        if (sp < STACK_SMEM) sstack[sp][tid] = farc;
-        else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+        if (sp < SSTACK) sstack[sp][tid] = farc;
+        else if (sp < SSTACK + STACK_LOCAL) lstack[sp - SSTACK] = farc;
         else { atomicOr(err, ERR_STACK); break; }
         ++sp;
         cur = nearc;
@@ -135,7 +137,7 @@ __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy,
     }
     if (sp == 0) break;
     --sp;
-    cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+    cur = sp < SSTACK ? sstack[sp][tid] : lstack[sp - SSTACK];
   }
 }
 

@@ -154,9 +154,12 @@ def l2_loss(image, target):
 
 
 def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 200, lr: float = 0.02,
-                   n_free: int | None = None, seed_per_step: bool = True):
+                   n_free: int | None = None, seed_per_step: bool = True, seed: int = 0):
     """Adam on (albedo, roughness, env) towards the target image; materials at
-    index >= n_free stay fixed.  Returns the parameters and the loss history."""
+    index >= n_free stay fixed.  Step k renders with seed + k (fresh samples)
+    or, with seed_per_step=False, always with `seed` (common random numbers:
+    a deterministic objective; with the target's seed its minimum is the
+    target's parameters).  Returns the parameters and the loss history."""
     import torch
     a = albedo.clone().requires_grad_(True)
     r = rough.clone().requires_grad_(True)
@@ -168,7 +171,7 @@ def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 20
     hist = []
     for k in range(steps):
         opt.zero_grad()
-        loss = l2_loss(render(scene, a, r, e, seed=k if seed_per_step else 0), target)
+        loss = l2_loss(render(scene, a, r, e, seed=seed + k if seed_per_step else seed), target)
         loss.backward()
         opt.step()
         with torch.no_grad():
