@@ -471,6 +471,72 @@ def adjoint_form(args, local: int):
                                   "albedo_mae_end": float((a[:n_free] - albedo[:n_free]).abs().mean())}}
 
 
+def batch_form(args, local: int):
+    """Form (2), the batching workload: 64 requests over three resident scenes
+    (ground + 833 boxes = 9,998 triangles; icosphere7 + box = 327,690;
+    icosphere8 + box = 1,310,730), resolutions log-uniform 128x128..1920x1080,
+    spp in {1,4,16,64}, depth 4..8, random orbit cameras.  One persistent
+    launch (autotuned) against the same requests run one after another,
+    through the batch kernel and through the drop-in pipeline."""
+    import numpy as np
+    from pike_gb300 import synth
+    from pike_gb300._lib import ptr
+    from pike_gb300.batch import Batch, random_requests, scene_context
+    srcs = [synth.small_scene(n_boxes=833), synth.displaced_sphere_scene(subdivisions=7, width=16, height=16),
+            synth.displaced_sphere_scene(subdivisions=args.subdivisions, width=16, height=16)]
+    ctxs = [scene_context(s, local) for s in srcs]
+    reqs = sorted(random_requests(64, 3, seed=2025), key=lambda r: r.paths)  # shortest first, in both runs
+    batch = Batch(ctxs)
+    batch.set_requests(reqs)
+    total_paths = batch.info()[0]
+    tune_ms = batch.autotune(sample_paths=min(total_paths, 32_000_000))
+    cfg = batch.config()
+    batch.render(1)  # graph capture + warm-up
+    batch.reset()
+    batch_ms = batch.render(1)
+    lat = batch.latencies()
+    # one request at a time through the same kernel
+    seq_batch = []
+    for r in reqs:
+        batch.set_requests([r])
+        batch.render(1)
+        batch.reset()
+        seq_batch.append(batch.render(1))
+    batch.close()
+    # one request at a time through the drop-in pipeline (spp frames of depth bounces)
+    from pike_gb300.batch import _camera_struct
+    seq_plain = []
+    for r in reqs:
+        ctx = ctxs[r.scene]
+        ctx.call("pk_configure", r.width, r.height, r.width * r.height)
+        ctx.call("pk_set_camera", _camera_struct(r.camera))
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_render_frames", 1, r.depth)  # warm-up (graph capture at this size)
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_sync")
+        ctx.timer_start()
+        ctx.call("pk_render_frames", r.spp, r.depth)
+        seq_plain.append(ctx.timer_stop())
+    for c in ctxs:
+        c.close()
+    done_b = np.cumsum(seq_batch)
+    done_p = np.cumsum(seq_plain)
+    return {"workload": "64 requests, 3 resident scenes (9,998 / 327,690 / 1,310,730 triangles), "
+                        "128x128..1920x1080 log-uniform, spp {1,4,16,64}, depth 4..8, orbit cameras",
+            "paths": int(total_paths), "autotuned": {"block": cfg[0], "stack": cfg[1], "chunk": cfg[2],
+                                                     "sample_ms": tune_ms},
+            "batch_ms": batch_ms, "paths_per_s": total_paths / (batch_ms / 1000.0),
+            "request_order": "ascending path count (shortest first) in every column",
+            "batch_latency_ms": {"mean": float(lat.mean()), "median": float(np.median(lat)),
+                                 "max": float(lat.max())},
+            "sequential_same_kernel": {"total_ms": float(done_b[-1]), "mean_latency_ms": float(done_b.mean())},
+            "sequential_dropin": {"total_ms": float(done_p[-1]), "mean_latency_ms": float(done_p.mean())},
+            "speedup_vs_sequential_same_kernel": float(done_b[-1]) / batch_ms,
+            "speedup_vs_sequential_dropin": float(done_p[-1]) / batch_ms,
+            "note": "batch images equal the drop-in's in distribution; the drop-in column renders spp frames "
+                    "of 1 sample each (its wavefront queues are sized per request)"}
+
+
 def gpu_arm(args):
     import ctypes as C
 
@@ -557,6 +623,7 @@ def gpu_arm(args):
     if rank == 0 and args.trace_mode != "wide" and not args.no_forms:
         forms = {"wide_bvh": wide_form(ctx, args, B, first_sample, mode)}
         forms["adjoint"] = adjoint_form(args, local)
+        forms["batching"] = batch_form(args, local)
 
     if rank == 0:
         peak, peak_kind = load_peak_hbm()

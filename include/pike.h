@@ -343,6 +343,11 @@ int pk_batch_reset(pk_batch* batch);
 /* Mean radiance (width x height x 4 floats) of request `req` over the frames rendered. */
 int pk_batch_read(pk_batch* batch, uint32_t req, float* rgba_mean);
 int pk_batch_info(pk_batch* batch, uint64_t* total_paths, uint32_t* frames, float* last_ms);
+/* Completion time of each request in the last rendered frame, in ms from the
+ * start of that frame's launch (the lane that retires a request's last path
+ * stamps the GPU global timer).  Requests are served in the order given, so
+ * listing small requests first lowers the mean latency. */
+int pk_batch_latencies(pk_batch* batch, float* ms);
 
 #ifdef __cplusplus
 }

@@ -156,6 +156,12 @@ class Batch:
         self._call("pk_batch_info", C.byref(n), C.byref(f), C.byref(ms))
         return int(n.value), int(f.value), float(ms.value)
 
+    def latencies(self) -> np.ndarray:
+        """Per-request completion times (ms from the launch) of the last frame."""
+        out = np.zeros(len(self.requests), np.float32)
+        self._call("pk_batch_latencies", ptr(out))
+        return out
+
     def image(self, i: int) -> np.ndarray:
         r = self.requests[i]
         out = np.zeros((r.height, r.width, 4), np.float32)

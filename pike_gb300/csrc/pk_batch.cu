@@ -29,6 +29,7 @@ struct pk_batch {
   DevBuf<float4> accum;
   DevBuf<unsigned long long> counter;
   DevBuf<uint32_t> frame, errflag;
+  DevBuf<unsigned long long> remaining, remaining_init, done_ns;  // per request; done_ns[n] = launch start
   unsigned long long total = 0, n_accum = 0;
   BatchConfig cfg{128, 32, 4};
   unsigned grid = 1;
@@ -72,8 +73,11 @@ unsigned grid_for_cfg(pk_batch* b, const BatchConfig& c) {
 
 void enqueue_frame(pk_batch* b, const BatchConfig& c, unsigned grid, unsigned long long total) {
   check(cudaMemsetAsync(b->counter.p, 0, 8, b->stream), "memset");
+  check(cudaMemcpyAsync(b->remaining.p, b->remaining_init.p, b->remaining.bytes(), cudaMemcpyDeviceToDevice,
+                        b->stream), "D2D");
+  check(cudaMemsetAsync(b->done_ns.p, 0, b->done_ns.bytes(), b->stream), "memset");
   launch_batch(b->stream, c, grid, b->d_scenes.p, (int)b->scenes.size(), b->d_reqs.p, (int)b->reqs.size(), total,
-               b->counter.p, b->frame.p, b->accum.p, b->n_accum, b->errflag.p);
+               b->counter.p, b->frame.p, b->accum.p, b->n_accum, b->errflag.p, b->remaining.p, b->done_ns.p);
   check(cudaGetLastError(), "k_batch");
   launch_batch_next_frame(b->stream, b->frame.p);
 }
@@ -139,6 +143,9 @@ int pk_batch_destroy(pk_batch* b) {
   b->counter.release();
   b->frame.release();
   b->errflag.release();
+  b->remaining.release();
+  b->remaining_init.release();
+  b->done_ns.release();
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PK_OK;
@@ -184,6 +191,12 @@ int pk_batch_set_requests(pk_batch* b, const pk_batch_request* reqs, uint32_t n)
     b->n_accum = pixels;
     b->d_reqs.alloc(n);
     check(cudaMemcpyAsync(b->d_reqs.p, v.data(), n * sizeof(BatchReq), cudaMemcpyHostToDevice, b->stream), "H2D");
+    std::vector<unsigned long long> counts(n);
+    for (uint32_t i = 0; i < n; i++) counts[i] = (unsigned long long)v[i].W * v[i].H * v[i].spp;
+    b->remaining.alloc(n);
+    b->remaining_init.alloc(n);
+    b->done_ns.alloc(n + 1);
+    check(cudaMemcpyAsync(b->remaining_init.p, counts.data(), n * 8, cudaMemcpyHostToDevice, b->stream), "H2D");
     b->accum.alloc(pixels);
     reset_accum(b);
     check(cudaStreamSynchronize(b->stream), "sync");
@@ -285,6 +298,18 @@ int pk_batch_read(pk_batch* b, uint32_t req, float* rgba_mean) {
     check(cudaStreamSynchronize(b->stream), "sync");
     const float inv = b->frames ? 1.0f / ((float)b->frames * (float)q.spp) : 0.0f;
     for (size_t i = 0; i < 4 * n; i++) rgba_mean[i] *= inv;
+    return PK_OK;
+  });
+}
+
+int pk_batch_latencies(pk_batch* b, float* ms) {
+  return bguard(b, [&]() {
+    if (!ms || b->reqs.empty()) return bfail(b, PK_ERR_ARG, "no requests or null output");
+    std::vector<unsigned long long> t(b->reqs.size() + 1);
+    check(cudaMemcpyAsync(t.data(), b->done_ns.p, t.size() * 8, cudaMemcpyDeviceToHost, b->stream), "D2H");
+    check(cudaStreamSynchronize(b->stream), "sync");
+    const unsigned long long t0 = t[b->reqs.size()];
+    for (size_t i = 0; i < b->reqs.size(); i++) ms[i] = t[i] >= t0 ? (float)((double)(t[i] - t0) * 1e-6) : -1.0f;
     return PK_OK;
   });
 }

@@ -958,19 +958,28 @@ uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) 
 // warp.  Shading is the drop-in's (shade_one); the slot that seeds its RNG
 // is the bounce index, since no hit queue orders the paths here.
 // =====================================================================
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 template <int BLOCK, int SSTACK>
 __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ scenes, int nscenes,
                                                  const BatchReq* __restrict__ reqs, int nreq,
                                                  unsigned long long total, int chunk,
                                                  unsigned long long* __restrict__ counter,
                                                  const uint32_t* __restrict__ frame, float4* __restrict__ accum,
-                                                 unsigned long long n_accum, uint32_t* __restrict__ err) {
+                                                 unsigned long long n_accum, uint32_t* __restrict__ err,
+                                                 unsigned long long* __restrict__ remaining,
+                                                 unsigned long long* __restrict__ done_ns) {
   __shared__ int sstack[SSTACK][BLOCK];
   __shared__ unsigned long long s_begin[BATCH_MAX_REQ + 1];
   __shared__ BatchScene s_scene[BATCH_MAX_SCENES];
   for (int i = threadIdx.x; i < nreq; i += BLOCK) s_begin[i] = reqs[i].path_begin;
   if (threadIdx.x == 0) s_begin[nreq] = total;
   for (int i = threadIdx.x; i < nscenes; i += BLOCK) s_scene[i] = scenes[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) done_ns[nreq] = globaltimer_ns();  // launch start
   __syncthreads();
   const uint32_t fr = *frame;
   const int lane = threadIdx.x & 31;
@@ -1027,56 +1036,66 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
       if (warp_done) break;
       continue;
     }
-    if (!have) continue;
-    const BatchReq& q = reqs[req];
-    const BatchScene& S = s_scene[q.scene];
-    const unsigned long long oi = q.out_offset + pix;
-    float t;
-    int idx;
-    uint32_t bary, nf = 0, nt = 0;
-    traverse<false, false, BLOCK, SSTACK>(S.sc, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, t, idx, bary, sstack, err, nf,
-                                          nt);
-    float cr = 0.0f, cg = 0.0f, cb = 0.0f;
-    bool next = false;
-    if (idx < 0) {
-      const V3 e = env_color(S.env, S.theta, v3(d4.x, d4.y, d4.z));
-      cr = e.x * t4.x; cg = e.y * t4.y; cb = e.z * t4.z;
-    } else {
-      bool eb = false, es = false;
-      float4 bo, bd, bt, so, sd, st;
-      V3 em;
-      const uint4 hr = make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u);
-      if (shade_one(S.sc, S.env, S.theta, samples, (uint32_t)bounce, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd,
-                    st)) {
-        cr = em.x; cg = em.y; cb = em.z;
-      }
-      if (es) {
-        float ts;
-        int is;
-        uint32_t bs;
-        traverse<true, false, BLOCK, SSTACK>(S.sc, so.x, so.y, so.z, sd.x, sd.y, sd.z, ts, is, bs, sstack, err, nf,
-                                             nt);
-        if (is < 0) {
-          const V3 e = env_color(S.env, S.theta, v3(sd.x, sd.y, sd.z));
-          cr += e.x * st.x; cg += e.y * st.y; cb += e.z * st.z;
+    bool finished = false;
+    if (have) {
+      const BatchReq& q = reqs[req];
+      const BatchScene& S = s_scene[q.scene];
+      const unsigned long long oi = q.out_offset + pix;
+      float t;
+      int idx;
+      uint32_t bary, nf = 0, nt = 0;
+      traverse<false, false, BLOCK, SSTACK>(S.sc, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, t, idx, bary, sstack, err, nf,
+                                            nt);
+      float cr = 0.0f, cg = 0.0f, cb = 0.0f;
+      bool next = false;
+      if (idx < 0) {
+        const V3 e = env_color(S.env, S.theta, v3(d4.x, d4.y, d4.z));
+        cr = e.x * t4.x; cg = e.y * t4.y; cb = e.z * t4.z;
+      } else {
+        bool eb = false, es = false;
+        float4 bo, bd, bt, so, sd, st;
+        V3 em;
+        const uint4 hr = make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u);
+        if (shade_one(S.sc, S.env, S.theta, samples, (uint32_t)bounce, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd,
+                      st)) {
+          cr = em.x; cg = em.y; cb = em.z;
+        }
+        if (es) {
+          float ts;
+          int is;
+          uint32_t bs;
+          traverse<true, false, BLOCK, SSTACK>(S.sc, so.x, so.y, so.z, sd.x, sd.y, sd.z, ts, is, bs, sstack, err, nf,
+                                               nt);
+          if (is < 0) {
+            const V3 e = env_color(S.env, S.theta, v3(sd.x, sd.y, sd.z));
+            cr += e.x * st.x; cg += e.y * st.y; cb += e.z * st.z;
+          }
+        }
+        if (eb && bounce + 1 < (int)q.depth) {
+          o4 = bo; d4 = bd; t4 = bt;
+          bounce++;
+          next = true;
         }
       }
-      if (eb && bounce + 1 < (int)q.depth) {
-        o4 = bo; d4 = bd; t4 = bt;
-        bounce++;
-        next = true;
+      if (cr != 0.0f || cg != 0.0f || cb != 0.0f) {
+        if (oi < n_accum) {
+          atomicAdd(&accum[oi].x, cr);
+          atomicAdd(&accum[oi].y, cg);
+          atomicAdd(&accum[oi].z, cb);
+        } else {
+          atomicOr(err, ERR_PIXEL);
+        }
       }
+      finished = !next;
+      have = next;
     }
-    if (cr != 0.0f || cg != 0.0f || cb != 0.0f) {
-      if (oi < n_accum) {
-        atomicAdd(&accum[oi].x, cr);
-        atomicAdd(&accum[oi].y, cg);
-        atomicAdd(&accum[oi].z, cb);
-      } else {
-        atomicOr(err, ERR_PIXEL);
-      }
+    // per-request completion: one atomic per request per warp step; the lane
+    // that retires a request's last path stamps its completion time
+    const unsigned peers = __match_any_sync(0xffffffffu, finished ? req : -1);
+    if (finished && (int)(threadIdx.x & 31u) == __ffs(peers) - 1) {
+      const unsigned long long n = (unsigned long long)__popc(peers);
+      if (atomicAdd(&remaining[req], (unsigned long long)(-(long long)n)) == n) done_ns[req] = globaltimer_ns();
     }
-    have = next;
   }
 }
 
@@ -1102,11 +1121,12 @@ int batch_blocks_per_sm(const BatchConfig& c) {
 
 void launch_batch(cudaStream_t s, const BatchConfig& c, unsigned grid, const BatchScene* scenes, int nscenes,
                   const BatchReq* reqs, int nreq, unsigned long long total, unsigned long long* counter,
-                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err) {
+                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err,
+                  unsigned long long* remaining, unsigned long long* done_ns) {
 #define PK_B_LAUNCH(B, S)                                                                                          \
   if (c.block == B && c.stack == S) {                                                                              \
     k_batch<B, S><<<grid, B, 0, s>>>(scenes, nscenes, reqs, nreq, total, c.chunk, counter, frame, accum, n_accum, \
-                                     err);                                                                         \
+                                     err, remaining, done_ns);                                                     \
     return;                                                                                                        \
   }
   PK_BATCH_CONFIGS(PK_B_LAUNCH)

@@ -85,7 +85,8 @@ bool batch_config_ok(const BatchConfig& c);
 int batch_blocks_per_sm(const BatchConfig& c);
 void launch_batch(cudaStream_t s, const BatchConfig& c, unsigned grid, const BatchScene* scenes, int nscenes,
                   const BatchReq* reqs, int nreq, unsigned long long total, unsigned long long* counter,
-                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err);
+                  uint32_t* frame, float4* accum, unsigned long long n_accum, uint32_t* err,
+                  unsigned long long* remaining, unsigned long long* done_ns);
 void launch_batch_next_frame(cudaStream_t s, uint32_t* frame);
 
 }  // namespace pk

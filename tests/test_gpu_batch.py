@@ -65,6 +65,8 @@ def test_duplicate_requests_agree_and_shapes(scenes):
     assert np.allclose(a, c, rtol=1e-5, atol=1e-6)  # same paths; only the summation order may differ
     n, frames, ms = batch.info()
     assert n == 96 * 64 * 4 * 2 + 40 * 30 * 16 and frames == 2 and ms > 0
+    lat = batch.latencies()  # of the last frame
+    assert (lat > 0).all() and (lat <= ms).all()
 
 
 def test_configurations_agree(scenes):
