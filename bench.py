@@ -537,6 +537,31 @@ def batch_form(args, local: int):
                     "of 1 sample each (its wavefront queues are sized per request)"}
 
 
+def binned_form(ctx, args, B: int, first_sample: int, sweep_ms: float):
+    """The binned SAH build (PK_BVH_BINNED) of the same scene: build time and
+    the drop-in frame rate on its tree (a different topology from bvh.js)."""
+    from pike_gb300 import _lib
+    times = []
+    for _ in range(3):
+        ctx.call("pk_sync")
+        ctx.timer_start()
+        ctx.call("pk_bvh_build", _lib.PK_BVH_BINNED)
+        times.append(ctx.timer_stop())
+    ctx.call("pk_set_trace_mode", _lib.PK_TRACE_PERSISTENT)
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", 2, B)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_sync")
+    steps = max(1, min(args.steps, 32))
+    ctx.timer_start()
+    ctx.call("pk_render_frames", steps, B)
+    ms = ctx.timer_stop()
+    rays = read_stats(ctx)["rays_traced"]
+    return {"build_ms": min(times), "sweep_build_ms": sweep_ms, "value": rays / (ms / 1000.0) / 1e6, "unit": UNIT,
+            "ms_per_step": ms / steps, "note": "binned SAH, 16 bins, leaves <= 8; frames differ from the reference's"}
+
+
 def gpu_arm(args):
     import ctypes as C
 
@@ -624,6 +649,7 @@ def gpu_arm(args):
         forms = {"wide_bvh": wide_form(ctx, args, B, first_sample, mode)}
         forms["adjoint"] = adjoint_form(args, local)
         forms["batching"] = batch_form(args, local)
+        forms["binned_bvh"] = binned_form(ctx, args, B, first_sample, bvh_ms)
 
     if rank == 0:
         peak, peak_kind = load_peak_hbm()

@@ -120,6 +120,11 @@ int pk_materials_download(pk_ctx* ctx, uint32_t* n_mats, uint32_t* n_layers, int
  * mode PK_BVH_SWEEP: the reference's full-sweep object SAH (same topology,
  * primitive order and quantised boxes as bvh.js). */
 #define PK_BVH_SWEEP 0
+/* mode PK_BVH_BINNED: a binned SAH build (16 bins per axis, leaves of at
+ * most 8 triangles) in the same layout; NOT the reference's topology, so
+ * frames differ from the reference's; for callers that want a fast build
+ * (no reference counterpart). */
+#define PK_BVH_BINNED 1
 int pk_bvh_build(pk_ctx* ctx, int mode);
 /* Upload a BVH serialised by the reference: nodes5 = n_nodes * BVHNodeStruct
  * {childBaseIdx, triangles, xMask, yMask, zMask} (20 B), tri4_leaf = leaf-ordered

@@ -18,6 +18,7 @@ HEADER = os.path.join(HERE, "..", "include", "pike.h")
 
 PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED = range(6)
 PK_BVH_SWEEP = 0
+PK_BVH_BINNED = 1
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
 PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE = 0, 1, 2, 4
 

@@ -364,12 +364,14 @@ int pk_bvh_upload(pk_ctx* c, const int32_t* nodes5, uint32_t n_nodes, const int3
 
 int pk_bvh_build(pk_ctx* c, int mode) {
   return guarded(c, [&]() {
-    if (mode != PK_BVH_SWEEP) return fail(c, PK_ERR_UNSUPPORTED, "unknown BVH mode");
+    if (mode != PK_BVH_SWEEP && mode != PK_BVH_BINNED) return fail(c, PK_ERR_UNSUPPORTED, "unknown BVH mode");
     if (!c->pos.p || !c->n_tris) return fail(c, PK_ERR_STATE, "no scene");
     BvhOut out;
     std::string why;
-    if (build_bvh_sweep(c->stream, c->pos.p, c->n_verts, c->tri4.p, c->n_tris, out, why))
-      return fail(c, PK_ERR_ARG, "pk_bvh_build: " + why);
+    const int rc = mode == PK_BVH_SWEEP
+                       ? build_bvh_sweep(c->stream, c->pos.p, c->n_verts, c->tri4.p, c->n_tris, out, why)
+                       : build_bvh_binned(c->stream, c->pos.p, c->n_verts, c->tri4.p, c->n_tris, out, why);
+    if (rc) return fail(c, PK_ERR_ARG, "pk_bvh_build: " + why);
     c->nodes5 = std::move(out.nodes5);
     c->node_box_d = std::move(out.node_box);
     c->tri4_leaf = std::move(out.tri4_leaf);

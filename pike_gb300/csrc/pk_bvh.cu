@@ -13,6 +13,9 @@
 // minimum in (axis, index) order is the reference's strict `<` winner.
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <vector>
+
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -633,6 +636,547 @@ int build_bvh_sweep(cudaStream_t s, const double* pos3, uint32_t n_verts, const 
   check(cudaMemcpyAsync(out.node_box.p, node_box.p, (size_t)n_nodes * sizeof(Box6), cudaMemcpyDeviceToDevice, s),
         "memcpy");
   check(cudaGetLastError(), "bvh pack");
+  check(cudaStreamSynchronize(s), "sync");
+  out.n_nodes = n_nodes;
+  out.n_leaf_tris = T;
+  out.depth = depth;
+  for (int i = 0; i < 3; i++) out.norm[i] = center[i];
+  out.norm[3] = 2.0 / longest;
+  return 0;
+}
+
+
+// =====================================================================
+// Binned SAH builder (PK_BVH_BINNED): not the reference's topology; a fast
+// build for callers that do not need bit parity with bvh.js.
+//
+// Phase 1, level-synchronous over nodes of more than BIN_SMALL triangles:
+// each block bins one tile of one node (16 bins per axis by centroid, counts
+// and exact double boxes through order-preserving 64-bit keys in shared
+// memory, flushed with global atomics), one warp per node scans the bins for
+// the cheapest SAH split, and a stable partition (global scan of the
+// left flags) keeps every node's triangles contiguous.  Phase 2: one block
+// per remaining node builds its whole subtree in place with the same binned
+// SAH, allocating child pairs with an atomic counter (children always get
+// larger indices than their parent).  Leaves hold at most BIN_MAX_LEAF
+// triangles; a node whose centroids share one bin is split at its middle.
+// =====================================================================
+namespace {
+
+constexpr int NB = 16;
+constexpr uint32_t BIN_SMALL = 1024;
+constexpr uint32_t BIN_MAX_LEAF = 8;
+constexpr int BIN_TILE = 2048;
+constexpr int BIN_THREADS = 256;
+constexpr double C_TRAV = 1.0;
+
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dval(unsigned long long k) {
+  const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return __longlong_as_double((long long)u);
+}
+
+// One bin: count, triangle-box bounds and centroid bounds as 64-bit keys.
+struct Bin {
+  unsigned long long bmin[3], bmax[3], cmin[3], cmax[3];
+  unsigned int n, pad;
+};
+__device__ __forceinline__ void bin_clear(Bin& b) {
+  for (int a = 0; a < 3; a++) { b.bmin[a] = b.cmin[a] = ~0ull; b.bmax[a] = b.cmax[a] = 0ull; }
+  b.n = 0;
+}
+template <bool GLOBAL>
+__device__ __forceinline__ void bin_add(Bin& b, const Box6& box, const double* c) {
+  atomicAdd(&b.n, 1u);
+  for (int a = 0; a < 3; a++) {
+    atomicMin(&b.bmin[a], dkey(box.mn[a]));
+    atomicMax(&b.bmax[a], dkey(box.mx[a]));
+    atomicMin(&b.cmin[a], dkey(c[a]));
+    atomicMax(&b.cmax[a], dkey(c[a]));
+  }
+}
+__device__ __forceinline__ void bin_merge_global(Bin& dst, const Bin& src) {
+  if (!src.n) return;
+  atomicAdd(&dst.n, src.n);
+  for (int a = 0; a < 3; a++) {
+    atomicMin(&dst.bmin[a], src.bmin[a]);
+    atomicMax(&dst.bmax[a], src.bmax[a]);
+    atomicMin(&dst.cmin[a], src.cmin[a]);
+    atomicMax(&dst.cmax[a], src.cmax[a]);
+  }
+}
+
+struct NodeInfo {
+  uint32_t start, count, node;   // element range in the permutation, node index
+  int axis, split;               // chosen split: axis and last left bin (-1: middle split)
+  uint32_t nleft;
+  double cmin[3], cmax[3];       // centroid bounds of the node
+  double lcmin[3], lcmax[3], rcmin[3], rcmax[3];
+};
+
+__device__ __forceinline__ int bin_of(double c, double lo, double hi) {
+  const double ext = hi - lo;
+  if (!(ext > 0.0)) return 0;
+  int b = (int)((c - lo) * ((double)NB / ext));
+  return b < 0 ? 0 : (b >= NB ? NB - 1 : b);
+}
+
+__device__ __forceinline__ void centroid(const Box6& b, double* c) {
+  for (int a = 0; a < 3; a++) c[a] = (b.mn[a] + b.mx[a]) * 0.5;
+}
+
+__global__ void k_tri_boxes_plain(const double* __restrict__ pos3, const int4* __restrict__ tri4, uint32_t n,
+                                  Box6* __restrict__ boxes, uint32_t* __restrict__ ids) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int4 tr = tri4[t];
+  const int v[3] = {tr.x, tr.y, tr.z};
+  Box6 b = box_empty();
+  for (int k = 0; k < 3; k++) {
+    const double* p = pos3 + 3 * (size_t)v[k];
+    for (int a = 0; a < 3; a++) { b.mn[a] = fmin(p[a], b.mn[a]); b.mx[a] = fmax(p[a], b.mx[a]); }
+  }
+  boxes[t] = b;
+  ids[t] = t;
+}
+
+// Root box and centroid bounds (one bin holding everything).
+__global__ void k_root_bounds(const Box6* __restrict__ boxes, uint32_t n, Bin* __restrict__ root) {
+  __shared__ Bin s;
+  if (threadIdx.x == 0) bin_clear(s);
+  __syncthreads();
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const Box6 b = boxes[t];
+    double c[3];
+    centroid(b, c);
+    bin_add<false>(s, b, c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) bin_merge_global(*root, s);
+}
+
+struct Tile {
+  uint32_t slot, begin, count;
+};
+
+__global__ void __launch_bounds__(BIN_THREADS) k_bin_tiles(const Tile* __restrict__ tiles,
+                                                           const NodeInfo* __restrict__ nodes,
+                                                           const uint32_t* __restrict__ A,
+                                                           const Box6* __restrict__ boxes, Bin* __restrict__ bins) {
+  __shared__ Bin s[3 * NB];
+  const Tile t = tiles[blockIdx.x];
+  const NodeInfo& nd = nodes[t.slot];
+  for (int i = threadIdx.x; i < 3 * NB; i += BIN_THREADS) bin_clear(s[i]);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < t.count; i += BIN_THREADS) {
+    const Box6 b = boxes[A[t.begin + i]];
+    double c[3];
+    centroid(b, c);
+    for (int a = 0; a < 3; a++) bin_add<false>(s[a * NB + bin_of(c[a], nd.cmin[a], nd.cmax[a])], b, c);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * NB; i += BIN_THREADS) bin_merge_global(bins[(size_t)t.slot * 3 * NB + i], s[i]);
+}
+
+// Best binned SAH split of a node from its 3 x NB bins (one thread).
+__device__ void choose_split(const Bin* bins, uint32_t count, int& axis, int& split, uint32_t& nleft, Box6& lb,
+                             Box6& rb, double* lcmin, double* lcmax, double* rcmin, double* rcmax) {
+  double best = 1e300;
+  axis = -1;
+  split = -1;
+  for (int a = 0; a < 3; a++) {
+    // suffix areas and counts
+    double rarea[NB];
+    uint32_t rcount[NB];
+    Box6 acc = box_empty();
+    uint32_t n = 0;
+    for (int b = NB - 1; b >= 0; b--) {
+      const Bin& x = bins[a * NB + b];
+      if (x.n) {
+        for (int k = 0; k < 3; k++) { acc.mn[k] = fmin(acc.mn[k], dval(x.bmin[k])); acc.mx[k] = fmax(acc.mx[k], dval(x.bmax[k])); }
+        n += x.n;
+      }
+      rarea[b] = n ? box_sa(acc) : 0.0;
+      rcount[b] = n;
+    }
+    acc = box_empty();
+    n = 0;
+    for (int b = 0; b < NB - 1; b++) {
+      const Bin& x = bins[a * NB + b];
+      if (x.n) {
+        for (int k = 0; k < 3; k++) { acc.mn[k] = fmin(acc.mn[k], dval(x.bmin[k])); acc.mx[k] = fmax(acc.mx[k], dval(x.bmax[k])); }
+        n += x.n;
+      }
+      if (n == 0 || rcount[b + 1] == 0) continue;
+      const double cost = box_sa(acc) * n + rarea[b + 1] * rcount[b + 1];
+      if (cost < best) { best = cost; axis = a; split = b; nleft = n; }
+    }
+  }
+  if (axis < 0) {  // every centroid in one bin on every axis: split the range in the middle
+    nleft = count / 2;
+    return;
+  }
+  lb = box_empty();
+  rb = box_empty();
+  for (int k = 0; k < 3; k++) { lcmin[k] = rcmin[k] = 1e300; lcmax[k] = rcmax[k] = -1e300; }
+  for (int b = 0; b < NB; b++) {
+    const Bin& x = bins[axis * NB + b];
+    if (!x.n) continue;
+    Box6& d = b <= split ? lb : rb;
+    double* cmn = b <= split ? lcmin : rcmin;
+    double* cmx = b <= split ? lcmax : rcmax;
+    for (int k = 0; k < 3; k++) {
+      d.mn[k] = fmin(d.mn[k], dval(x.bmin[k]));
+      d.mx[k] = fmax(d.mx[k], dval(x.bmax[k]));
+      cmn[k] = fmin(cmn[k], dval(x.cmin[k]));
+      cmx[k] = fmax(cmx[k], dval(x.cmax[k]));
+    }
+  }
+  (void)best;
+}
+
+__global__ void k_choose_large(NodeInfo* __restrict__ nodes, uint32_t m, const Bin* __restrict__ bins,
+                               uint32_t child_base, int32_t* __restrict__ nodes5, Box6* __restrict__ node_box) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  NodeInfo& nd = nodes[k];
+  Box6 lb, rb;
+  choose_split(bins + (size_t)k * 3 * NB, nd.count, nd.axis, nd.split, nd.nleft, lb, rb, nd.lcmin, nd.lcmax,
+               nd.rcmin, nd.rcmax);
+  const uint32_t c = child_base + 2 * k;
+  int32_t* p = nodes5 + 5 * (size_t)nd.node;
+  p[0] = (int32_t)c;
+  p[1] = -1;
+  if (nd.axis >= 0) {
+    node_box[c] = lb;
+    node_box[c + 1] = rb;
+  } else {  // middle split: both halves keep the node's bounds
+    node_box[c] = node_box[nd.node];
+    node_box[c + 1] = node_box[nd.node];
+    for (int a = 0; a < 3; a++) {
+      nd.lcmin[a] = nd.rcmin[a] = nd.cmin[a];
+      nd.lcmax[a] = nd.rcmax[a] = nd.cmax[a];
+    }
+  }
+}
+
+__global__ void k_left_flags_binned(const Tile* __restrict__ tiles, const NodeInfo* __restrict__ nodes,
+                                    const uint32_t* __restrict__ A, const Box6* __restrict__ boxes,
+                                    uint32_t* __restrict__ flags) {
+  const Tile t = tiles[blockIdx.x];
+  const NodeInfo& nd = nodes[t.slot];
+  for (uint32_t i = threadIdx.x; i < t.count; i += blockDim.x) {
+    const uint32_t pos = t.begin + i;
+    bool left;
+    if (nd.axis < 0) {
+      left = pos - nd.start < nd.nleft;
+    } else {
+      double c[3];
+      centroid(boxes[A[pos]], c);
+      left = bin_of(c[nd.axis], nd.cmin[nd.axis], nd.cmax[nd.axis]) <= nd.split;
+    }
+    flags[pos] = left ? 1u : 0u;
+  }
+}
+
+// Stable partition of each large node's range; X = exclusive scan of flags over all T.
+__global__ void k_partition_binned(const Tile* __restrict__ tiles, const NodeInfo* __restrict__ nodes,
+                                   const uint32_t* __restrict__ A, const uint32_t* __restrict__ flags,
+                                   const uint32_t* __restrict__ X, uint32_t* __restrict__ A2,
+                                   uint32_t* __restrict__ err) {
+  const Tile t = tiles[blockIdx.x];
+  const NodeInfo& nd = nodes[t.slot];
+  const uint32_t x0 = X[nd.start];
+  for (uint32_t i = threadIdx.x; i < t.count; i += blockDim.x) {
+    const uint32_t pos = t.begin + i;
+    const uint32_t before_left = X[pos] - x0;
+    const uint32_t np = flags[pos] ? nd.start + before_left : nd.start + nd.nleft + (pos - nd.start - before_left);
+    if (np < nd.start + nd.count) A2[np] = A[pos];
+    else atomicOr(err, ERR_BVH);
+  }
+}
+
+// Phase 2: one block builds the subtree of one node of at most BIN_SMALL triangles.
+struct SmallTask {
+  uint32_t start, count, node;
+};
+__global__ void __launch_bounds__(BIN_THREADS) k_build_small(const SmallTask* __restrict__ tasks,
+                                                             uint32_t* __restrict__ A, const Box6* __restrict__ boxes,
+                                                             int32_t* __restrict__ nodes5,
+                                                             Box6* __restrict__ node_box,
+                                                             uint32_t* __restrict__ node_counter,
+                                                             uint32_t max_nodes, uint32_t* __restrict__ err) {
+  __shared__ Bin s[3 * NB];
+  __shared__ SmallTask stack[256];
+  __shared__ int sp;
+  __shared__ uint32_t tmp[BIN_SMALL];
+  __shared__ uint32_t warp_sums[BIN_THREADS / 32];
+  __shared__ int s_axis, s_split;
+  __shared__ uint32_t s_nleft, s_child;
+  __shared__ double s_cmin[3], s_cmax[3];
+  if (threadIdx.x == 0) { stack[0] = tasks[blockIdx.x]; sp = 1; }
+  __syncthreads();
+  while (true) {
+    __syncthreads();
+    if (sp == 0) break;
+    const SmallTask task = stack[sp - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) sp--;
+    if (task.count <= 2) {
+      if (threadIdx.x == 0) {
+        int32_t* p = nodes5 + 5 * (size_t)task.node;
+        p[0] = -1;
+        p[1] = (int32_t)((task.count << 24) | task.start);
+      }
+      continue;
+    }
+    // centroid bounds
+    if (threadIdx.x < 3) { s_cmin[threadIdx.x] = 1e300; s_cmax[threadIdx.x] = -1e300; }
+    for (int i = threadIdx.x; i < 3 * NB; i += BIN_THREADS) bin_clear(s[i]);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < task.count; i += BIN_THREADS) {
+      double c[3];
+      centroid(boxes[A[task.start + i]], c);
+      bin_add<false>(s[0], boxes[A[task.start + i]], c);  // bin 0 of axis 0 collects the node's bounds first
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) { s_cmin[threadIdx.x] = dval(s[0].cmin[threadIdx.x]); s_cmax[threadIdx.x] = dval(s[0].cmax[threadIdx.x]); }
+    __syncthreads();
+    if (threadIdx.x == 0) bin_clear(s[0]);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < task.count; i += BIN_THREADS) {
+      const Box6 b = boxes[A[task.start + i]];
+      double c[3];
+      centroid(b, c);
+      for (int a = 0; a < 3; a++) bin_add<false>(s[a * NB + bin_of(c[a], s_cmin[a], s_cmax[a])], b, c);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int axis, split;
+      uint32_t nleft;
+      Box6 lb, rb;
+      double lcmin[3], lcmax[3], rcmin[3], rcmax[3];
+      choose_split(s, task.count, axis, split, nleft, lb, rb, lcmin, lcmax, rcmin, rcmax);
+      // leaf if small enough and the split is not cheaper than testing every triangle
+      const Box6 nb = node_box[task.node];
+      const double area = box_sa(nb);
+      bool leaf = false;
+      if (task.count <= BIN_MAX_LEAF) {
+        const double split_cost = axis >= 0 && area > 0.0 ? C_TRAV + (box_sa(lb) * nleft + box_sa(rb) * (task.count - nleft)) / area : 1e300;
+        leaf = !(split_cost < (double)task.count);
+      }
+      if (leaf) {
+        int32_t* p = nodes5 + 5 * (size_t)task.node;
+        p[0] = -1;
+        p[1] = (int32_t)((task.count << 24) | task.start);
+        s_child = ~0u;
+      } else {
+        const uint32_t c = atomicAdd(node_counter, 2u);
+        if (c + 1 >= max_nodes) {
+          atomicOr(err, ERR_BVH);
+          s_child = ~0u;
+          int32_t* p = nodes5 + 5 * (size_t)task.node;
+          p[0] = -1;
+          p[1] = (int32_t)((min(task.count, 127u) << 24) | task.start);
+        } else {
+          s_child = c;
+          int32_t* p = nodes5 + 5 * (size_t)task.node;
+          p[0] = (int32_t)c;
+          p[1] = -1;
+          node_box[c] = axis >= 0 ? lb : nb;
+          node_box[c + 1] = axis >= 0 ? rb : nb;
+        }
+      }
+      s_axis = axis;
+      s_split = split;
+      s_nleft = nleft;
+    }
+    __syncthreads();
+    if (s_child == ~0u) continue;
+    // stable partition through shared memory: left flags, block scan, scatter
+    const uint32_t n = task.count;
+    const uint32_t per = (n + BIN_THREADS - 1) / BIN_THREADS;
+    const uint32_t b0 = threadIdx.x * per, b1 = min(n, b0 + per);
+    uint32_t mine = 0;
+    for (uint32_t i = b0; i < b1; i++) {
+      bool left;
+      if (s_axis < 0) left = i < s_nleft;
+      else {
+        double c[3];
+        centroid(boxes[A[task.start + i]], c);
+        left = bin_of(c[s_axis], s_cmin[s_axis], s_cmax[s_axis]) <= s_split;
+      }
+      mine += left ? 1u : 0u;
+    }
+    // exclusive scan of `mine` across the block
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0;
+    for (int k = 0; k < w; k++) wbase += warp_sums[k];
+    uint32_t lpos = wbase + incl - mine;
+    uint32_t rpos = s_nleft + (b0 - lpos);
+    for (uint32_t i = b0; i < b1; i++) {
+      bool left;
+      if (s_axis < 0) left = i < s_nleft;
+      else {
+        double c[3];
+        centroid(boxes[A[task.start + i]], c);
+        left = bin_of(c[s_axis], s_cmin[s_axis], s_cmax[s_axis]) <= s_split;
+      }
+      const uint32_t id = A[task.start + i];
+      const uint32_t q = left ? lpos++ : rpos++;
+      if (q < n) tmp[q] = id;
+      else atomicOr(err, ERR_BVH);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += BIN_THREADS) A[task.start + i] = tmp[i];
+    if (threadIdx.x == 0) {
+      if (sp + 2 <= 256) {
+        stack[sp++] = SmallTask{task.start + s_nleft, n - s_nleft, s_child + 1};
+        stack[sp++] = SmallTask{task.start, s_nleft, s_child};
+      } else {
+        atomicOr(err, ERR_BVH);
+      }
+    }
+  }
+}
+
+__global__ void k_init_bins(Bin* bins, size_t n) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) bin_clear(bins[i]);
+}
+
+}  // namespace
+
+int build_bvh_binned(cudaStream_t s, const double* pos3, uint32_t n_verts, const int4* tri4, uint32_t T,
+                     BvhOut& out, std::string& why) {
+  if (T == 0) { why = "no triangles"; return 1; }
+  if (T >= (1u << 24)) { why = "too many triangles for the 24-bit leaf base"; return 1; }
+  const uint32_t max_nodes = 2 * T;
+  DevBuf<Box6> tri_box(T), node_box(max_nodes);
+  DevBuf<uint32_t> A(T), A2(T), flags(T), X(T), counter(1), derr(1);
+  DevBuf<int32_t> nodes5(5 * (size_t)max_nodes);
+  DevBuf<Bin> root_bin(1);
+  check(cudaMemsetAsync(derr.p, 0, 4, s), "memset");
+  k_tri_boxes_plain<<<blocks(T), 256, 0, s>>>(pos3, tri4, T, tri_box.p, A.p);
+  k_init_bins<<<1, 32, 0, s>>>(root_bin.p, 1);
+  k_root_bounds<<<std::min<unsigned>(blocks(T), 1024u), 256, 0, s>>>(tri_box.p, T, root_bin.p);
+  check(cudaGetLastError(), "binned roots");
+  Bin rb;
+  check(cudaMemcpyAsync(&rb, root_bin.p, sizeof(Bin), cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaStreamSynchronize(s), "sync");
+  auto hval = [](unsigned long long k) {
+    const unsigned long long u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+    double d;
+    std::memcpy(&d, &u, 8);
+    return d;
+  };
+  Box6 root;
+  for (int a = 0; a < 3; a++) { root.mn[a] = hval(rb.bmin[a]); root.mx[a] = hval(rb.bmax[a]); }
+  check(cudaMemcpyAsync(node_box.p, &root, sizeof(Box6), cudaMemcpyHostToDevice, s), "H2D");
+
+  std::vector<NodeInfo> large;
+  std::vector<SmallTask> small;
+  uint32_t next = 1;
+  {
+    NodeInfo r{};
+    r.start = 0; r.count = T; r.node = 0;
+    for (int a = 0; a < 3; a++) { r.cmin[a] = hval(rb.cmin[a]); r.cmax[a] = hval(rb.cmax[a]); }
+    if (T > BIN_SMALL) large.push_back(r);
+    else small.push_back(SmallTask{0, T, 0});
+  }
+  DevBuf<NodeInfo> d_nodes;
+  DevBuf<Tile> d_tiles;
+  DevBuf<Bin> bins;
+  uint32_t depth = 1;
+  while (!large.empty()) {
+    depth++;
+    const uint32_t m = (uint32_t)large.size();
+    std::vector<Tile> tiles;
+    for (uint32_t k = 0; k < m; k++)
+      for (uint32_t b = 0; b < large[k].count; b += BIN_TILE)
+        tiles.push_back(Tile{k, large[k].start + b, std::min<uint32_t>(BIN_TILE, large[k].count - b)});
+    d_nodes.alloc(m);
+    d_tiles.alloc(tiles.size());
+    bins.alloc((size_t)m * 3 * NB);
+    check(cudaMemcpyAsync(d_nodes.p, large.data(), m * sizeof(NodeInfo), cudaMemcpyHostToDevice, s), "H2D");
+    check(cudaMemcpyAsync(d_tiles.p, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, s), "H2D");
+    k_init_bins<<<(unsigned)(((size_t)m * 3 * NB + 255) / 256), 256, 0, s>>>(bins.p, (size_t)m * 3 * NB);
+    k_bin_tiles<<<(unsigned)tiles.size(), BIN_THREADS, 0, s>>>(d_tiles.p, d_nodes.p, A.p, tri_box.p, bins.p);
+    if (next + 2 * m > max_nodes) { why = "node budget exceeded"; return 1; }
+    k_choose_large<<<blocks(m, 64), 64, 0, s>>>(d_nodes.p, m, bins.p, next, nodes5.p, node_box.p);
+    check(cudaMemsetAsync(flags.p, 0, (size_t)T * 4, s), "memset");
+    k_left_flags_binned<<<(unsigned)tiles.size(), BIN_THREADS, 0, s>>>(d_tiles.p, d_nodes.p, A.p, tri_box.p, flags.p);
+    scan_exclusive_u32(s, flags.p, X.p, T, nullptr);
+    check(cudaMemcpyAsync(A2.p, A.p, (size_t)T * 4, cudaMemcpyDeviceToDevice, s), "memcpy");
+    k_partition_binned<<<(unsigned)tiles.size(), BIN_THREADS, 0, s>>>(d_tiles.p, d_nodes.p, A.p, flags.p, X.p, A2.p,
+                                                                      derr.p);
+    check(cudaGetLastError(), "binned level");
+    std::swap(A.p, A2.p);
+    check(cudaMemcpyAsync(large.data(), d_nodes.p, m * sizeof(NodeInfo), cudaMemcpyDeviceToHost, s), "D2H");
+    uint32_t lerr = 0;
+    check(cudaMemcpyAsync(&lerr, derr.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "sync");
+    if (lerr) { why = "binned partition out of range"; return 1; }
+    std::vector<NodeInfo> nl;
+    for (uint32_t k = 0; k < m; k++) {
+      const NodeInfo& p = large[k];
+      const uint32_t c = next + 2 * k;
+      NodeInfo L{}, R{};
+      L.start = p.start; L.count = p.nleft; L.node = c;
+      R.start = p.start + p.nleft; R.count = p.count - p.nleft; R.node = c + 1;
+      for (int a = 0; a < 3; a++) {
+        L.cmin[a] = p.lcmin[a]; L.cmax[a] = p.lcmax[a];
+        R.cmin[a] = p.rcmin[a]; R.cmax[a] = p.rcmax[a];
+      }
+      for (const NodeInfo& q : {L, R}) {
+        if (q.count == 0) { why = "empty child"; return 1; }
+        if (q.count > BIN_SMALL) nl.push_back(q);
+        else small.push_back(SmallTask{q.start, q.count, q.node});
+      }
+    }
+    next += 2 * m;
+    large.swap(nl);
+  }
+  check(cudaMemcpyAsync(counter.p, &next, 4, cudaMemcpyHostToDevice, s), "H2D");
+  if (!small.empty()) {
+    DevBuf<SmallTask> d_small(small.size());
+    check(cudaMemcpyAsync(d_small.p, small.data(), small.size() * sizeof(SmallTask), cudaMemcpyHostToDevice, s), "H2D");
+    k_build_small<<<(unsigned)small.size(), BIN_THREADS, 0, s>>>(d_small.p, A.p, tri_box.p, nodes5.p, node_box.p,
+                                                                counter.p, max_nodes, derr.p);
+    check(cudaGetLastError(), "k_build_small");
+  }
+  uint32_t n_nodes = 0, herr = 0;
+  check(cudaMemcpyAsync(&n_nodes, counter.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaStreamSynchronize(s), "sync");
+  if (herr) { why = "binned build ran out of node or stack budget"; return 1; }
+
+  double span[3], center[3];
+  for (int i = 0; i < 3; i++) span[i] = root.mx[i] - root.mn[i];
+  const double longest = js_max(js_max(span[0], span[1]), span[2]);
+  for (int i = 0; i < 3; i++) center[i] = root.mn[i] + span[i] * 0.5;
+  out.nodes5.alloc(5 * (size_t)n_nodes);
+  check(cudaMemcpyAsync(out.nodes5.p, nodes5.p, 5 * (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, s), "memcpy");
+  k_quantize_nodes<<<blocks(n_nodes), 256, 0, s>>>(n_nodes, node_box.p, center[0], center[1], center[2], longest,
+                                                    out.nodes5.p);
+  out.verts4.alloc(n_verts);
+  k_norm_verts<<<blocks(n_verts), 256, 0, s>>>(pos3, n_verts, center[0], center[1], center[2], longest, out.verts4.p);
+  out.tri4_leaf.alloc(T);
+  k_gather_tris<<<blocks(T), 256, 0, s>>>(tri4, reinterpret_cast<const int32_t*>(A.p), T, out.tri4_leaf.p);
+  out.node_box.alloc(6 * (size_t)n_nodes);
+  check(cudaMemcpyAsync(out.node_box.p, node_box.p, (size_t)n_nodes * sizeof(Box6), cudaMemcpyDeviceToDevice, s),
+        "memcpy");
+  check(cudaGetLastError(), "binned pack");
   check(cudaStreamSynchronize(s), "sync");
   out.n_nodes = n_nodes;
   out.n_leaf_tris = T;

@@ -26,4 +26,9 @@ struct BvhOut {
 int build_bvh_sweep(cudaStream_t s, const double* pos3, uint32_t n_verts, const int4* tri4, uint32_t n_tris,
                     BvhOut& out, std::string& why);
 
+// Binned SAH (16 bins per axis, leaves of at most 8 triangles): a different,
+// faster-to-build topology than bvh.js; same output layout.
+int build_bvh_binned(cudaStream_t s, const double* pos3, uint32_t n_verts, const int4* tri4, uint32_t n_tris,
+                     BvhOut& out, std::string& why);
+
 }  // namespace pk
