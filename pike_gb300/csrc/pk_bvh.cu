@@ -899,154 +899,229 @@ __global__ void k_partition_binned(const Tile* __restrict__ tiles, const NodeInf
   }
 }
 
-// Phase 2: one block builds the subtree of one node of at most BIN_SMALL triangles.
+// Phase 2: one warp builds the subtree of one node of at most BIN_SMALL
+// triangles, depth first, with warp-private bins (no atomics: peers that hit
+// the same bin are combined with __match_any_sync / __reduce_*_sync and their
+// leader updates the bin), a ballot-based stable partition through a
+// warp-private buffer, and exact double node boxes from warp reductions.
 struct SmallTask {
   uint32_t start, count, node;
 };
-__global__ void __launch_bounds__(BIN_THREADS) k_build_small(const SmallTask* __restrict__ tasks,
-                                                             uint32_t* __restrict__ A, const Box6* __restrict__ boxes,
-                                                             int32_t* __restrict__ nodes5,
-                                                             Box6* __restrict__ node_box,
-                                                             uint32_t* __restrict__ node_counter,
-                                                             uint32_t max_nodes, uint32_t* __restrict__ err) {
-  __shared__ Bin s[3 * NB];
-  __shared__ SmallTask stack[256];
-  __shared__ int sp;
-  __shared__ uint32_t tmp[BIN_SMALL];
-  __shared__ uint32_t warp_sums[BIN_THREADS / 32];
-  __shared__ int s_axis, s_split;
-  __shared__ uint32_t s_nleft, s_child;
-  __shared__ double s_cmin[3], s_cmax[3];
-  if (threadIdx.x == 0) { stack[0] = tasks[blockIdx.x]; sp = 1; }
-  __syncthreads();
-  while (true) {
-    __syncthreads();
-    if (sp == 0) break;
+constexpr int SMALL_WARPS = 4;
+constexpr int SMALL_STACK = 128;
+
+__device__ __forceinline__ uint32_t fkey(float x) {
+  const uint32_t u = __float_as_uint(x);
+  return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fval(uint32_t k) {
+  return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
+}
+struct FBin {
+  uint32_t n, mn[3], mx[3];
+};
+
+__device__ __forceinline__ double warp_min_d(double v) {
+  for (int o = 16; o; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+  for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(SMALL_WARPS * 32) k_build_small(const SmallTask* __restrict__ tasks,
+                                                                  uint32_t n_tasks, uint32_t* __restrict__ A,
+                                                                  const Box6* __restrict__ boxes,
+                                                                  int32_t* __restrict__ nodes5,
+                                                                  Box6* __restrict__ node_box,
+                                                                  uint32_t* __restrict__ node_counter,
+                                                                  uint32_t max_nodes, uint32_t* __restrict__ err) {
+  __shared__ FBin sbin[SMALL_WARPS][3 * NB];
+  __shared__ SmallTask sstack[SMALL_WARPS][SMALL_STACK];
+  __shared__ uint32_t stmp[SMALL_WARPS][BIN_SMALL];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ti = blockIdx.x * SMALL_WARPS + w;
+  if (ti >= n_tasks) return;  // whole warps only
+  FBin* bins = sbin[w];
+  SmallTask* stack = sstack[w];
+  uint32_t* tmp = stmp[w];
+  int sp = 1;
+  if (lane == 0) stack[0] = tasks[ti];
+  __syncwarp();
+  while (sp > 0) {
     const SmallTask task = stack[sp - 1];
-    __syncthreads();
-    if (threadIdx.x == 0) sp--;
-    if (task.count <= 2) {
-      if (threadIdx.x == 0) {
+    __syncwarp();
+    sp--;
+    const uint32_t n = task.count;
+    // exact node box (double) and centroid bounds (float)
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    float cmn[3] = {3e38f, 3e38f, 3e38f}, cmx[3] = {-3e38f, -3e38f, -3e38f};
+    for (uint32_t i = lane; i < n; i += 32) {
+      const Box6 b = boxes[A[task.start + i]];
+      for (int a = 0; a < 3; a++) {
+        mn[a] = fmin(mn[a], b.mn[a]);
+        mx[a] = fmax(mx[a], b.mx[a]);
+        const float c = (float)((b.mn[a] + b.mx[a]) * 0.5);
+        cmn[a] = fminf(cmn[a], c);
+        cmx[a] = fmaxf(cmx[a], c);
+      }
+    }
+    Box6 nb;
+    for (int a = 0; a < 3; a++) {
+      nb.mn[a] = warp_min_d(mn[a]);
+      nb.mx[a] = warp_max_d(mx[a]);
+      cmn[a] = fval(__reduce_min_sync(0xffffffffu, fkey(cmn[a])));
+      cmx[a] = fval(__reduce_max_sync(0xffffffffu, fkey(cmx[a])));
+    }
+    if (lane == 0) node_box[task.node] = nb;
+    bool leaf = n <= 3;
+    int axis = -1, split = -1;
+    uint32_t nleft = n / 2;
+    if (!leaf) {
+      for (int i = lane; i < 3 * NB; i += 32) {
+        bins[i].n = 0;
+        for (int a = 0; a < 3; a++) { bins[i].mn[a] = ~0u; bins[i].mx[a] = 0u; }
+      }
+      __syncwarp();
+      for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t i = base + lane;
+        const bool on = i < n;
+        Box6 b = box_empty();
+        if (on) b = boxes[A[task.start + i]];
+        for (int ax = 0; ax < 3; ax++) {
+          float c = 0.0f;
+          int bin = -1;
+          if (on) {
+            c = (float)((b.mn[ax] + b.mx[ax]) * 0.5);
+            const float ext = cmx[ax] - cmn[ax];
+            bin = ext > 0.0f ? min(NB - 1, max(0, (int)((c - cmn[ax]) * ((float)NB / ext)))) : 0;
+          }
+          const unsigned peers = __match_any_sync(0xffffffffu, bin);
+          const uint32_t cnt = __popc(peers);
+          uint32_t kmn[3], kmx[3];
+          for (int a = 0; a < 3; a++) {
+            kmn[a] = __reduce_min_sync(peers, on ? fkey((float)b.mn[a]) : ~0u);
+            kmx[a] = __reduce_max_sync(peers, on ? fkey((float)b.mx[a]) : 0u);
+          }
+          if (on && lane == __ffs(peers) - 1) {
+            FBin& x = bins[ax * NB + bin];
+            x.n += cnt;
+            for (int a = 0; a < 3; a++) { x.mn[a] = min(x.mn[a], kmn[a]); x.mx[a] = max(x.mx[a], kmx[a]); }
+          }
+          __syncwarp();
+        }
+      }
+      // every lane evaluates candidate planes (axis, bin) = divmod(l, NB - 1) for
+      // l = lane and lane + 32; the warp keeps the cheapest (lowest index on ties)
+      double best = 1e300;
+      int bl = 1 << 30;
+      for (int l = lane; l < 3 * (NB - 1); l += 32) {
+        const int ax = l / (NB - 1), sb = l % (NB - 1);
+        float lmn[3] = {3e38f, 3e38f, 3e38f}, lmx[3] = {-3e38f, -3e38f, -3e38f};
+        float rmn[3] = {3e38f, 3e38f, 3e38f}, rmx[3] = {-3e38f, -3e38f, -3e38f};
+        uint32_t lc = 0, rc = 0;
+        for (int bi = 0; bi < NB; bi++) {
+          const FBin& x = bins[ax * NB + bi];
+          if (!x.n) continue;
+          float* mnp = bi <= sb ? lmn : rmn;
+          float* mxp = bi <= sb ? lmx : rmx;
+          for (int a2 = 0; a2 < 3; a2++) { mnp[a2] = fminf(mnp[a2], fval(x.mn[a2])); mxp[a2] = fmaxf(mxp[a2], fval(x.mx[a2])); }
+          if (bi <= sb) lc += x.n; else rc += x.n;
+        }
+        if (!lc || !rc) continue;
+        const float lx = lmx[0] - lmn[0], ly = lmx[1] - lmn[1], lz = lmx[2] - lmn[2];
+        const float rx = rmx[0] - rmn[0], ry = rmx[1] - rmn[1], rz = rmx[2] - rmn[2];
+        const double cost = (double)(lx * ly + ly * lz + lz * lx) * lc + (double)(rx * ry + ry * rz + rz * rx) * rc;
+        if (cost < best) { best = cost; bl = l; }
+      }
+      for (int o = 16; o; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
+        if (ob < best || (ob == best && ol < bl)) { best = ob; bl = ol; }
+      }
+      if (bl < (1 << 30)) {
+        axis = bl / (NB - 1);
+        split = bl % (NB - 1);
+        uint32_t lc = 0;
+        for (int bi = 0; bi <= split; bi++) lc += bins[axis * NB + bi].n;
+        nleft = lc;
+      } else {
+        axis = -1;
+        nleft = n / 2;
+      }
+      if (lane == 0 && n <= BIN_MAX_LEAF) {
+        const double ex = nb.mx[0] - nb.mn[0], ey = nb.mx[1] - nb.mn[1], ez = nb.mx[2] - nb.mn[2];
+        const double area = ex * ey + ey * ez + ez * ex;
+        const double split_cost = axis >= 0 && area > 0.0 ? C_TRAV + best / area : 1e300;
+        leaf = !(split_cost < (double)n);
+      }
+      leaf = __shfl_sync(0xffffffffu, leaf, 0);
+      axis = __shfl_sync(0xffffffffu, axis, 0);
+      split = __shfl_sync(0xffffffffu, split, 0);
+      nleft = __shfl_sync(0xffffffffu, nleft, 0);
+    }
+    if (leaf) {
+      if (lane == 0) {
         int32_t* p = nodes5 + 5 * (size_t)task.node;
         p[0] = -1;
-        p[1] = (int32_t)((task.count << 24) | task.start);
+        p[1] = (int32_t)((n << 24) | task.start);
       }
       continue;
     }
-    // centroid bounds
-    if (threadIdx.x < 3) { s_cmin[threadIdx.x] = 1e300; s_cmax[threadIdx.x] = -1e300; }
-    for (int i = threadIdx.x; i < 3 * NB; i += BIN_THREADS) bin_clear(s[i]);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < task.count; i += BIN_THREADS) {
-      double c[3];
-      centroid(boxes[A[task.start + i]], c);
-      bin_add<false>(s[0], boxes[A[task.start + i]], c);  // bin 0 of axis 0 collects the node's bounds first
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) { s_cmin[threadIdx.x] = dval(s[0].cmin[threadIdx.x]); s_cmax[threadIdx.x] = dval(s[0].cmax[threadIdx.x]); }
-    __syncthreads();
-    if (threadIdx.x == 0) bin_clear(s[0]);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < task.count; i += BIN_THREADS) {
-      const Box6 b = boxes[A[task.start + i]];
-      double c[3];
-      centroid(b, c);
-      for (int a = 0; a < 3; a++) bin_add<false>(s[a * NB + bin_of(c[a], s_cmin[a], s_cmax[a])], b, c);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int axis, split;
-      uint32_t nleft;
-      Box6 lb, rb;
-      double lcmin[3], lcmax[3], rcmin[3], rcmax[3];
-      choose_split(s, task.count, axis, split, nleft, lb, rb, lcmin, lcmax, rcmin, rcmax);
-      // leaf if small enough and the split is not cheaper than testing every triangle
-      const Box6 nb = node_box[task.node];
-      const double area = box_sa(nb);
-      bool leaf = false;
-      if (task.count <= BIN_MAX_LEAF) {
-        const double split_cost = axis >= 0 && area > 0.0 ? C_TRAV + (box_sa(lb) * nleft + box_sa(rb) * (task.count - nleft)) / area : 1e300;
-        leaf = !(split_cost < (double)task.count);
-      }
-      if (leaf) {
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(node_counter, 2u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c + 1 >= max_nodes || sp + 2 > SMALL_STACK) {
+      if (lane == 0) {
+        atomicOr(err, ERR_BVH);
         int32_t* p = nodes5 + 5 * (size_t)task.node;
         p[0] = -1;
-        p[1] = (int32_t)((task.count << 24) | task.start);
-        s_child = ~0u;
-      } else {
-        const uint32_t c = atomicAdd(node_counter, 2u);
-        if (c + 1 >= max_nodes) {
-          atomicOr(err, ERR_BVH);
-          s_child = ~0u;
-          int32_t* p = nodes5 + 5 * (size_t)task.node;
-          p[0] = -1;
-          p[1] = (int32_t)((min(task.count, 127u) << 24) | task.start);
+        p[1] = (int32_t)((min(n, 127u) << 24) | task.start);
+      }
+      continue;
+    }
+    // stable partition: left elements in order, then right elements in order
+    uint32_t lbase = 0, rbase = nleft;
+    for (uint32_t base = 0; base < n; base += 32) {
+      const uint32_t i = base + lane;
+      const bool on = i < n;
+      bool left = false;
+      uint32_t id = 0;
+      if (on) {
+        id = A[task.start + i];
+        if (axis < 0) {
+          left = i < nleft;
         } else {
-          s_child = c;
-          int32_t* p = nodes5 + 5 * (size_t)task.node;
-          p[0] = (int32_t)c;
-          p[1] = -1;
-          node_box[c] = axis >= 0 ? lb : nb;
-          node_box[c + 1] = axis >= 0 ? rb : nb;
+          const Box6 b = boxes[id];
+          const float cc = (float)((b.mn[axis] + b.mx[axis]) * 0.5);
+          const float ext = cmx[axis] - cmn[axis];
+          const int bin = ext > 0.0f ? min(NB - 1, max(0, (int)((cc - cmn[axis]) * ((float)NB / ext)))) : 0;
+          left = bin <= split;
         }
       }
-      s_axis = axis;
-      s_split = split;
-      s_nleft = nleft;
-    }
-    __syncthreads();
-    if (s_child == ~0u) continue;
-    // stable partition through shared memory: left flags, block scan, scatter
-    const uint32_t n = task.count;
-    const uint32_t per = (n + BIN_THREADS - 1) / BIN_THREADS;
-    const uint32_t b0 = threadIdx.x * per, b1 = min(n, b0 + per);
-    uint32_t mine = 0;
-    for (uint32_t i = b0; i < b1; i++) {
-      bool left;
-      if (s_axis < 0) left = i < s_nleft;
-      else {
-        double c[3];
-        centroid(boxes[A[task.start + i]], c);
-        left = bin_of(c[s_axis], s_cmin[s_axis], s_cmax[s_axis]) <= s_split;
+      const unsigned lm = __ballot_sync(0xffffffffu, on && left), rm = __ballot_sync(0xffffffffu, on && !left);
+      const uint32_t below = (1u << lane) - 1u;
+      if (on) {
+        const uint32_t q = left ? lbase + __popc(lm & below) : rbase + __popc(rm & below);
+        if (q < n) tmp[q] = id;
+        else atomicOr(err, ERR_BVH);
       }
-      mine += left ? 1u : 0u;
+      lbase += __popc(lm);
+      rbase += __popc(rm);
     }
-    // exclusive scan of `mine` across the block
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t incl = mine;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+    __syncwarp();
+    if (lbase != nleft && lane == 0) atomicOr(err, ERR_BVH);
+    for (uint32_t i = lane; i < n; i += 32) A[task.start + i] = tmp[i];
+    if (lane == 0) {
+      int32_t* p = nodes5 + 5 * (size_t)task.node;
+      p[0] = (int32_t)c;
+      p[1] = -1;
+      stack[sp] = SmallTask{task.start + nleft, n - nleft, c + 1};
+      stack[sp + 1] = SmallTask{task.start, nleft, c};
     }
-    if (lane == 31) warp_sums[w] = incl;
-    __syncthreads();
-    uint32_t wbase = 0;
-    for (int k = 0; k < w; k++) wbase += warp_sums[k];
-    uint32_t lpos = wbase + incl - mine;
-    uint32_t rpos = s_nleft + (b0 - lpos);
-    for (uint32_t i = b0; i < b1; i++) {
-      bool left;
-      if (s_axis < 0) left = i < s_nleft;
-      else {
-        double c[3];
-        centroid(boxes[A[task.start + i]], c);
-        left = bin_of(c[s_axis], s_cmin[s_axis], s_cmax[s_axis]) <= s_split;
-      }
-      const uint32_t id = A[task.start + i];
-      const uint32_t q = left ? lpos++ : rpos++;
-      if (q < n) tmp[q] = id;
-      else atomicOr(err, ERR_BVH);
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += BIN_THREADS) A[task.start + i] = tmp[i];
-    if (threadIdx.x == 0) {
-      if (sp + 2 <= 256) {
-        stack[sp++] = SmallTask{task.start + s_nleft, n - s_nleft, s_child + 1};
-        stack[sp++] = SmallTask{task.start, s_nleft, s_child};
-      } else {
-        atomicOr(err, ERR_BVH);
-      }
-    }
+    sp += 2;
+    __syncwarp();
   }
 }
 
@@ -1094,9 +1169,11 @@ int build_bvh_binned(cudaStream_t s, const double* pos3, uint32_t n_verts, const
     if (T > BIN_SMALL) large.push_back(r);
     else small.push_back(SmallTask{0, T, 0});
   }
-  DevBuf<NodeInfo> d_nodes;
-  DevBuf<Tile> d_tiles;
-  DevBuf<Bin> bins;
+  // per-level buffers at their largest: every large node holds more than BIN_SMALL triangles
+  const uint32_t m_max = T / BIN_SMALL + 2;
+  DevBuf<NodeInfo> d_nodes(m_max);
+  DevBuf<Tile> d_tiles(T / BIN_TILE + m_max + 1);
+  DevBuf<Bin> bins((size_t)m_max * 3 * NB);
   uint32_t depth = 1;
   while (!large.empty()) {
     depth++;
@@ -1105,9 +1182,7 @@ int build_bvh_binned(cudaStream_t s, const double* pos3, uint32_t n_verts, const
     for (uint32_t k = 0; k < m; k++)
       for (uint32_t b = 0; b < large[k].count; b += BIN_TILE)
         tiles.push_back(Tile{k, large[k].start + b, std::min<uint32_t>(BIN_TILE, large[k].count - b)});
-    d_nodes.alloc(m);
-    d_tiles.alloc(tiles.size());
-    bins.alloc((size_t)m * 3 * NB);
+    if (m > m_max || tiles.size() > d_tiles.n) { why = "internal: level buffers too small"; return 1; }
     check(cudaMemcpyAsync(d_nodes.p, large.data(), m * sizeof(NodeInfo), cudaMemcpyHostToDevice, s), "H2D");
     check(cudaMemcpyAsync(d_tiles.p, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, s), "H2D");
     k_init_bins<<<(unsigned)(((size_t)m * 3 * NB + 255) / 256), 256, 0, s>>>(bins.p, (size_t)m * 3 * NB);
@@ -1151,8 +1226,9 @@ int build_bvh_binned(cudaStream_t s, const double* pos3, uint32_t n_verts, const
   if (!small.empty()) {
     DevBuf<SmallTask> d_small(small.size());
     check(cudaMemcpyAsync(d_small.p, small.data(), small.size() * sizeof(SmallTask), cudaMemcpyHostToDevice, s), "H2D");
-    k_build_small<<<(unsigned)small.size(), BIN_THREADS, 0, s>>>(d_small.p, A.p, tri_box.p, nodes5.p, node_box.p,
-                                                                counter.p, max_nodes, derr.p);
+    const unsigned nb = (unsigned)((small.size() + SMALL_WARPS - 1) / SMALL_WARPS);
+    k_build_small<<<nb, SMALL_WARPS * 32, 0, s>>>(d_small.p, (uint32_t)small.size(), A.p, tri_box.p, nodes5.p,
+                                                 node_box.p, counter.p, max_nodes, derr.p);
     check(cudaGetLastError(), "k_build_small");
   }
   uint32_t n_nodes = 0, herr = 0;
