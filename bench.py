@@ -366,6 +366,24 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
     ms = ctx.timer_stop()
     rays = read_stats(ctx)["rays_traced"]
     total, differ = hit_agreement(ctx, plain_mode, wide_mode)
+    # the FP32 binary reference of form (1): same tree, outward-rounded FP32 boxes, (t, slot) ties
+    exact_mode = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_EXACT
+    etotal, ediffer = hit_agreement(ctx, exact_mode, wide_mode)
+    ctx.call("pk_set_trace_mode", exact_mode)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_counting", 1)
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_render_frames", 1, B)
+    ctx.call("pk_sync")
+    ecounts = read_stats(ctx)
+    ctx.call("pk_set_counting", 0)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    ctx.call("pk_render_frames", steps, B)
+    ems = ctx.timer_stop()
+    erays = read_stats(ctx)["rays_traced"]
     ctx.call("pk_set_trace_mode", plain_mode)
     tr = kt["trace"]
     R = max(counts["closest_rays"], 1)
@@ -377,7 +395,12 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
             "closest_hit_agreement": {"rays": total, "differ": differ, "fraction_equal": 1.0 - differ / max(total, 1),
                                       "note": "camera + first bounce rays, pass path; differing rays are the "
                                               "drop-in's truncated-box misses and t ties (the wide result "
-                                              "equals brute force, tests/test_gpu_wide.py)"}}
+                                              "equals brute force, tests/test_gpu_wide.py)"},
+            "fp32_binary": {"value": erays / (ems / 1000.0) / 1e6, "unit": UNIT, "ms_per_step": ems / steps,
+                            "node_bytes": 64,
+                            "fetch_units_per_ray": ecounts["closest_fetch"] / max(ecounts["closest_rays"], 1),
+                            "closest_hit_agreement_with_wide": {"rays": etotal, "differ": ediffer,
+                                                                "fraction_equal": 1.0 - ediffer / max(etotal, 1)}}}
 
 
 def adjoint_form(args, local: int):

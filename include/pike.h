@@ -274,6 +274,11 @@ int pk_read_display_async(pk_ctx* ctx, uint8_t* out8);
  * its inward-truncated snorm16 boxes, so the two differ only on rays where
  * those boxes lose a hit or two triangles tie on t. */
 #define PK_TRACE_WIDE 4
+/* OR PK_TRACE_EXACT (with PK_TRACE_PERSISTENT) to trace the same binary BVH
+ * with FP32 boxes rounded outward from the triangles (plus a margin), slack in
+ * the box tests and (t, slot) ties: the FP32 binary reference of the wide
+ * traversal; both give the brute-force closest hit (no reference counterpart). */
+#define PK_TRACE_EXACT 8
 int pk_set_trace_mode(pk_ctx* ctx, int mode);
 /* Elementwise evaluation of the library's built-in definitions on the GPU
  * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */

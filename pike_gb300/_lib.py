@@ -20,7 +20,7 @@ PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED 
 PK_BVH_SWEEP = 0
 PK_BVH_BINNED = 1
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
-PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE = 0, 1, 2, 4
+PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE, PK_TRACE_EXACT = 0, 1, 2, 4, 8
 
 
 class PikeError(RuntimeError):

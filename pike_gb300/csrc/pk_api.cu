@@ -303,9 +303,32 @@ static int build_wide(pk_ctx* c) {
   return PK_OK;
 }
 
+// Binary records with outward-rounded FP32 boxes for PK_TRACE_EXACT.
+static int build_exact(pk_ctx* c) {
+  std::vector<int32_t> nodes(5 * (size_t)c->n_nodes);
+  std::vector<float> tris(12 * (size_t)c->n_leaf_tris);
+  check(cudaMemcpyAsync(nodes.data(), c->nodes5.p, nodes.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  if (c->n_leaf_tris)
+    check(cudaMemcpyAsync(tris.data(), c->tris.p, tris.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  check(cudaStreamSynchronize(c->stream), "sync");
+  std::vector<float> rec;
+  int32_t root = 0;
+  std::string why;
+  if (build_exact_binary(nodes.data(), c->n_nodes, tris.data(), c->n_leaf_tris, rec, root, why))
+    return fail(c, PK_ERR_ARG, "exact binary records: " + why);
+  upload(c->exact, reinterpret_cast<const float4*>(rec.data()), rec.size() / 4, c->stream);
+  check(cudaStreamSynchronize(c->stream), "sync");
+  c->exact_root = root;
+  c->exact_ready = true;
+  c->invalidate_graph();
+  return PK_OK;
+}
+
 static int finish_bvh(pk_ctx* c) {
   c->wide_ready = false;
   c->wide.release();
+  c->exact_ready = false;
+  c->exact.release();
   c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->inner32.alloc(2 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
@@ -322,6 +345,10 @@ static int finish_bvh(pk_ctx* c) {
   c->bvh_ready = true;
   if (c->trace_mode & TRACE_WIDE) {
     const int rc = build_wide(c);
+    if (rc != PK_OK) return rc;
+  }
+  if (c->trace_mode & TRACE_EXACT) {
+    const int rc = build_exact(c);
     if (rc != PK_OK) return rc;
   }
   c->invalidate_graph();
@@ -863,13 +890,23 @@ int pk_set_trace_mode(pk_ctx* c, int mode) {
   return guarded(c, [&]() {
     c->invalidate_graph();
     const int sched = mode & 1;
-    if (mode & ~(1 | PK_TRACE_COMPACT_RECORDS | PK_TRACE_WIDE)) return fail(c, PK_ERR_ARG, "unknown trace mode");
+    if (mode & ~(1 | PK_TRACE_COMPACT_RECORDS | PK_TRACE_WIDE | PK_TRACE_EXACT))
+      return fail(c, PK_ERR_ARG, "unknown trace mode");
+    if ((mode & PK_TRACE_WIDE) && (mode & PK_TRACE_EXACT))
+      return fail(c, PK_ERR_ARG, "PK_TRACE_WIDE and PK_TRACE_EXACT exclude each other");
+    if ((mode & PK_TRACE_EXACT) && !(mode & PK_TRACE_PERSISTENT))
+      return fail(c, PK_ERR_ARG, "PK_TRACE_EXACT needs PK_TRACE_PERSISTENT");
     if ((mode & PK_TRACE_WIDE) && !c->wide_ready) {
       if (!c->bvh_ready) return fail(c, PK_ERR_STATE, "PK_TRACE_WIDE needs a BVH");
       const int rc = build_wide(c);
       if (rc != PK_OK) return rc;
     }
-    c->trace_mode = sched | (mode & PK_TRACE_WIDE ? TRACE_WIDE : 0);
+    if ((mode & PK_TRACE_EXACT) && !c->exact_ready) {
+      if (!c->bvh_ready) return fail(c, PK_ERR_STATE, "PK_TRACE_EXACT needs a BVH");
+      const int rc = build_exact(c);
+      if (rc != PK_OK) return rc;
+    }
+    c->trace_mode = sched | (mode & PK_TRACE_WIDE ? TRACE_WIDE : 0) | (mode & PK_TRACE_EXACT ? TRACE_EXACT : 0);
     c->compact_nodes = (mode & PK_TRACE_COMPACT_RECORDS) != 0;
     return PK_OK;
   });

@@ -81,6 +81,9 @@ struct pk_ctx {
   DevBuf<double> node_box_d;  // exact double node bounds (pk_bvh_build only)
   bool compact_nodes = false;  // traverse 32-byte records (same boxes as the 64-byte ones)
   DevBuf<float4> wide;         // 8-wide compressed BVH (built on first use of PK_TRACE_WIDE)
+  DevBuf<float4> exact;        // binary records with outward-rounded FP32 boxes (PK_TRACE_EXACT)
+  int exact_root = 0;
+  bool exact_ready = false;
   uint32_t wide_nodes = 0, wide_depth = 0;
   bool wide_ready = false;
   int root = 0;
@@ -115,8 +118,9 @@ struct pk_ctx {
     L.stream = stream;
     L.ctr = ctr.p;
     L.cam = cam.p;
-    L.scene = pk::SceneDev{inner.p, compact_nodes ? inner32.p : nullptr, tris.p, tri4_leaf.p, attrs.p, mat4.p,
-                           layers.p, (int)n_layers, (int)atlas_res, root,
+    const bool ex = (trace_mode & pk::TRACE_EXACT) && exact_ready;
+    L.scene = pk::SceneDev{ex ? exact.p : inner.p, (compact_nodes && !ex) ? inner32.p : nullptr, tris.p, tri4_leaf.p,
+                           attrs.p, mat4.p, layers.p, (int)n_layers, (int)atlas_res, ex ? exact_root : root,
                        n_leaf_tris, n_verts, n_mats, wide_ready ? wide.p : nullptr};
     L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
     L.color = color.p;

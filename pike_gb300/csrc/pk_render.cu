@@ -160,7 +160,31 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
 // Hit bits are set with atomicOr in a flag array zeroed before the launch.
 constexpr int REFILL_MIN = 16;
 
-template <bool ANY, bool FUSED, bool COUNT>
+// Box test of the exact binary records: like box_hit, with the far distance
+// widened by WIDE_SLACK (relative) so that rounding never drops a box.
+__device__ __forceinline__ float box_hit_exact(float xa, float xb, float ya, float yb, float za, float zb, float ox,
+                                               float oy, float oz, float ix, float iy, float iz) {
+  const float t1x = (xa - ox) * ix, t2x = (xb - ox) * ix;
+  const float t1y = (ya - oy) * iy, t2y = (yb - oy) * iy;
+  const float t1z = (za - oz) * iz, t2z = (zb - oz) * iz;
+  const float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
+  const float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
+  const float tmax_s = tmax + fabsf(tmax) * WIDE_SLACK;
+  return (tmax_s >= tmin && tmax_s >= 0.0f) ? tmin : MAX_T;
+}
+__device__ __forceinline__ void inner_children_exact(const SceneDev& sc, int cur, float ox, float oy, float oz,
+                                                     float ix, float iy, float iz, float& lh, float& rh, int& cl,
+                                                     int& cr) {
+  const float4* rec = sc.inner + 4 * (size_t)cur;
+  const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
+  const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
+  lh = box_hit_exact(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
+  rh = box_hit_exact(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+  cl = ch.x;
+  cr = ch.y;
+}
+
+template <bool ANY, bool FUSED, bool COUNT, bool EXACT>
 __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                               const uint32_t* __restrict__ countp, RayQ R,
                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
@@ -200,7 +224,8 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
           const float4 o = R.o[j], d = R.d[j];
           ox = o.x; oy = o.y; oz = o.z;
           dx = d.x; dy = d.y; dz = d.z;
-          ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
+          if (EXACT) { ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz); }
+          else { ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz; }
           best_t = MAX_T; best_i = -1; best_b = 0u;
           sp = 0;
           cur = sc.root;
@@ -218,8 +243,17 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
       if (COUNT) nfetch += 3;
       float lh, rh;
       int cl, cr;
-      inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
-      const bool lok = lh < best_t, rok = rh < best_t;
+      bool lok, rok;
+      if (EXACT) {
+        inner_children_exact(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
+        const float lim = best_t + best_t * WIDE_SLACK;
+        lok = lh < MAX_T && lh <= lim;
+        rok = rh < MAX_T && rh <= lim;
+      } else {
+        inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
+        lok = lh < best_t;
+        rok = rh < best_t;
+      }
       if (lok && rok) {
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
@@ -259,7 +293,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
         if (v < 0.0f || u + v > 1.0f) continue;
         const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
         const float res = dist > eps ? dist : MAX_T;
-        if (res < best_t) {
+        if (res < best_t || (EXACT && res == best_t && base + i < best_i)) {
           best_t = res;
           best_i = base + i;
           best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
@@ -1138,7 +1172,7 @@ void launch_batch_next_frame(cudaStream_t s, uint32_t* frame) { k_batch_next_fra
 void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade,
                   unsigned* trace_wide) {
   int t = 0, c = 0, s = 0, w = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false>, TRACE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w, k_trace_wide<false, true, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_shade, SHADE_THREADS, 0);
@@ -1174,11 +1208,18 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
 #undef PK_TRACEW
     return;
   }
-  if (L.trace_mode == TRACE_PERSISTENT) {
+  if (L.trace_mode & TRACE_PERSISTENT) {
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
-#define PK_TRACED(A, F, C) \
-  k_trace_dyn<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
+#define PK_TRACED(A, F, C)                                                                                         \
+  do {                                                                                                             \
+    if (L.trace_mode & TRACE_EXACT)                                                                                \
+      k_trace_dyn<A, F, C, true><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags,       \
+                                                               L.color, L.npix, ticket);                           \
+    else                                                                                                           \
+      k_trace_dyn<A, F, C, false><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags,      \
+                                                                L.color, L.npix, ticket);                          \
+  } while (0)
     if (!any_hit) {
       if (fused) { if (count) PK_TRACED(false, true, true); else PK_TRACED(false, true, false); }
       else { if (count) PK_TRACED(false, false, true); else PK_TRACED(false, false, false); }

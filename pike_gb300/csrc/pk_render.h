@@ -9,7 +9,7 @@ namespace pk {
 
 // Traversal scheduling: fixed 32-ray chunks per warp, or persistent lanes with
 // batched refill.  Both visit every ray's nodes in the reference order.
-enum TraceMode : int { TRACE_CHUNKED = 0, TRACE_PERSISTENT = 1, TRACE_WIDE = 4 };
+enum TraceMode : int { TRACE_CHUNKED = 0, TRACE_PERSISTENT = 1, TRACE_WIDE = 4, TRACE_EXACT = 8 };
 
 // Everything a launch needs that is fixed for a configured context.
 struct LaunchCtx {

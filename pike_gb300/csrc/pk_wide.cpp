@@ -60,17 +60,12 @@ float decode(float p, float s, int q) {
 
 constexpr double MARGIN = 0x1p-18;
 
-}  // namespace
-
-int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, WideHost& out,
-                   std::string& why) {
-  out = WideHost();
-  if (n_nodes == 0) {
-    why = "empty BVH";
-    return 1;
-  }
+// Bounds of every binary node over the triangle records the test reads
+// (v0, v0 + e1, v0 + e2), widened by MARGIN * max(1, |x|).
+int node_boxes(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, std::vector<DBox>& box,
+               std::string& why) {
   // ---- conservative binary node boxes (children have larger BFS indices)
-  std::vector<DBox> box(n_nodes);
+  box.assign(n_nodes, DBox());
   for (int64_t i = (int64_t)n_nodes - 1; i >= 0; i--) {
     const int32_t* nd = nodes5 + 5 * (size_t)i;
     DBox b;
@@ -107,6 +102,20 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, u
       b.lo[a] -= MARGIN * std::max(1.0, std::fabs(b.lo[a]));
       b.hi[a] += MARGIN * std::max(1.0, std::fabs(b.hi[a]));
     }
+  return 0;
+}
+
+}  // namespace
+
+int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, WideHost& out,
+                   std::string& why) {
+  out = WideHost();
+  if (n_nodes == 0) {
+    why = "empty BVH";
+    return 1;
+  }
+  std::vector<DBox> box;
+  if (node_boxes(nodes5, n_nodes, tris, n_tris, box, why)) return 1;
   auto is_leaf = [&](uint32_t i) { return nodes5[5 * (size_t)i + 1] > -1; };
 
   // ---- collapse, breadth first
@@ -219,6 +228,49 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, u
     why = "internal: wide node count mismatch";
     return 1;
   }
+  return 0;
+}
+
+int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris,
+                       std::vector<float>& records, int32_t& root_code, std::string& why) {
+  if (n_nodes == 0) {
+    why = "empty BVH";
+    return 1;
+  }
+  std::vector<DBox> box;
+  if (node_boxes(nodes5, n_nodes, tris, n_tris, box, why)) return 1;
+  std::vector<uint32_t> rank(n_nodes);
+  uint32_t n_inner = 0;
+  for (uint32_t i = 0; i < n_nodes; i++) {
+    rank[i] = n_inner;
+    if (nodes5[5 * (size_t)i + 1] <= -1) n_inner++;
+  }
+  auto code = [&](uint32_t i) -> int32_t {
+    const int32_t t = nodes5[5 * (size_t)i + 1];
+    return t > -1 ? (int32_t)(0x80000000u | (uint32_t)t) : (int32_t)rank[i];
+  };
+  auto put = [&](float* r, const DBox& b) {  // {hi, lo} per axis, rounded outward
+    for (int a = 0; a < 3; a++) {
+      const bool empty = !(b.lo[a] <= b.hi[a]);
+      // an empty child becomes a point at 1e30: its entry distance exceeds any hit
+      r[2 * a] = empty ? 1e30f : f_up(b.hi[a]);
+      r[2 * a + 1] = empty ? 1e30f : f_down(b.lo[a]);
+    }
+  };
+  records.assign(16 * (size_t)std::max<uint32_t>(n_inner, 1u), 0.0f);
+  for (uint32_t i = 0; i < n_nodes; i++) {
+    if (nodes5[5 * (size_t)i + 1] > -1) continue;
+    const uint32_t l = (uint32_t)nodes5[5 * (size_t)i];
+    float* r = &records[16 * (size_t)rank[i]];
+    float lb[6], rb[6];
+    put(lb, box[l]);
+    put(rb, box[l + 1]);
+    std::memcpy(r, lb, 24);
+    std::memcpy(r + 6, rb, 24);
+    const int32_t c[4] = {code(l), code(l + 1), 0, 0};
+    std::memcpy(r + 12, c, 16);
+  }
+  root_code = code(0);
   return 0;
 }
 

@@ -34,4 +34,12 @@ struct WideHost {
 int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, WideHost& out,
                    std::string& why);
 
+// The binary BVH's inner records (64-byte layout of the drop-in traversal:
+// both children's boxes, then their child codes) with FP32 boxes rounded
+// outward from the same triangle-record bounds and margin as the wide nodes,
+// instead of the reference's inward-truncated snorm16 boxes.  Traversed with
+// (t, slot) ties and slack in the box tests, closest hits equal brute force.
+int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris,
+                       std::vector<float>& records, int32_t& root_code, std::string& why);
+
 }  // namespace pk

@@ -14,11 +14,12 @@ from helpers import Pair, assert_bits_equal
 pytestmark = pytest.mark.gpu
 
 WIDE = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE
+EXACT = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_EXACT
 
 
-def wide_pair(oracle, src, **kw) -> Pair:
+def wide_pair(oracle, src, mode=WIDE, **kw) -> Pair:
     pair = Pair(src, oracle, **kw)
-    pair.ctx.call("pk_set_trace_mode", WIDE)
+    pair.ctx.call("pk_set_trace_mode", mode)
     pair.P.r.set_canonical(True)
     return pair
 
@@ -29,6 +30,15 @@ def wide_nodes(ctx):
     nodes = np.zeros((int(n[0]), 24), np.float32)
     ctx.call("pk_wide_download", ptr(nodes))
     return nodes, int(depth[0])
+
+
+def test_trace_mode_rules(pk_built, oracle):
+    src = synth.small_scene(width=8, height=8)
+    pair = Pair(src, oracle)
+    for bad in (_lib.PK_TRACE_WIDE | _lib.PK_TRACE_EXACT | 1, _lib.PK_TRACE_EXACT, 16):
+        with pytest.raises(_lib.PikeError) as e:
+            pair.ctx.call("pk_set_trace_mode", bad)
+        assert e.value.code == _lib.PK_ERR_ARG
 
 
 def test_wide_structure(oracle, pk_built):
@@ -61,13 +71,14 @@ def test_wide_structure(oracle, pk_built):
     assert 2 <= depth <= 16
 
 
+@pytest.mark.parametrize("mode", [WIDE, EXACT], ids=["wide", "exact-binary"])
 @pytest.mark.parametrize("make", [
     lambda: synth.small_scene(width=64, height=48),
     lambda: synth.displaced_sphere_scene(subdivisions=4, width=64, height=40, env_size=(128, 64)),
 ])
-def test_wide_frames_match_bruteforce_oracle(oracle, pk_built, make):
+def test_wide_frames_match_bruteforce_oracle(oracle, pk_built, make, mode):
     src = make()
-    pair = wide_pair(oracle, src, threads=16)
+    pair = wide_pair(oracle, src, mode=mode, threads=16)
     pair.ctx.call("pk_set_render_state", 0, 0.0)
     pair.ctx.call("pk_render_frames", 2, 4)
     pair.ctx.call("pk_sync")
@@ -79,11 +90,12 @@ def test_wide_frames_match_bruteforce_oracle(oracle, pk_built, make):
     assert pair.counters()["err"] == 0
 
 
-def test_wide_pass_hits_match_bruteforce(oracle, pk_built):
+@pytest.mark.parametrize("mode", [WIDE, EXACT], ids=["wide", "exact-binary"])
+def test_wide_pass_hits_match_bruteforce(oracle, pk_built, mode):
     """Camera and two bounces of rays through the pass path: every closest hit
     (slot, t, barycentrics) equals the brute-force answer."""
     src = synth.displaced_sphere_scene(subdivisions=6, width=120, height=80, env_size=(128, 64))
-    pair = wide_pair(oracle, src, threads=16)
+    pair = wide_pair(oracle, src, mode=mode, threads=16)
     c, P = pair.ctx, pair.P.r
     pair.set_render_state(0)
     for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
