@@ -55,7 +55,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
-    ap.add_argument("--no-forms", action="store_true", help="skip the 8-wide BVH (form 1) measurement")
+    ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
+    ap.add_argument("--precision", action="store_true",
+                    help="also run form (1)'s 8.4M-triangle soup workload (adds about a minute)")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
                     help="inner-node record size (identical results): decoded float boxes (64) or snorm16 (32)")
     return ap.parse_args()
@@ -585,6 +587,59 @@ def binned_form(ctx, args, B: int, first_sample: int, sweep_ms: float):
             "ms_per_step": ms / steps, "note": "binned SAH, 16 bins, leaves <= 8; frames differ from the reference's"}
 
 
+def precision_form(args, local: int):
+    """Form (1)'s precision workload: the 8,388,608-triangle soup with the
+    2048x1024 env at 1920x1080, depth 4: drop-in, FP32 binary reference and
+    8-wide traversal on the same sweep-SAH tree; closest-hit agreement (camera
+    + first bounce), work per ray and throughput."""
+    from pike_gb300 import _lib, synth
+    src = synth.triangle_soup_scene()
+    ctx, bvh_ms = setup_context(src, local)
+    ctx.call("pk_set_camera", camera_struct(src))
+    B = 4
+    out = {"workload": "triangle soup 8,388,608 tris (centroids U[-50,50]^3, edges log-uniform [0.01,1]), "
+                       "1920x1080, depth 4", "bvh_build_ms": bvh_ms}
+    modes = {"dropin": _lib.PK_TRACE_PERSISTENT, "fp32_binary": _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_EXACT,
+             "wide": _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE}
+    for name, mode in modes.items():
+      try:
+        ctx.call("pk_sync")
+        ctx.timer_start()
+        ctx.call("pk_set_trace_mode", mode)
+        prep_ms = ctx.timer_stop()
+        ctx.call("pk_reset_stats")
+        ctx.call("pk_set_counting", 1)
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_render_frames", 1, B)
+        ctx.call("pk_sync")
+        cnt = read_stats(ctx)
+        ctx.call("pk_set_counting", 0)
+        ctx.call("pk_reset_stats")
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_sync")
+        ctx.timer_start()
+        ctx.call("pk_render_frames", 4, B)
+        ms = ctx.timer_stop()
+        rays = read_stats(ctx)["rays_traced"]
+        R = max(cnt["closest_rays"], 1)
+        # bytes per fetch unit: the drop-in counts three 20-byte reference nodes per
+        # inner step (one 64-byte record here), the wide traversal one 96-byte node
+        node_bytes = {"dropin": 20.0, "fp32_binary": 64.0 / 3.0, "wide": 96.0}[name]
+        out[name] = {"value": rays / (ms / 1000.0) / 1e6, "unit": UNIT, "ms_per_frame": ms / 4,
+                     "structure_ms": prep_ms, "fetch_per_closest_ray": cnt["closest_fetch"] / R,
+                     "tests_per_closest_ray": cnt["closest_tests"] / R,
+                     "node_bytes_per_closest_ray": node_bytes * cnt["closest_fetch"] / R}
+      except Exception as e:  # e.g. a traversal stack overflow reported by the device
+        out[name] = {"error": str(e)}
+    wide, exact, plain = modes["wide"], modes["fp32_binary"], modes["dropin"]
+    t, d = hit_agreement(ctx, exact, wide)
+    out["agreement_fp32_binary_vs_wide"] = {"rays": t, "differ": d, "fraction_equal": 1.0 - d / max(t, 1)}
+    t, d = hit_agreement(ctx, plain, wide)
+    out["agreement_dropin_vs_wide"] = {"rays": t, "differ": d, "fraction_equal": 1.0 - d / max(t, 1)}
+    ctx.close()
+    return out
+
+
 def gpu_arm(args):
     import ctypes as C
 
@@ -673,6 +728,8 @@ def gpu_arm(args):
         forms["adjoint"] = adjoint_form(args, local)
         forms["batching"] = batch_form(args, local)
         forms["binned_bvh"] = binned_form(ctx, args, B, first_sample, bvh_ms)
+        if args.precision:
+            forms["precision_soup"] = precision_form(args, local)
 
     if rank == 0:
         peak, peak_kind = load_peak_hbm()
