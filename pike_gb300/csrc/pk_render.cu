@@ -998,6 +998,26 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
+// Out-of-line calls for the batch megakernel: inlining both traversals, the
+// whole shade_hit body and the camera into one loop overflows the instruction
+// cache (ncu: most warps stalled waiting for instructions).
+template <bool ANY, int BLOCK, int SSTACK>
+__device__ __noinline__ void batch_trace(const SceneDev& sc, float4 o, float4 d, float& t, int& idx, uint32_t& bary,
+                                         int (*sstack)[BLOCK], uint32_t* err) {
+  uint32_t nf = 0, nt = 0;
+  traverse<ANY, false, BLOCK, SSTACK>(sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf, nt);
+}
+__device__ __noinline__ bool batch_shade(const SceneDev& sc, const EnvDev& env, float theta, int32_t samples,
+                                         uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr, V3& em, bool& eb,
+                                         float4& bo, float4& bd, float4& bt, bool& es, float4& so, float4& sd,
+                                         float4& st) {
+  return shade_one(sc, env, theta, samples, r, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd, st);
+}
+__device__ __noinline__ void batch_camera(const CamState& cam, uint32_t px, uint32_t py, uint32_t W, uint32_t H,
+                                          int32_t samples, V3& org, V3& dir) {
+  camera_ray(cam, px, py, W, H, samples, org, dir);
+}
+
 template <int BLOCK, int SSTACK>
 __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ scenes, int nscenes,
                                                  const BatchReq* __restrict__ reqs, int nreq,
@@ -1056,7 +1076,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
           pix = (uint32_t)(local % npix);
           samples = (int32_t)(fr * q.spp + (uint32_t)(local / npix));
           V3 org, dir;
-          camera_ray(q.cam, pix % q.W, pix / q.W, q.W, q.H, samples, org, dir);
+          batch_camera(q.cam, pix % q.W, pix / q.W, q.W, q.H, samples, org, dir);
           o4 = make_float4(org.x, org.y, org.z, 0.0f);
           d4 = make_float4(dir.x, dir.y, dir.z, 0.0f);
           t4 = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(pix));
@@ -1077,9 +1097,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
       const unsigned long long oi = q.out_offset + pix;
       float t;
       int idx;
-      uint32_t bary, nf = 0, nt = 0;
-      traverse<false, false, BLOCK, SSTACK>(S.sc, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, t, idx, bary, sstack, err, nf,
-                                            nt);
+      uint32_t bary;
+      batch_trace<false, BLOCK, SSTACK>(S.sc, o4, d4, t, idx, bary, sstack, err);
       float cr = 0.0f, cg = 0.0f, cb = 0.0f;
       bool next = false;
       if (idx < 0) {
@@ -1090,16 +1109,15 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
         float4 bo, bd, bt, so, sd, st;
         V3 em;
         const uint4 hr = make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u);
-        if (shade_one(S.sc, S.env, S.theta, samples, (uint32_t)bounce, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd,
-                      st)) {
+        if (batch_shade(S.sc, S.env, S.theta, samples, (uint32_t)bounce, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so,
+                        sd, st)) {
           cr = em.x; cg = em.y; cb = em.z;
         }
         if (es) {
           float ts;
           int is;
           uint32_t bs;
-          traverse<true, false, BLOCK, SSTACK>(S.sc, so.x, so.y, so.z, sd.x, sd.y, sd.z, ts, is, bs, sstack, err, nf,
-                                               nt);
+          batch_trace<true, BLOCK, SSTACK>(S.sc, so, sd, ts, is, bs, sstack, err);
           if (is < 0) {
             const V3 e = env_color(S.env, S.theta, v3(sd.x, sd.y, sd.z));
             cr += e.x * st.x; cg += e.y * st.y; cb += e.z * st.z;
