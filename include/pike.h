@@ -245,6 +245,14 @@ int pk_read_stats(pk_ctx* ctx, uint64_t out10[10]);
  * context's stream; pk_read_timing returns summed milliseconds and launch
  * counts per kernel kind: camera, trace, compact, shade, shadow, accumulate,
  * postprocess, other (16 floats: 8 times then 8 counts). */
+/* Accumulation: PK_ACCUM_RUNNING_MEAN is accumulate.wgsl's running mean (the
+ * default, bit-exact with the reference); PK_ACCUM_COMPENSATED keeps Kahan
+ * sums of max(c, 0) per pixel and writes sum / n to the accumulation buffer
+ * (the precision form; no reference counterpart).  pk_write_accum only seeds
+ * the running mean. */
+#define PK_ACCUM_RUNNING_MEAN 0
+#define PK_ACCUM_COMPENSATED 1
+int pk_set_accumulation(pk_ctx* ctx, int mode);
 int pk_set_timing(pk_ctx* ctx, int timing);
 int pk_read_timing(pk_ctx* ctx, float out16[16]);
 /* CUDA events on the context's stream: op 0 records the start event, op 1

@@ -19,6 +19,7 @@ HEADER = os.path.join(HERE, "..", "include", "pike.h")
 PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED = range(6)
 PK_BVH_SWEEP = 0
 PK_BVH_BINNED = 1
+PK_ACCUM_RUNNING_MEAN, PK_ACCUM_COMPENSATED = 0, 1
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
 PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE, PK_TRACE_EXACT = 0, 1, 2, 4, 8
 
@@ -71,6 +72,7 @@ def load(path: str = LIB_PATH):
         "pk_batch_set_config": [_P, C.c_int, C.c_int, C.c_int], "pk_batch_get_config": [_P, _P, _P, _P],
         "pk_batch_autotune": [_P, C.c_uint64, _P], "pk_batch_render": [_P, u32], "pk_batch_reset": [_P],
         "pk_batch_read": [_P, u32, _P], "pk_batch_info": [_P, _P, _P, _P], "pk_batch_latencies": [_P, _P],
+        "pk_set_accumulation": [_P, C.c_int],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],
         "pk_bvh_info": [_P, _P, _P, _P], "pk_bvh_download": [_P, _P, _P, _P],
         "pk_env_build": [_P, _P, u32, u32], "pk_env_upload": [_P, _P, u32, u32, _P, u32, _P, _P],

@@ -116,6 +116,10 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
     c->W = width; c->H = height; c->B = batch;
     c->cap = (batch + 127u) / 128u * 128u;
     c->npix = width * height;
+    if (c->kahan) {
+      c->accum_sum.alloc(c->npix);
+      c->accum_comp.alloc(c->npix);
+    }
     c->ct = compact_tiles(c->cap);
     c->st = shade_tiles(c->cap);
     kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade, &c->g_trace_wide);
@@ -911,6 +915,20 @@ int pk_set_trace_mode(pk_ctx* c, int mode) {
     return PK_OK;
   });
 }
+int pk_set_accumulation(pk_ctx* c, int mode) {
+  return guarded(c, [&]() {
+    if (mode != PK_ACCUM_RUNNING_MEAN && mode != PK_ACCUM_COMPENSATED) return fail(c, PK_ERR_ARG, "unknown accumulation mode");
+    require_config(c);
+    c->kahan = mode == PK_ACCUM_COMPENSATED;
+    if (c->kahan && c->accum_sum.n != c->npix) {
+      c->accum_sum.alloc(c->npix);
+      c->accum_comp.alloc(c->npix);
+    }
+    c->invalidate_graph();
+    return PK_OK;
+  });
+}
+
 int pk_set_timing(pk_ctx* c, int on) { return guarded(c, [&]() { c->timing = on != 0; return PK_OK; }); }
 int pk_read_timing(pk_ctx* c, float out16[16]) {
   return guarded(c, [&]() {

@@ -56,6 +56,8 @@ struct pk_ctx {
   bool cam_set = false;
   float exposure = 1.0f, saturation = 1.0f;
   DevBuf<float4> color, accum, display;
+  DevBuf<float4> accum_sum, accum_comp;  // compensated accumulation buffers
+  bool kahan = false;
   DevBuf<uchar4> display8;
   DevBuf<float4> rq[2][3], sq[3], mq[3];
   int cur = 0;
@@ -132,6 +134,8 @@ struct pk_ctx {
     L.miss_capacity = 2 * cap;
     L.trace_blocks = g_trace;
     L.trace_blocks_wide = g_trace_wide;
+    L.accum_sum = kahan ? accum_sum.p : nullptr;
+    L.accum_comp = kahan ? accum_comp.p : nullptr;
     L.compact_blocks = g_compact;
     L.shade_blocks = g_shade;
     L.trace_mode = trace_mode;

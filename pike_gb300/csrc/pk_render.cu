@@ -908,6 +908,35 @@ __global__ void __launch_bounds__(256) k_accumulate(const Counters* __restrict__
   accum[i] = a;
 }
 
+// Compensated accumulation (precision form, not the reference's running
+// mean): Kahan sums of max(c, 0) per pixel; the accumulation buffer receives
+// sum / (n + 1) so postprocess and readback see the same mean.
+__global__ void __launch_bounds__(256) k_accumulate_kahan(const Counters* __restrict__ ctr,
+                                                          const float4* __restrict__ color, float4* __restrict__ sum,
+                                                          float4* __restrict__ comp, float4* __restrict__ accum,
+                                                          uint32_t npix) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npix) return;
+  const int32_t n = ctr->samples;
+  const float4 c = color[i];
+  float4 sv = n == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : sum[i];
+  float4 cv = n == 0 ? make_float4(0.f, 0.f, 0.f, 0.f) : comp[i];
+  const float in[3] = {fmax_(c.x, 0.0f), fmax_(c.y, 0.0f), fmax_(c.z, 0.0f)};
+  float* sp = &sv.x;
+  float* cp = &cv.x;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float y = in[k] - cp[k];
+    const float t = sp[k] + y;
+    cp[k] = (t - sp[k]) - y;
+    sp[k] = t;
+  }
+  sum[i] = sv;
+  comp[i] = cv;
+  const float s1 = (float)(n + 1);
+  accum[i] = make_float4(sv.x / s1, sv.y / s1, sv.z / s1, 1.0f);
+}
+
 // postprocess.wgsl:36-99 frag_main as a compute kernel writing a headless buffer.
 __device__ __forceinline__ float rrt(float v) {
   const float a = v * (v + 0.0245786f) - 0.000090537f;
@@ -1288,7 +1317,11 @@ void launch_shade_miss(const LaunchCtx& L, RayQ M) {
 }
 
 void launch_accumulate(const LaunchCtx& L) {
-  k_accumulate<<<grid_for(L.npix, 256), 256, 0, L.stream>>>(L.ctr, L.color, L.accum, L.npix);
+  if (L.accum_sum)
+    k_accumulate_kahan<<<grid_for(L.npix, 256), 256, 0, L.stream>>>(L.ctr, L.color, L.accum_sum, L.accum_comp,
+                                                                     L.accum, L.npix);
+  else
+    k_accumulate<<<grid_for(L.npix, 256), 256, 0, L.stream>>>(L.ctr, L.color, L.accum, L.npix);
 }
 
 void launch_postprocess(const LaunchCtx& L, float exposure, float saturation) {

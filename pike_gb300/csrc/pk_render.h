@@ -26,6 +26,8 @@ struct LaunchCtx {
   uint32_t capacity;       // ray / hit / shadow queue capacity (batch rounded up to 128)
   uint32_t miss_capacity;  // 2 * capacity
   unsigned trace_blocks, compact_blocks, shade_blocks, trace_blocks_wide;
+  float4* accum_sum = nullptr;   // compensated accumulation (pk_set_accumulation), else null
+  float4* accum_comp = nullptr;
   int trace_mode;
 };
 
