@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
     ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="serial frames: no shadow traversal beside the next bounce's closest-hit traversal")
     ap.add_argument("--precision", action="store_true",
                     help="also run form (1)'s 8.4M-triangle soup workload (adds about a minute)")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
@@ -654,6 +656,7 @@ def gpu_arm(args):
     if args.node_records == 32:
         mode |= _lib.PK_TRACE_COMPACT_RECORDS
     ctx.call("pk_set_trace_mode", mode)
+    ctx.call("pk_set_frame_overlap", 0 if args.no_overlap else 1)
     cam = camera_struct(src)
     ctx.call("pk_set_camera", cam)
     B = args.bounces
@@ -752,6 +755,7 @@ def gpu_arm(args):
                        "bounces": B, "env": "2048x1024 RGBE8", "spp_mpix_per_s": spp_mpix,
                        "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
                        "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}", "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
+                       "frame_overlap": not args.no_overlap and args.trace_mode != "chunked",
                        "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
                        "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},
             "roofline": {"bound": "hbm", "kernel": "closest-hit traversal (trace.wgsl + fused shade_miss)", "achieved": achieved, "peak": peak,

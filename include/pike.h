@@ -253,6 +253,12 @@ int pk_read_stats(pk_ctx* ctx, uint64_t out10[10]);
 #define PK_ACCUM_RUNNING_MEAN 0
 #define PK_ACCUM_COMPENSATED 1
 int pk_set_accumulation(pk_ctx* ctx, int mode);
+/* overlap != 0 (the default) lets pk_render_frame run each bounce's shadow
+ * traversal concurrently with the next bounce's closest-hit traversal on a
+ * second stream of its graph; images are bit-identical either way (pixels
+ * receive their contributions in the same order).  Applies to the persistent
+ * and 8-wide traversal modes without per-kernel timing. */
+int pk_set_frame_overlap(pk_ctx* ctx, int overlap);
 int pk_set_timing(pk_ctx* ctx, int timing);
 int pk_read_timing(pk_ctx* ctx, float out16[16]);
 /* CUDA events on the context's stream: op 0 records the start event, op 1

@@ -76,6 +76,9 @@ int pk_create(pk_ctx** out, int device) {
     if (device < 0 || device >= n) throw std::runtime_error("no such CUDA device");
     check(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "attr");
     check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaEventCreateWithFlags(&c->ev_shaded, cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaEventCreateWithFlags(&c->ev_shadow, cudaEventDisableTiming), "cudaEventCreate");
     c->ctr.alloc(1);
     c->cam.alloc(1);
     check(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->stream), "memset");
@@ -100,6 +103,9 @@ int pk_destroy(pk_ctx* c) {
   for (auto e : c->event_pool) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
+  if (c->ev_shaded) cudaEventDestroy(c->ev_shaded);
+  if (c->ev_shadow) cudaEventDestroy(c->ev_shadow);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PK_OK;
@@ -593,7 +599,7 @@ int pk_trace(pk_ctx* c) {
     });
     c->timed(K_COMPACT, [&]() {
       launch_compact_trace(L, true, c->hflags.p, c->hit_list.p, c->R(c->cur), c->M(), c->ticket(0, 1),
-                           c->tiles_compact(0));
+                           c->tiles_compact(0), nullptr);
     });
     check(cudaGetLastError(), "trace");
     return PK_OK;
@@ -698,8 +704,23 @@ static void render_frame(pk_ctx* c, uint32_t bounces) {
   c->frames++;
 }
 
+// One frame as its launch sequence.  With overlap (graph capture, persistent
+// or 8-wide traversal) each bounce's shadow traversal forks onto the side
+// stream after shading and joins before the next bounce's compaction; that
+// bounce's closest-hit misses are parked in their hit records and added by
+// the compaction, so every pixel still receives its contributions in the
+// serial order (shadow of bounce b before the miss of bounce b+1).
 static void render_frame_launches(pk_ctx* c, uint32_t bounces) {
   LaunchCtx L = c->launch();
+  const bool ov = c->overlap && !c->timing && (c->trace_mode & (pk::TRACE_PERSISTENT | pk::TRACE_WIDE)) != 0;
+  L.defer_miss = ov;
+  LaunchCtx Ls = L;
+  Ls.stream = c->side;
+  bool forked = false;
+  auto join = [&]() {
+    if (forked) check(cudaStreamWaitEvent(c->stream, c->ev_shadow, 0), "cudaStreamWaitEvent");
+    forked = false;
+  };
   const uint32_t nb = std::min(bounces, MAX_BOUNCES);
   // RenderState.generateCommands + tick(): clear colour, hit/miss and ray counts
   check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
@@ -711,6 +732,7 @@ static void render_frame_launches(pk_ctx* c, uint32_t bounces) {
   for (uint32_t b = 0; b < bounces; b++) {
     const uint32_t slot = b % MAX_BOUNCES;
     if (b && slot == 0) {
+      join();  // the shadow traversal in flight still uses its slot's ticket
       check(cudaMemsetAsync(c->tickets.p, 0, c->tickets.bytes(), c->stream), "memset");
       check(cudaMemsetAsync(c->tiles.p, 0, c->tiles.bytes(), c->stream), "memset");
     }
@@ -718,20 +740,31 @@ static void render_frame_launches(pk_ctx* c, uint32_t bounces) {
       launch_trace(L, false, true, c->counting, &c->ctr.p->num_rays, c->R(c->cur), c->hrec.p, c->hflags.p,
                    c->ticket(slot, 0));
     });
+    join();
     c->timed(K_COMPACT, [&]() {
       launch_compact_trace(L, false, c->hflags.p, c->hit_list.p, c->R(c->cur), c->M(), c->ticket(slot, 1),
-                           c->tiles_compact(slot));
+                           c->tiles_compact(slot), ov ? c->hrec.p : nullptr);
     });
     c->timed(K_SHADE, [&]() {
       launch_shade(L, c->hit_list.p, c->hrec.p, c->R(c->cur), c->R(c->cur ^ 1), c->S(), c->ticket(slot, 2),
                    c->tiles_shade(slot));
     });
     c->cur ^= 1;
-    c->timed(K_SHADOW, [&]() {
-      launch_trace(L, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
+    if (ov) {
+      check(cudaEventRecord(c->ev_shaded, c->stream), "cudaEventRecord");
+      check(cudaStreamWaitEvent(c->side, c->ev_shaded, 0), "cudaStreamWaitEvent");
+      launch_trace(Ls, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
                    c->ticket(slot, 3));
-    });
+      check(cudaEventRecord(c->ev_shadow, c->side), "cudaEventRecord");
+      forked = true;
+    } else {
+      c->timed(K_SHADOW, [&]() {
+        launch_trace(L, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
+                     c->ticket(slot, 3));
+      });
+    }
   }
+  join();
   c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
   c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
   c->timed(K_OTHER, [&]() { launch_end_frame(L); });
@@ -924,6 +957,14 @@ int pk_set_accumulation(pk_ctx* c, int mode) {
       c->accum_sum.alloc(c->npix);
       c->accum_comp.alloc(c->npix);
     }
+    c->invalidate_graph();
+    return PK_OK;
+  });
+}
+
+int pk_set_frame_overlap(pk_ctx* c, int on) {
+  return guarded(c, [&]() {
+    c->overlap = on != 0;
     c->invalidate_graph();
     return PK_OK;
   });

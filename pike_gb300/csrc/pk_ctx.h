@@ -33,6 +33,11 @@ struct pk_ctx {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;
+  // Second stream of pk_render_frame's graph: each bounce's shadow traversal
+  // runs on it beside the next bounce's closest-hit traversal.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_shaded = nullptr, ev_shadow = nullptr;
+  bool overlap = true;
   std::string err;
   // configuration
   uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;

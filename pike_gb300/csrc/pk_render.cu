@@ -96,6 +96,17 @@ __device__ __forceinline__ void add_color(float4* color, uint32_t npix, uint32_t
   color[idx] = c;
 }
 
+// shade_miss.wgsl:45-57 for a ray that left the scene inside a traversal
+// kernel: add its contribution now, or (closest hit, `defer`) park it in the
+// ray's hit record {r, g, b, pixel} for the compaction of this trace to add
+// once the previous bounce's shadow rays are done with the pixel.
+template <bool ANY>
+__device__ __forceinline__ void fused_miss(float4* color, uint32_t npix, uint4* hrec, uint32_t j, uint32_t idx,
+                                           float r, float g, float b, int defer, uint32_t* err) {
+  if (!ANY && defer) hrec[j] = make_uint4(__float_as_uint(r), __float_as_uint(g), __float_as_uint(b), idx);
+  else add_color(color, npix, idx, r, g, b, 1.0f, err);
+}
+
 // trace.wgsl:191-213 main (closest hit) and trace_shadow.wgsl:192-207 main (any
 // hit).  Warps claim 32 consecutive queue slots at a time; the outcome bit of
 // every slot goes to flags[slot / 32].  FUSED: a ray that reaches the
@@ -189,7 +200,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
                                                               const uint32_t* __restrict__ countp, RayQ R,
                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
                                                               float4* __restrict__ color, uint32_t npix,
-                                                              uint32_t* __restrict__ ticket) {
+                                                              uint32_t* __restrict__ ticket, int defer) {
   __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
   int lstack[STACK_LOCAL];
   const uint32_t n = *countp;
@@ -313,8 +324,8 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_dyn(SceneDev sc, EnvDev
       } else if (FUSED) {
         const float4 tpv = R.t[j];
         const V3 e = env_color(env, theta, v3(dx, dy, dz));
-        add_color(color, npix, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y, e.z * tpv.z, 1.0f,
-                  &ctr->err);
+        fused_miss<ANY>(color, npix, hrec, j, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y,
+                        e.z * tpv.z, defer, &ctr->err);
       }
       have = false;
     }
@@ -353,7 +364,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
                                                                const uint32_t* __restrict__ countp, RayQ R,
                                                                uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
                                                                float4* __restrict__ color, uint32_t npix,
-                                                               uint32_t* __restrict__ ticket) {
+                                                               uint32_t* __restrict__ ticket, int defer) {
   __shared__ int sstack[WIDE_STACK_SMEM][TRACE_THREADS];
   __shared__ float sdist[WIDE_STACK_SMEM][TRACE_THREADS];
   int lstack[WIDE_STACK_LOCAL];
@@ -461,8 +472,8 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
       } else if (FUSED) {
         const float4 tpv = R.t[j];
         const V3 e = env_color(env, theta, v3(dx, dy, dz));
-        add_color(color, npix, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y, e.z * tpv.z, 1.0f,
-                  &ctr->err);
+        fused_miss<ANY>(color, npix, hrec, j, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y,
+                        e.z * tpv.z, defer, &ctr->err);
       }
       have = false;
     }
@@ -476,7 +487,8 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
 
 // =====================================================================
 // Stable compaction of trace / shadow outcomes.
-//   MODE 0: closest-hit flags -> hit list (+ miss queue when MISSQ)
+//   MODE 0: closest-hit flags -> hit list (+ miss queue when MISSQ; + the
+//           contributions of misses parked in miss_rec when given)
 //   MODE 1: any-hit flags     -> unoccluded shadow rays appended to the miss queue
 // =====================================================================
 constexpr int COMPACT_THREADS = 256;
@@ -486,7 +498,9 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
                                                               const uint32_t* __restrict__ flags,
                                                               uint32_t* __restrict__ hit_list, RayQ src, RayQ M,
                                                               uint32_t miss_capacity, uint32_t* __restrict__ ticket,
-                                                              unsigned long long* __restrict__ tiles) {
+                                                              unsigned long long* __restrict__ tiles,
+                                                              const uint4* __restrict__ miss_rec,
+                                                              float4* __restrict__ color, uint32_t npix) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warp[COMPACT_THREADS / 32 + 1][2];
   __shared__ unsigned long long s_excl;
@@ -527,6 +541,16 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
         const int b = __ffs(bits) - 1;
         bits &= bits - 1u;
         hit_list[k++] = w * 32u + (uint32_t)b;
+      }
+    }
+    if (MODE == 0 && !MISSQ && miss_rec) {  // misses parked by a deferring closest-hit trace
+      uint32_t bits = mm;
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        const uint4 m = miss_rec[w * 32u + (uint32_t)b];
+        add_color(color, npix, m.w, __uint_as_float(m.x), __uint_as_float(m.y), __uint_as_float(m.z), 1.0f,
+                  &ctr->err);
       }
     }
     if (MODE == 1 || MISSQ) {
@@ -1239,12 +1263,14 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
   const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
+  const int defer = (L.defer_miss && fused && !any_hit) ? 1 : 0;
   if (L.trace_mode & TRACE_WIDE) {
     const dim3 grid(L.trace_blocks_wide);
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
 #define PK_TRACEW(A, F, C) \
-  k_trace_wide<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, ticket)
+  k_trace_wide<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, \
+                                                      ticket, defer)
     if (!any_hit) {
       if (fused) { if (count) PK_TRACEW(false, true, true); else PK_TRACEW(false, true, false); }
       else { if (count) PK_TRACEW(false, false, true); else PK_TRACEW(false, false, false); }
@@ -1262,10 +1288,10 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
   do {                                                                                                             \
     if (L.trace_mode & TRACE_EXACT)                                                                                \
       k_trace_dyn<A, F, C, true><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags,       \
-                                                               L.color, L.npix, ticket);                           \
+                                                               L.color, L.npix, ticket, defer);                    \
     else                                                                                                           \
       k_trace_dyn<A, F, C, false><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags,      \
-                                                                L.color, L.npix, ticket);                          \
+                                                                L.color, L.npix, ticket, defer);                   \
   } while (0)
     if (!any_hit) {
       if (fused) { if (count) PK_TRACED(false, true, true); else PK_TRACED(false, true, false); }
@@ -1290,20 +1316,21 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
 }
 
 void launch_compact_trace(const LaunchCtx& L, bool missq, const uint32_t* flags, uint32_t* hit_list, RayQ src,
-                          RayQ M, uint32_t* ticket, unsigned long long* tiles) {
+                          RayQ M, uint32_t* ticket, unsigned long long* tiles, const uint4* miss_rec) {
   const unsigned grid = L.compact_blocks;
   if (missq)
     k_compact<0, true><<<grid, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, hit_list, src, M, L.miss_capacity,
-                                                                ticket, tiles);
+                                                                ticket, tiles, nullptr, L.color, L.npix);
   else
     k_compact<0, false><<<grid, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, hit_list, src, M, L.miss_capacity,
-                                                                 ticket, tiles);
+                                                                 ticket, tiles, miss_rec, L.color, L.npix);
 }
 
 void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, RayQ M, uint32_t* ticket,
                            unsigned long long* tiles) {
   k_compact<1, true><<<L.compact_blocks, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, nullptr, S, M,
-                                                                           L.miss_capacity, ticket, tiles);
+                                                                           L.miss_capacity, ticket, tiles, nullptr,
+                                                                           L.color, L.npix);
 }
 
 void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,

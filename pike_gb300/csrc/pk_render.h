@@ -29,6 +29,9 @@ struct LaunchCtx {
   float4* accum_sum = nullptr;   // compensated accumulation (pk_set_accumulation), else null
   float4* accum_comp = nullptr;
   int trace_mode;
+  // Closest-hit misses park their contribution in the hit record for the
+  // compaction to add (frames whose shadow traversal overlaps the next bounce).
+  bool defer_miss = false;
 };
 
 void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads);
@@ -36,8 +39,10 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads);
 // look-back kernels also take a zeroed tile-state array (one word per tile).
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket);
+// miss_rec: the hit records of a trace launched with L.defer_miss (whose parked
+// miss contributions this compaction adds), else null.
 void launch_compact_trace(const LaunchCtx& L, bool missq, const uint32_t* flags, uint32_t* hit_list, RayQ src,
-                          RayQ M, uint32_t* ticket, unsigned long long* tiles);
+                          RayQ M, uint32_t* ticket, unsigned long long* tiles, const uint4* miss_rec);
 void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, RayQ M, uint32_t* ticket,
                            unsigned long long* tiles);
 void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,

@@ -154,3 +154,24 @@ def test_counting_kernels_match_oracle_counts(oracle, pk_built):
     assert int(s[4]) == o["trace_rays"] and int(s[5]) == o["shadow_rays"]
     assert int(s[0]) == o["trace_fetch"] and int(s[1]) == o["trace_tests"]
     assert int(s[2]) == o["shadow_fetch"] and int(s[3]) == o["shadow_tests"]
+
+
+@pytest.mark.parametrize("mode,bounces", [(_lib.PK_TRACE_PERSISTENT, 8), (_lib.PK_TRACE_PERSISTENT, 20),
+                                          (_lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE, 8)])
+def test_frame_overlap_is_bit_identical(oracle, pk_built, mode, bounces):
+    """Shadow traversal of bounce b beside the closest-hit traversal of b+1 (the
+    default) against the serial frame; 20 bounces wrap the 16 per-bounce
+    ticket slots.  The persistent binary mode is also checked against the oracle."""
+    src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
+    pair = Pair(src, oracle)
+    pair.ctx.call("pk_set_trace_mode", mode)  # after the BVH: the 8-wide tree is built from it
+    fused_frames(pair, 2, bounces)
+    on = pair.image("accum").copy()
+    assert pair.counters()["err"] == 0
+    pair.ctx.call("pk_set_frame_overlap", 0)
+    pair.ctx.call("pk_write_accum", ptr(np.zeros_like(on)))
+    fused_frames(pair, 2, bounces)
+    assert_bits_equal(pair.image("accum"), on, "serial vs overlapped frame")
+    if mode == _lib.PK_TRACE_PERSISTENT:
+        oracle_frames(pair, 2, bounces)
+        assert_bits_equal(on, pair.P.r.accum(), "overlapped frame vs oracle")
