@@ -74,6 +74,7 @@ def load(path: str = LIB_PATH):
         "pk_batch_read": [_P, u32, _P], "pk_batch_info": [_P, _P, _P, _P], "pk_batch_latencies": [_P, _P],
         "pk_set_accumulation": [_P, C.c_int],
         "pk_set_frame_overlap": [_P, C.c_int],
+        "pk_set_frames_in_flight": [_P, C.c_int],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],
         "pk_bvh_info": [_P, _P, _P, _P], "pk_bvh_download": [_P, _P, _P, _P],
         "pk_env_build": [_P, _P, u32, u32], "pk_env_upload": [_P, _P, u32, u32, _P, u32, _P, _P],

@@ -28,17 +28,102 @@ int fail(pk_ctx* c, int code, const std::string& msg) {
   return code;
 }
 
-template <class F>
-int guarded(pk_ctx* c, F fn) {
+// Orders the API stream after every frame still in flight and after the last
+// asynchronous display read, so what follows on it sees their results and may
+// overwrite what they read.
+void join_frames(pk_ctx* c) {
+  for (FrameSlot& s : c->slot)
+    if (s.busy) {
+      check(cudaStreamWaitEvent(c->stream, s.ev_done, 0), "cudaStreamWaitEvent");
+      s.busy = false;
+    }
+  if (c->read_pending) check(cudaStreamWaitEvent(c->stream, c->ev_read, 0), "cudaStreamWaitEvent");
+  c->read_pending = false;
+  c->tail_pending = false;
+}
+
+// Brings slot 0's counters and camera up to the render state the host holds
+// (pk_set_render_state, pk_set_camera, frames rendered since).
+void apply_state(pk_ctx* c) {
+  if (!c->state_dirty || !c->ctr.p) return;
+  launch_set_state(c->stream, c->ctr.p, c->cam.p, c->samples_next, c->theta_next, c->cam_host, c->cam_set);
+  check(cudaGetLastError(), "k_set_state");
+  c->state_dirty = false;
+}
+
+template <bool JOIN, class F>
+int guarded_impl(pk_ctx* c, F fn) {
   if (!c) return PK_ERR_ARG;
   try {
     check(cudaSetDevice(c->device), "cudaSetDevice");
+    if (JOIN) {
+      join_frames(c);
+      apply_state(c);
+    }
     return fn();
   } catch (CudaError& e) {
     return fail(c, PK_ERR_CUDA, e.what());
   } catch (std::exception& e) {
     return fail(c, PK_ERR_ARG, e.what());
   }
+}
+// Entry points that touch device state run after the frames in flight.
+template <class F>
+int guarded(pk_ctx* c, F fn) {
+  return guarded_impl<true>(c, fn);
+}
+// Frame submission, render state and asynchronous reads order themselves.
+template <class F>
+int guarded_nojoin(pk_ctx* c, F fn) {
+  return guarded_impl<false>(c, fn);
+}
+
+// Buffers of frame slot k, sized for the current configuration.
+void alloc_slot(pk_ctx* c, int k) {
+  FrameSlot& s = c->slot[k];
+  s.drop_graph();
+  if (!s.ctr.p) {
+    s.ctr.alloc(1);
+    check(cudaMemsetAsync(s.ctr.p, 0, sizeof(Counters), c->stream), "memset");
+  }
+  if (!s.cam.p) s.cam.alloc(1);
+  for (int i = 0; i < 3; i++) {
+    s.rq[0][i].alloc(c->cap);
+    s.rq[1][i].alloc(c->cap);
+    s.sq[i].alloc(c->cap);
+  }
+  s.hrec.alloc(c->cap);
+  s.hflags.alloc(c->cap / 32 + 1);
+  s.sflags.alloc(c->cap / 32 + 1);
+  s.hit_list.alloc(c->cap);
+  s.color.alloc(c->npix);
+  s.tickets.alloc(4 * MAX_BOUNCES);
+  s.tiles.alloc((size_t)MAX_BOUNCES * (2 * c->ct + c->st));
+  check(cudaMemsetAsync(s.color.p, 0, s.color.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(s.hflags.p, 0, s.hflags.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(s.sflags.p, 0, s.sflags.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(s.hit_list.p, 0, s.hit_list.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(s.hrec.p, 0, s.hrec.bytes(), c->stream), "memset");
+  check(cudaMemsetAsync(&s.ctr.p->num_hits, 0, 16, c->stream), "memset");
+  s.cur = 0;
+  s.cap = c->cap;
+}
+
+void release_slot(FrameSlot& s) {
+  s.drop_graph();
+  for (int i = 0; i < 3; i++) {
+    s.rq[0][i].release();
+    s.rq[1][i].release();
+    s.sq[i].release();
+  }
+  s.hrec.release();
+  s.hflags.release();
+  s.sflags.release();
+  s.hit_list.release();
+  s.color.release();
+  s.tickets.release();
+  s.tiles.release();
+  s.cap = 0;
 }
 
 template <class T>
@@ -76,9 +161,15 @@ int pk_create(pk_ctx** out, int device) {
     if (device < 0 || device >= n) throw std::runtime_error("no such CUDA device");
     check(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device), "attr");
     check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    check(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking), "cudaStreamCreate");
-    check(cudaEventCreateWithFlags(&c->ev_shaded, cudaEventDisableTiming), "cudaEventCreate");
-    check(cudaEventCreateWithFlags(&c->ev_shadow, cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (cudaEvent_t* e : {&c->ev_api, &c->ev_tail, &c->ev_read})
+      check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+    for (FrameSlot& s : c->slot) {
+      check(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+      check(cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking), "cudaStreamCreate");
+      for (cudaEvent_t* e : {&s.ev_shaded, &s.ev_shadow, &s.ev_done})
+        check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+    }
     c->ctr.alloc(1);
     c->cam.alloc(1);
     check(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->stream), "memset");
@@ -97,15 +188,26 @@ int pk_create(pk_ctx** out, int device) {
 int pk_destroy(pk_ctx* c) {
   if (!c) return PK_ERR_ARG;
   cudaSetDevice(c->device);
+  for (FrameSlot& s : c->slot) {
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    if (s.side) cudaStreamSynchronize(s.side);
+  }
+  if (c->copy) cudaStreamSynchronize(c->copy);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->frame_graph) cudaGraphExecDestroy(c->frame_graph);
+  for (FrameSlot& s : c->slot) {
+    s.drop_graph();
+    for (cudaEvent_t e : {s.ev_shaded, s.ev_shadow, s.ev_done})
+      if (e) cudaEventDestroy(e);
+    if (s.side) cudaStreamDestroy(s.side);
+    if (s.stream) cudaStreamDestroy(s.stream);
+  }
+  for (cudaEvent_t e : {c->ev_api, c->ev_tail, c->ev_read})
+    if (e) cudaEventDestroy(e);
+  if (c->copy) cudaStreamDestroy(c->copy);
   for (auto& p : c->events) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto e : c->event_pool) cudaEventDestroy(e);
   if (c->t0) cudaEventDestroy(c->t0);
   if (c->t1) cudaEventDestroy(c->t1);
-  if (c->ev_shaded) cudaEventDestroy(c->ev_shaded);
-  if (c->ev_shadow) cudaEventDestroy(c->ev_shadow);
-  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PK_OK;
@@ -129,33 +231,17 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
     c->ct = compact_tiles(c->cap);
     c->st = shade_tiles(c->cap);
     kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade, &c->g_trace_wide);
-    for (int i = 0; i < 3; i++) {
-      c->rq[0][i].alloc(c->cap);
-      c->rq[1][i].alloc(c->cap);
-      c->sq[i].alloc(c->cap);
-      c->mq[i].alloc(2 * (size_t)c->cap);
-    }
-    c->hrec.alloc(c->cap);
-    c->hflags.alloc(c->cap / 32 + 1);
-    c->sflags.alloc(c->cap / 32 + 1);
-    c->hit_list.alloc(c->cap);
-    c->color.alloc(c->npix);
+    for (int i = 0; i < 3; i++) c->mq[i].alloc(2 * (size_t)c->cap);
+    alloc_slot(c, 0);
+    release_slot(c->slot[1]);  // sized again on first use
+    c->next_slot = c->last_slot = 0;
     c->accum.alloc(c->npix);
     c->display.alloc(c->npix);
     c->display8.alloc(c->npix);
-    c->tickets.alloc(4 * MAX_BOUNCES);
-    c->tiles.alloc((size_t)MAX_BOUNCES * (2 * c->ct + c->st));
-    check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
     check(cudaMemsetAsync(c->accum.p, 0, c->accum.bytes(), c->stream), "memset");
     check(cudaMemsetAsync(c->display.p, 0, c->display.bytes(), c->stream), "memset");
     check(cudaMemsetAsync(c->display8.p, 0, c->display8.bytes(), c->stream), "memset");
-    check(cudaMemsetAsync(c->hflags.p, 0, c->hflags.bytes(), c->stream), "memset");
-    check(cudaMemsetAsync(c->sflags.p, 0, c->sflags.bytes(), c->stream), "memset");
-    check(cudaMemsetAsync(c->hit_list.p, 0, c->hit_list.bytes(), c->stream), "memset");
-    check(cudaMemsetAsync(c->hrec.p, 0, c->hrec.bytes(), c->stream), "memset");
-    check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 16, c->stream), "memset");
     check(cudaStreamSynchronize(c->stream), "sync");
-    c->cur = 0;
     return PK_OK;
   });
 }
@@ -511,16 +597,20 @@ int pk_env_download(pk_ctx* c, int32_t* bins2, int32_t* coords2, float* pdf) {
 }
 
 // ---------------- render state ----------------
+// The render state and camera are kept on the host and handed to each frame
+// by value (and to slot 0 before a pass), so setting them never waits for a
+// frame in flight.
 int pk_set_render_state(pk_ctx* c, int32_t samples, float env_theta) {
-  return guarded(c, [&]() {
-    struct { int32_t s; float t; } h{samples, env_theta};
-    check(cudaMemcpyAsync(c->ctr.p, &h, 8, cudaMemcpyHostToDevice, c->stream), "H2D");
+  return guarded_nojoin(c, [&]() {
+    c->samples_next = samples;
+    c->theta_next = env_theta;
+    c->state_dirty = true;
     return PK_OK;
   });
 }
 
 int pk_set_camera(pk_ctx* c, const pk_camera_state* cam) {
-  return guarded(c, [&]() {
+  return guarded_nojoin(c, [&]() {
     require_config(c);
     if (!cam) return fail(c, PK_ERR_ARG, "null camera");
     CamState s;
@@ -534,8 +624,9 @@ int pk_set_camera(pk_ctx* c, const pk_camera_state* cam) {
     s.distortion = cam->distortion;
     s.bokeh = cam->bokeh;
     s.invocation_offset = cam->invocation_offset;
-    check(cudaMemcpyAsync(c->cam.p, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream), "H2D");
+    c->cam_host = s;
     c->cam_set = true;
+    c->state_dirty = true;
     return PK_OK;
   });
 }
@@ -551,6 +642,7 @@ int pk_set_postprocess(pk_ctx* c, float exposure, float saturation) {
 
 int pk_clear_color(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_config(c);
     check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
     return PK_OK;
@@ -558,12 +650,14 @@ int pk_clear_color(pk_ctx* c) {
 }
 int pk_clear_hits_misses(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 8, c->stream), "memset");
     return PK_OK;
   });
 }
 int pk_clear_rays(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     check(cudaMemsetAsync(&c->ctr.p->num_rays, 0, 8, c->stream), "memset");
     return PK_OK;
   });
@@ -577,6 +671,7 @@ static void reset_slot(pk_ctx* c, uint32_t slot) {
 
 int pk_camera(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_config(c);
     if (!c->cam_set) return fail(c, PK_ERR_STATE, "no camera");
     LaunchCtx L = c->launch();
@@ -589,6 +684,7 @@ int pk_camera(pk_ctx* c) {
 
 int pk_trace(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_render(c);
     LaunchCtx L = c->launch();
     reset_slot(c, 0);
@@ -608,6 +704,7 @@ int pk_trace(pk_ctx* c) {
 
 int pk_shade_hit(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_render(c);
     LaunchCtx L = c->launch();
     reset_slot(c, 0);
@@ -623,6 +720,7 @@ int pk_shade_hit(pk_ctx* c) {
 
 int pk_trace_shadow(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_render(c);
     LaunchCtx L = c->launch();
     reset_slot(c, 0);
@@ -637,6 +735,7 @@ int pk_trace_shadow(pk_ctx* c) {
 
 int pk_shade_miss(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_config(c);
     if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
     LaunchCtx L = c->launch();
@@ -648,6 +747,7 @@ int pk_shade_miss(pk_ctx* c) {
 
 int pk_accumulate(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_config(c);
     LaunchCtx L = c->launch();
     c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
@@ -658,6 +758,7 @@ int pk_accumulate(pk_ctx* c) {
 
 int pk_postprocess(pk_ctx* c) {
   return guarded(c, [&]() {
+    c->last_slot = 0;
     require_config(c);
     LaunchCtx L = c->launch();
     c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
@@ -666,114 +767,151 @@ int pk_postprocess(pk_ctx* c) {
   });
 }
 
-static void render_frame_launches(pk_ctx* c, uint32_t bounces);
-
-// pk_render_frame's launches are captured once into a CUDA graph and replayed
-// (the sequence only reads device-side counts, so it is the same every frame);
-// with per-kernel timing on, the launches are issued directly instead.
-static void render_frame(pk_ctx* c, uint32_t bounces) {
-  if (c->timing) {
-    render_frame_launches(c, bounces);
-    return;
-  }
-  if (!c->frame_graph || c->graph_bounces != bounces || c->graph_counting != c->counting ||
-      c->graph_key != c->state_version) {
-    if (c->frame_graph) cudaGraphExecDestroy(c->frame_graph);
-    c->frame_graph = nullptr;
-    cudaGraph_t g = nullptr;
-    check(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    try {
-      render_frame_launches(c, bounces);
-    } catch (...) {
-      cudaStreamEndCapture(c->stream, &g);
-      if (g) cudaGraphDestroy(g);
-      throw;
-    }
-    check(cudaStreamEndCapture(c->stream, &g), "cudaStreamEndCapture");
-    cudaGraphExec_t e = nullptr;
-    const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
-    cudaGraphDestroy(g);
-    check(ie, "cudaGraphInstantiate");
-    c->frame_graph = e;
-    c->graph_bounces = bounces;
-    c->graph_counting = c->counting;
-    c->graph_key = c->state_version;
-    c->frames--;  // the capture itself rendered nothing
-  }
-  check(cudaGraphLaunch(c->frame_graph, c->stream), "cudaGraphLaunch");
-  c->frames++;
-}
-
-// One frame as its launch sequence.  With overlap (graph capture, persistent
-// or 8-wide traversal) each bounce's shadow traversal forks onto the side
-// stream after shading and joins before the next bounce's compaction; that
-// bounce's closest-hit misses are parked in their hit records and added by
-// the compaction, so every pixel still receives its contributions in the
-// serial order (shadow of bounce b before the miss of bounce b+1).
-static void render_frame_launches(pk_ctx* c, uint32_t bounces) {
-  LaunchCtx L = c->launch();
+// One frame of slot k as its launch sequence on `st`.  With overlap
+// (persistent or 8-wide traversal, no per-kernel timing) each bounce's shadow
+// traversal forks onto the slot's side stream after shading and joins before
+// the next bounce's compaction; that bounce's closest-hit misses are parked
+// in their hit records and added by the compaction, so every pixel still
+// receives its contributions in the serial order (shadow of bounce b before
+// the miss of bounce b+1).  `tail`: accumulate, postprocess and the sample
+// count too (frames in flight issue those outside, ordered across slots).
+static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bounces, bool tail) {
+  FrameSlot& fs = c->slot[k];
+  LaunchCtx L = c->launch(k, st);
   const bool ov = c->overlap && !c->timing && (c->trace_mode & (pk::TRACE_PERSISTENT | pk::TRACE_WIDE)) != 0;
   L.defer_miss = ov;
   LaunchCtx Ls = L;
-  Ls.stream = c->side;
+  Ls.stream = fs.side;
   bool forked = false;
   auto join = [&]() {
-    if (forked) check(cudaStreamWaitEvent(c->stream, c->ev_shadow, 0), "cudaStreamWaitEvent");
+    if (forked) check(cudaStreamWaitEvent(st, fs.ev_shadow, 0), "cudaStreamWaitEvent");
     forked = false;
   };
   const uint32_t nb = std::min(bounces, MAX_BOUNCES);
   // RenderState.generateCommands + tick(): clear colour, hit/miss and ray counts
-  check(cudaMemsetAsync(c->color.p, 0, c->color.bytes(), c->stream), "memset");
-  check(cudaMemsetAsync(&c->ctr.p->num_hits, 0, 16, c->stream), "memset");
-  check(cudaMemsetAsync(c->tickets.p, 0, c->tickets.bytes(), c->stream), "memset");
-  check(cudaMemsetAsync(c->tiles.p, 0, (size_t)std::max(nb, 1u) * (2 * c->ct + c->st) * 8, c->stream), "memset");
-  c->cur = 0;
-  c->timed(K_CAMERA, [&]() { launch_camera(L, c->R(0), c->cap); });
+  check(cudaMemsetAsync(fs.color.p, 0, fs.color.bytes(), st), "memset");
+  check(cudaMemsetAsync(&fs.ctr.p->num_hits, 0, 16, st), "memset");
+  check(cudaMemsetAsync(fs.tickets.p, 0, fs.tickets.bytes(), st), "memset");
+  check(cudaMemsetAsync(fs.tiles.p, 0, (size_t)std::max(nb, 1u) * (2 * c->ct + c->st) * 8, st), "memset");
+  fs.cur = 0;
+  c->timed(K_CAMERA, [&]() { launch_camera(L, fs.R(0), c->cap); });
   for (uint32_t b = 0; b < bounces; b++) {
     const uint32_t slot = b % MAX_BOUNCES;
     if (b && slot == 0) {
       join();  // the shadow traversal in flight still uses its slot's ticket
-      check(cudaMemsetAsync(c->tickets.p, 0, c->tickets.bytes(), c->stream), "memset");
-      check(cudaMemsetAsync(c->tiles.p, 0, c->tiles.bytes(), c->stream), "memset");
+      check(cudaMemsetAsync(fs.tickets.p, 0, fs.tickets.bytes(), st), "memset");
+      check(cudaMemsetAsync(fs.tiles.p, 0, fs.tiles.bytes(), st), "memset");
     }
     c->timed(K_TRACE, [&]() {
-      launch_trace(L, false, true, c->counting, &c->ctr.p->num_rays, c->R(c->cur), c->hrec.p, c->hflags.p,
-                   c->ticket(slot, 0));
+      launch_trace(L, false, true, c->counting, &fs.ctr.p->num_rays, fs.R(fs.cur), fs.hrec.p, fs.hflags.p,
+                   fs.ticket(slot, 0));
     });
     join();
     c->timed(K_COMPACT, [&]() {
-      launch_compact_trace(L, false, c->hflags.p, c->hit_list.p, c->R(c->cur), c->M(), c->ticket(slot, 1),
-                           c->tiles_compact(slot), ov ? c->hrec.p : nullptr);
+      launch_compact_trace(L, false, fs.hflags.p, fs.hit_list.p, fs.R(fs.cur), c->M(), fs.ticket(slot, 1),
+                           c->tiles_compact(slot, k), ov ? fs.hrec.p : nullptr);
     });
     c->timed(K_SHADE, [&]() {
-      launch_shade(L, c->hit_list.p, c->hrec.p, c->R(c->cur), c->R(c->cur ^ 1), c->S(), c->ticket(slot, 2),
-                   c->tiles_shade(slot));
+      launch_shade(L, fs.hit_list.p, fs.hrec.p, fs.R(fs.cur), fs.R(fs.cur ^ 1), fs.S(), fs.ticket(slot, 2),
+                   c->tiles_shade(slot, k));
     });
-    c->cur ^= 1;
+    fs.cur ^= 1;
     if (ov) {
-      check(cudaEventRecord(c->ev_shaded, c->stream), "cudaEventRecord");
-      check(cudaStreamWaitEvent(c->side, c->ev_shaded, 0), "cudaStreamWaitEvent");
-      launch_trace(Ls, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
-                   c->ticket(slot, 3));
-      check(cudaEventRecord(c->ev_shadow, c->side), "cudaEventRecord");
+      check(cudaEventRecord(fs.ev_shaded, st), "cudaEventRecord");
+      check(cudaStreamWaitEvent(fs.side, fs.ev_shaded, 0), "cudaStreamWaitEvent");
+      launch_trace(Ls, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
+                   fs.ticket(slot, 3));
+      check(cudaEventRecord(fs.ev_shadow, fs.side), "cudaEventRecord");
       forked = true;
     } else {
       c->timed(K_SHADOW, [&]() {
-        launch_trace(L, true, true, c->counting, &c->ctr.p->num_shadow, c->S(), nullptr, c->sflags.p,
-                     c->ticket(slot, 3));
+        launch_trace(L, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
+                     fs.ticket(slot, 3));
       });
     }
   }
   join();
-  c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
-  c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
-  c->timed(K_OTHER, [&]() { launch_end_frame(L); });
+  if (tail) {
+    c->timed(K_ACCUM, [&]() { launch_accumulate(L); });
+    c->timed(K_POST, [&]() { launch_postprocess(L, c->exposure, c->saturation); });
+    c->timed(K_OTHER, [&]() { launch_end_frame(L); });
+  }
   check(cudaGetLastError(), "render_frame");
+}
+
+// pk_render_frame.  A frame's launches are captured once per slot into a CUDA
+// graph and replayed (the sequence only reads device-side counts).  With two
+// frames in flight, frames alternate between the slots' streams: each waits
+// for the API stream, takes the render state by value, replays its graph,
+// then accumulates and postprocesses after the previous frame did (the
+// accumulation and display buffers are shared) and after the last
+// asynchronous display read.  With per-kernel timing the launches are issued
+// directly on the API stream.
+static void render_frame(pk_ctx* c, uint32_t bounces) {
+  const bool piped = c->in_flight == 2 && !c->timing;
+  const int k = piped ? c->next_slot : 0;
+  FrameSlot& fs = c->slot[k];
+  if (fs.cap != c->cap) alloc_slot(c, k);
+  const cudaStream_t st = piped ? fs.stream : c->stream;
+  if (piped) {
+    check(cudaEventRecord(c->ev_api, c->stream), "cudaEventRecord");
+    check(cudaStreamWaitEvent(st, c->ev_api, 0), "cudaStreamWaitEvent");
+  } else if (c->read_pending) {  // the display is rewritten below
+    check(cudaStreamWaitEvent(st, c->ev_read, 0), "cudaStreamWaitEvent");
+    c->read_pending = false;
+  }
+  launch_set_state(st, fs.ctr.p, fs.cam.p, c->samples_next, c->theta_next, c->cam_host, true);
+  if (c->timing) {
+    render_frame_launches(c, k, st, bounces, true);
+  } else {
+    const bool tail = !piped;
+    if (!fs.graph || fs.graph_bounces != bounces || fs.graph_counting != c->counting ||
+        fs.graph_key != c->state_version || fs.graph_tail != tail) {
+      fs.drop_graph();
+      cudaGraph_t g = nullptr;
+      check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+      try {
+        render_frame_launches(c, k, st, bounces, tail);
+      } catch (...) {
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      check(cudaStreamEndCapture(st, &g), "cudaStreamEndCapture");
+      cudaGraphExec_t e = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
+      cudaGraphDestroy(g);
+      check(ie, "cudaGraphInstantiate");
+      fs.graph = e;
+      fs.graph_bounces = bounces;
+      fs.graph_counting = c->counting;
+      fs.graph_key = c->state_version;
+      fs.graph_tail = tail;
+    }
+    check(cudaGraphLaunch(fs.graph, st), "cudaGraphLaunch");
+  }
+  if (piped) {
+    LaunchCtx L = c->launch(k, st);
+    if (c->tail_pending) check(cudaStreamWaitEvent(st, c->ev_tail, 0), "cudaStreamWaitEvent");
+    launch_accumulate(L);
+    if (c->read_pending) check(cudaStreamWaitEvent(st, c->ev_read, 0), "cudaStreamWaitEvent");
+    launch_postprocess(L, c->exposure, c->saturation);
+    launch_end_frame(L);
+    check(cudaGetLastError(), "render_frame");
+    check(cudaEventRecord(c->ev_tail, st), "cudaEventRecord");
+    check(cudaEventRecord(fs.ev_done, st), "cudaEventRecord");
+    c->tail_pending = true;
+    fs.busy = true;
+    c->next_slot ^= 1;
+  }
+  c->last_slot = k;
+  c->samples_next++;
+  c->state_dirty = true;
   c->frames++;
 }
 
 int pk_render_frame(pk_ctx* c, uint32_t bounces) {
-  return guarded(c, [&]() {
+  return guarded_nojoin(c, [&]() {
     require_render(c);
     if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
     render_frame(c, bounces);
@@ -782,7 +920,7 @@ int pk_render_frame(pk_ctx* c, uint32_t bounces) {
 }
 
 int pk_render_frames(pk_ctx* c, uint32_t frames, uint32_t bounces) {
-  return guarded(c, [&]() {
+  return guarded_nojoin(c, [&]() {
     require_render(c);
     if (!c->env_ready) return fail(c, PK_ERR_STATE, "no environment");
     for (uint32_t f = 0; f < frames; f++) render_frame(c, bounces);
@@ -796,7 +934,12 @@ int pk_sync(pk_ctx* c) {
     check(cudaStreamSynchronize(c->stream), "sync");
     c->collect_events();
     uint32_t err = 0;
-    check(cudaMemcpy(&err, &c->ctr.p->err, 4, cudaMemcpyDeviceToHost), "D2H");
+    for (FrameSlot& fs : c->slot) {
+      if (!fs.ctr.p) continue;
+      uint32_t e = 0;
+      check(cudaMemcpy(&e, &fs.ctr.p->err, 4, cudaMemcpyDeviceToHost), "D2H");
+      err |= e;
+    }
     if (err) {
       char buf[96];
       std::snprintf(buf, sizeof buf, "device error flags 0x%x", err);
@@ -811,7 +954,14 @@ int pk_read_counters(pk_ctx* c, uint32_t out8[8]) {
     if (!out8) return fail(c, PK_ERR_ARG, "null output");
     Counters h;
     check(cudaStreamSynchronize(c->stream), "sync");
-    check(cudaMemcpy(&h, c->ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
+    check(cudaMemcpy(&h, c->slot[c->last_slot].ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
+    const int other = c->last_slot ^ 1;
+    if (c->slot[other].ctr.p) {
+      Counters o;
+      check(cudaMemcpy(&o, c->slot[other].ctr.p, sizeof(o), cudaMemcpyDeviceToHost), "D2H");
+      h.rays_traced += o.rays_traced;
+      h.err |= o.err;
+    }
     out8[0] = (uint32_t)h.samples; out8[1] = h.num_hits; out8[2] = h.num_misses; out8[3] = h.num_rays;
     out8[4] = h.num_shadow; out8[5] = h.err;
     out8[6] = (uint32_t)(h.rays_traced & 0xffffffffu); out8[7] = (uint32_t)(h.rays_traced >> 32);
@@ -878,7 +1028,9 @@ static int read_px(pk_ctx* c, const void* src, void* dst, size_t bytes) {
     return PK_OK;
   });
 }
-int pk_read_color(pk_ctx* c, float* out) { return c ? read_px(c, c->color.p, out, c->color.bytes()) : PK_ERR_ARG; }
+int pk_read_color(pk_ctx* c, float* out) {
+  return c ? read_px(c, c->slot[c->last_slot].color.p, out, c->color.bytes()) : PK_ERR_ARG;
+}
 int pk_read_accum(pk_ctx* c, float* out) { return c ? read_px(c, c->accum.p, out, c->accum.bytes()) : PK_ERR_ARG; }
 int pk_write_accum(pk_ctx* c, const float* in) {
   return guarded(c, [&]() {
@@ -903,7 +1055,10 @@ int pk_read_display(pk_ctx* c, float* out, uint8_t* out8) {
 int pk_set_counting(pk_ctx* c, int on) { return guarded(c, [&]() { c->counting = on != 0; return PK_OK; }); }
 int pk_reset_stats(pk_ctx* c) {
   return guarded(c, [&]() {
-    check(cudaMemsetAsync(&c->ctr.p->rays_traced, 0, sizeof(Counters) - offsetof(Counters, rays_traced), c->stream), "memset");
+    for (FrameSlot& fs : c->slot)
+      if (fs.ctr.p)
+        check(cudaMemsetAsync(&fs.ctr.p->rays_traced, 0, sizeof(Counters) - offsetof(Counters, rays_traced), c->stream),
+              "memset");
     check(cudaStreamSynchronize(c->stream), "sync");
     c->collect_events();
     for (int k = 0; k < N_KINDS; k++) { c->kind_ms[k] = 0; c->kind_n[k] = 0; }
@@ -914,11 +1069,15 @@ int pk_reset_stats(pk_ctx* c) {
 int pk_read_stats(pk_ctx* c, uint64_t out10[10]) {
   return guarded(c, [&]() {
     if (!out10) return fail(c, PK_ERR_ARG, "null output");
-    Counters h;
     check(cudaStreamSynchronize(c->stream), "sync");
-    check(cudaMemcpy(&h, c->ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
-    for (int i = 0; i < 8; i++) out10[i] = h.stat[i];
-    out10[8] = h.rays_traced;
+    for (int i = 0; i < 9; i++) out10[i] = 0;
+    for (FrameSlot& fs : c->slot) {
+      if (!fs.ctr.p) continue;
+      Counters h;
+      check(cudaMemcpy(&h, fs.ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
+      for (int i = 0; i < 8; i++) out10[i] += h.stat[i];
+      out10[8] += h.rays_traced;
+    }
     out10[9] = c->frames;
     return PK_OK;
   });
@@ -970,6 +1129,16 @@ int pk_set_frame_overlap(pk_ctx* c, int on) {
   });
 }
 
+int pk_set_frames_in_flight(pk_ctx* c, int n) {
+  return guarded(c, [&]() {
+    if (n != 1 && n != 2) return fail(c, PK_ERR_ARG, "frames in flight must be 1 or 2");
+    c->in_flight = n;
+    c->next_slot = 0;
+    c->invalidate_graph();
+    return PK_OK;
+  });
+}
+
 int pk_set_timing(pk_ctx* c, int on) { return guarded(c, [&]() { c->timing = on != 0; return PK_OK; }); }
 int pk_read_timing(pk_ctx* c, float out16[16]) {
   return guarded(c, [&]() {
@@ -1012,11 +1181,18 @@ int pk_host_free(pk_ctx* c, void* p) {
   });
 }
 
+// On the copy stream, after the API stream and the last frame's postprocess;
+// the next frame's postprocess waits for it.  Complete after pk_sync.
 int pk_read_display_async(pk_ctx* c, uint8_t* out8) {
-  return guarded(c, [&]() {
+  return guarded_nojoin(c, [&]() {
     require_config(c);
     if (!out8) return fail(c, PK_ERR_ARG, "null output");
-    check(cudaMemcpyAsync(out8, c->display8.p, c->display8.bytes(), cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaEventRecord(c->ev_api, c->stream), "cudaEventRecord");
+    check(cudaStreamWaitEvent(c->copy, c->ev_api, 0), "cudaStreamWaitEvent");
+    if (c->tail_pending) check(cudaStreamWaitEvent(c->copy, c->ev_tail, 0), "cudaStreamWaitEvent");
+    check(cudaMemcpyAsync(out8, c->display8.p, c->display8.bytes(), cudaMemcpyDeviceToHost, c->copy), "D2H");
+    check(cudaEventRecord(c->ev_read, c->copy), "cudaEventRecord");
+    c->read_pending = true;
     return PK_OK;
   });
 }

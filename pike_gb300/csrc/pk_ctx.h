@@ -20,6 +20,42 @@ struct EventPair {
   cudaEvent_t a, b;
 };
 
+// The transient state of one frame of pk_render_frame.  Two slots let two
+// frames be in flight: each renders on its own stream (plus a side stream for
+// its shadow traversals) from its own counters, camera, colour buffer and
+// queues; the scene, BVH, environment, accumulation and display buffers are
+// shared.  Slot 0 is also the state of the pass-by-pass API.
+struct FrameSlot {
+  DevBuf<Counters> ctr;
+  DevBuf<CamState> cam;
+  DevBuf<float4> color;
+  DevBuf<float4> rq[2][3], sq[3];
+  DevBuf<uint4> hrec;
+  DevBuf<uint32_t> hflags, sflags, hit_list;
+  DevBuf<uint32_t> tickets;          // 4 per bounce slot
+  DevBuf<unsigned long long> tiles;  // per bounce slot: ct (compact) + st (shade) + ct (shadow compact)
+  int cur = 0;
+  uint32_t cap = 0;                  // queue capacity the buffers were sized for (0: none)
+  cudaStream_t stream = nullptr;     // frames of this slot when two are in flight
+  cudaStream_t side = nullptr;       // shadow traversals (frame overlap)
+  cudaEvent_t ev_shaded = nullptr, ev_shadow = nullptr, ev_done = nullptr;
+  bool busy = false;                 // a frame was issued here since the last join
+  // CUDA graph of this slot's frame; rebuilt when any captured pointer or
+  // launch parameter changes.
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_bounces = 0;
+  bool graph_counting = false, graph_tail = false;
+  unsigned long long graph_key = 0;
+
+  RayQ R(int i) { return RayQ{rq[i][0].p, rq[i][1].p, rq[i][2].p}; }
+  RayQ S() { return RayQ{sq[0].p, sq[1].p, sq[2].p}; }
+  uint32_t* ticket(uint32_t bounce_slot, int k) { return tickets.p + 4 * bounce_slot + k; }
+  void drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+  }
+};
+
 }  // namespace pk
 
 struct pk_ctx {
@@ -32,44 +68,50 @@ struct pk_ctx {
   using EventPair = pk::EventPair;
   int device = 0;
   int sms = 0;
-  cudaStream_t stream = nullptr;
-  // Second stream of pk_render_frame's graph: each bounce's shadow traversal
-  // runs on it beside the next bounce's closest-hit traversal.
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_shaded = nullptr, ev_shadow = nullptr;
-  bool overlap = true;
+  cudaStream_t stream = nullptr;  // the API stream: uploads, passes, readbacks, serial frames
+  cudaStream_t copy = nullptr;    // pk_read_display_async
+  cudaEvent_t ev_api = nullptr, ev_tail = nullptr, ev_read = nullptr;
+  bool overlap = true;            // shadow traversal beside the next closest-hit traversal
+  int in_flight = 2;              // frames of pk_render_frame in flight (1 or 2)
+  int next_slot = 0, last_slot = 0;
+  bool tail_pending = false;      // ev_tail: accumulate/postprocess of the last pipelined frame
+  bool read_pending = false;      // ev_read: the last asynchronous display read
   std::string err;
   // configuration
   uint32_t W = 0, H = 0, B = 0, cap = 0, npix = 0;
   uint32_t ct = 0, st = 0;  // look-back tiles per compaction / shade launch
   unsigned g_trace = 1, g_compact = 1, g_shade = 1, g_trace_wide = 1;  // persistent grid sizes
   int trace_mode = pk::TRACE_PERSISTENT;
-  // CUDA graph of one pk_render_frame (replayed per frame); rebuilt when any
-  // pointer or launch parameter captured in it changes.
-  cudaGraphExec_t frame_graph = nullptr;
-  uint32_t graph_bounces = 0;
-  bool graph_counting = false;
-  unsigned long long graph_key = 0, state_version = 1;
+  unsigned long long state_version = 1;
+  pk::FrameSlot slot[2];
   void invalidate_graph() {
-    if (frame_graph) cudaGraphExecDestroy(frame_graph);
-    frame_graph = nullptr;
+    slot[0].drop_graph();
+    slot[1].drop_graph();
     state_version++;
   }
-  // render state
-  DevBuf<Counters> ctr;
-  DevBuf<CamState> cam;
+  // render state for the next frame (pk_set_render_state / pk_set_camera);
+  // each frame receives it by value, pk_render_frame advances samples.
+  int32_t samples_next = 0;
+  float theta_next = 0.0f;
+  CamState cam_host{};
+  bool state_dirty = false;  // slot 0's device copy is stale
+  DevBuf<Counters>& ctr = slot[0].ctr;
+  DevBuf<CamState>& cam = slot[0].cam;
   bool cam_set = false;
   float exposure = 1.0f, saturation = 1.0f;
-  DevBuf<float4> color, accum, display;
+  DevBuf<float4>& color = slot[0].color;
+  DevBuf<float4> accum, display;
   DevBuf<float4> accum_sum, accum_comp;  // compensated accumulation buffers
   bool kahan = false;
   DevBuf<uchar4> display8;
-  DevBuf<float4> rq[2][3], sq[3], mq[3];
-  int cur = 0;
-  DevBuf<uint4> hrec;
-  DevBuf<uint32_t> hflags, sflags, hit_list;
-  DevBuf<uint32_t> tickets;              // 4 per bounce slot
-  DevBuf<unsigned long long> tiles;      // per bounce slot: ct (compact) + st (shade) + ct (shadow compact)
+  DevBuf<float4> mq[3];
+  int& cur = slot[0].cur;
+  DevBuf<uint4>& hrec = slot[0].hrec;
+  DevBuf<uint32_t>& hflags = slot[0].hflags;
+  DevBuf<uint32_t>& sflags = slot[0].sflags;
+  DevBuf<uint32_t>& hit_list = slot[0].hit_list;
+  DevBuf<uint32_t>& tickets = slot[0].tickets;
+  DevBuf<unsigned long long>& tiles = slot[0].tiles;
   // scene
   uint32_t n_verts = 0, n_tris = 0;
   DevBuf<double> pos;
@@ -112,25 +154,26 @@ struct pk_ctx {
   unsigned long long frames = 0;
   unsigned long long diff_rays = 0;  // rays of the last differentiable render / adjoint
 
-  RayQ R(int i) { return RayQ{rq[i][0].p, rq[i][1].p, rq[i][2].p}; }
-  RayQ S() { return RayQ{sq[0].p, sq[1].p, sq[2].p}; }
+  RayQ R(int i) { return slot[0].R(i); }
+  RayQ S() { return slot[0].S(); }
   RayQ M() { return RayQ{mq[0].p, mq[1].p, mq[2].p}; }
-  uint32_t* ticket(uint32_t slot, int k) { return tickets.p + 4 * slot + k; }
-  unsigned long long* tiles_compact(uint32_t slot) { return tiles.p + (size_t)slot * (2 * ct + st); }
-  unsigned long long* tiles_shade(uint32_t slot) { return tiles_compact(slot) + ct; }
-  unsigned long long* tiles_shadow(uint32_t slot) { return tiles_compact(slot) + ct + st; }
+  uint32_t* ticket(uint32_t b, int k) { return slot[0].ticket(b, k); }
+  unsigned long long* tiles_compact(uint32_t b, int k = 0) { return slot[k].tiles.p + (size_t)b * (2 * ct + st); }
+  unsigned long long* tiles_shade(uint32_t b, int k = 0) { return tiles_compact(b, k) + ct; }
+  unsigned long long* tiles_shadow(uint32_t b, int k = 0) { return tiles_compact(b, k) + ct + st; }
 
-  LaunchCtx launch() {
+  // Launch parameters for frame slot k on stream s (default: slot 0 on the API stream).
+  LaunchCtx launch(int k = 0, cudaStream_t s = nullptr) {
     LaunchCtx L;
-    L.stream = stream;
-    L.ctr = ctr.p;
-    L.cam = cam.p;
+    L.stream = s ? s : stream;
+    L.ctr = slot[k].ctr.p;
+    L.cam = slot[k].cam.p;
     const bool ex = (trace_mode & pk::TRACE_EXACT) && exact_ready;
     L.scene = pk::SceneDev{ex ? exact.p : inner.p, (compact_nodes && !ex) ? inner32.p : nullptr, tris.p, tri4_leaf.p,
                            attrs.p, mat4.p, layers.p, (int)n_layers, (int)atlas_res, ex ? exact_root : root,
                        n_leaf_tris, n_verts, n_mats, wide_ready ? wide.p : nullptr};
     L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
-    L.color = color.p;
+    L.color = slot[k].color.p;
     L.accum = accum.p;
     L.display = display.p;
     L.display8 = display8.p;

@@ -1001,6 +1001,12 @@ __global__ void __launch_bounds__(256) k_postprocess(const float4* __restrict__ 
 }
 
 __global__ void k_end_frame(Counters* ctr) { ctr->samples += 1; }
+// The render state a frame starts from (RenderState + CameraPass uniforms).
+__global__ void k_set_state(Counters* ctr, CamState* cam, int32_t samples, float theta, CamState cs, int with_cam) {
+  ctr->samples = samples;
+  ctr->env_theta = theta;
+  if (with_cam) *cam = cs;
+}
 
 // Elementwise math probes (same numbering as the oracle's or_math).
 __global__ void k_math(int fn, const float* __restrict__ x, const float* __restrict__ y, float* __restrict__ out,
@@ -1357,6 +1363,10 @@ void launch_postprocess(const LaunchCtx& L, float exposure, float saturation) {
 }
 
 void launch_end_frame(const LaunchCtx& L) { k_end_frame<<<1, 1, 0, L.stream>>>(L.ctr); }
+void launch_set_state(cudaStream_t s, Counters* ctr, CamState* cam, int32_t samples, float theta, const CamState& cs,
+                      bool with_cam) {
+  k_set_state<<<1, 1, 0, s>>>(ctr, cam, samples, theta, cs, with_cam ? 1 : 0);
+}
 
 void launch_math(cudaStream_t s, int fn, const float* x, const float* y, float* out, uint32_t n) {
   if (n == 0) return;

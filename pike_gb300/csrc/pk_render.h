@@ -57,6 +57,9 @@ void launch_shade_miss(const LaunchCtx& L, RayQ M);
 void launch_accumulate(const LaunchCtx& L);
 void launch_postprocess(const LaunchCtx& L, float exposure, float saturation);
 void launch_end_frame(const LaunchCtx& L);
+// Sets a frame's sample index, environment rotation and (with_cam) camera.
+void launch_set_state(cudaStream_t s, Counters* ctr, CamState* cam, int32_t samples, float theta, const CamState& cs,
+                      bool with_cam);
 void launch_math(cudaStream_t s, int fn, const float* x, const float* y, float* out, uint32_t n);
 
 // pk_scene.cu

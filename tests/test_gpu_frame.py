@@ -1,13 +1,15 @@
 """Whole-frame parity: pk_render_frame (misses shaded inside the traversal
 kernels) against the oracle's tick(), and against the GPU's own pass-by-pass
 path; plus size-independent properties at the benchmark's full size."""
+import ctypes
+
 import numpy as np
 import pytest
 
 from pike_gb300 import _lib, synth
 from pike_gb300._lib import ptr
 
-from helpers import Pair, assert_bits_equal
+from helpers import Pair, assert_bits_equal, camera_struct
 
 pytestmark = pytest.mark.gpu
 
@@ -175,3 +177,83 @@ def test_frame_overlap_is_bit_identical(oracle, pk_built, mode, bounces):
     if mode == _lib.PK_TRACE_PERSISTENT:
         oracle_frames(pair, 2, bounces)
         assert_bits_equal(on, pair.P.r.accum(), "overlapped frame vs oracle")
+
+
+def _orbit(src, f: int) -> dict:
+    st = dict(src.camera_state())
+    a = 0.05 * f
+    x, z = st["dir"][0], st["dir"][2]
+    st["dir"] = [x * np.cos(a) - z * np.sin(a), st["dir"][1], x * np.sin(a) + z * np.cos(a)]
+    return st
+
+
+def _stepped_frames(pair: Pair, src, frames: int, bounces: int):
+    """A render loop as an application writes it: per frame the render state,
+    a moving camera, pk_render_frame and an asynchronous display read into its
+    own pinned buffer (all enqueued before one pk_sync)."""
+    c = pair.ctx
+    bufs = [c.pinned((src.height, src.width, 4), "uint8") for _ in range(frames)]
+    for f in range(frames):
+        c.call("pk_set_render_state", f, 0.01 * f)
+        c.call("pk_set_camera", camera_struct(_orbit(src, f)))
+        c.call("pk_render_frame", bounces)
+        c.call("pk_read_display_async", bufs[f].array.ctypes.data_as(ctypes.c_void_p))
+    c.call("pk_sync")
+    out = [b.array.copy() for b in bufs]
+    for b in bufs:
+        b.free()
+    return out
+
+
+def test_frames_in_flight_bit_identical(oracle, pk_built):
+    """Two frames in flight (the default) against one at a time: the same
+    display after every frame, accumulation, colour of the last frame, counters
+    and ray totals; the pass API afterwards starts from the host's render state."""
+    src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
+    runs = {}
+    for n in (2, 1):
+        pair = Pair(src, oracle)
+        pair.ctx.call("pk_set_frames_in_flight", n)
+        pair.ctx.call("pk_reset_stats")
+        disp = _stepped_frames(pair, src, 5, 6)
+        s = np.zeros(10, np.uint64)
+        pair.ctx.call("pk_read_stats", ptr(s))
+        runs[n] = (disp, pair.image("accum").copy(), pair.image("color").copy(), pair.counters(), s.copy())
+        c = pair.counters()
+        assert c["samples"] == 5 and c["err"] == 0
+    (d2, a2, c2, k2, s2), (d1, a1, c1, k1, s1) = runs[2], runs[1]
+    for f in range(5):
+        assert np.array_equal(d2[f], d1[f]), f"display after frame {f}"
+    assert len({d.tobytes() for d in d1}) == 5  # the camera moved: every frame differs
+    assert_bits_equal(a2, a1, "accumulation")
+    assert_bits_equal(c2, c1, "colour of the last frame")
+    assert k2 == k1 and np.array_equal(s2, s1)
+    # the oracle renders the same stepped sequence
+    P = pair.P.r
+    P.set_render_state(0)
+    for f in range(5):
+        pair.set_camera(_orbit(src, f))
+        P.set_render_state(f, 0.01 * f)
+        P.tick(6)
+    assert_bits_equal(a1, P.accum(), "stepped frames vs oracle")
+
+
+def test_passes_after_frames_in_flight(oracle, pk_built):
+    """Frames in flight, then pass-by-pass frames on the same context: the
+    passes see the render state advanced by the frames and the accumulated
+    image equals an all-frames render."""
+    src = synth.displaced_sphere_scene(subdivisions=5, width=96, height=64, env_size=(256, 128))
+    ref = Pair(src, oracle)
+    fused_frames(ref, 4, 6)
+    want = ref.image("accum").copy()
+    a = Pair(src, oracle)
+    fused_frames(a, 3, 6)  # frames 0..2 in flight; frame 3 by passes, no render state set in between
+    c = a.ctx
+    for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera"):
+        c.call("pk_" + name)
+    for _ in range(6):
+        for name in ("trace", "shade_hit", "trace_shadow", "shade_miss"):
+            c.call("pk_" + name)
+    c.call("pk_accumulate")
+    assert a.counters()["samples"] == 3  # passes do not advance the sample index
+    assert_bits_equal(a.image("accum"), want, "passes after frames in flight")
