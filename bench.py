@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
     ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
-    ap.add_argument("--frames-in-flight", type=int, default=2, choices=[1, 2],
+    ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
     ap.add_argument("--no-overlap", action="store_true",
                     help="serial frames: no shadow traversal beside the next bounce's closest-hit traversal")
@@ -339,10 +339,10 @@ def hit_agreement(ctx, mode_a: int, mode_b: int, bounces: int = 2):
 
 
 def warm_graphs(ctx, first_sample: int, B: int):
-    """Replays both frame slots once (a counting or timing frame re-captures a
+    """Replays every frame slot once (a counting or timing frame re-captures a
     slot's graph), so no capture falls inside a timed region."""
     ctx.call("pk_set_render_state", first_sample, 0.0)
-    ctx.call("pk_render_frames", 2, B)
+    ctx.call("pk_render_frames", 4, B)
     ctx.call("pk_sync")
 
 
@@ -550,7 +550,7 @@ def batch_form(args, local: int):
         ctx.call("pk_configure", r.width, r.height, r.width * r.height)
         ctx.call("pk_set_camera", _camera_struct(r.camera))
         ctx.call("pk_set_render_state", 0, 0.0)
-        ctx.call("pk_render_frames", 2, r.depth)  # warm-up (graph capture of both slots at this size)
+        ctx.call("pk_render_frames", 4, r.depth)  # warm-up (graph capture of every slot at this size)
         ctx.call("pk_set_render_state", 0, 0.0)
         ctx.call("pk_sync")
         ctx.timer_start()
@@ -588,7 +588,7 @@ def binned_form(ctx, args, B: int, first_sample: int, sweep_ms: float):
         times.append(ctx.timer_stop())
     ctx.call("pk_set_trace_mode", _lib.PK_TRACE_PERSISTENT)
     ctx.call("pk_set_render_state", first_sample, 0.0)
-    ctx.call("pk_render_frames", 2, B)
+    ctx.call("pk_render_frames", 4, B)
     ctx.call("pk_reset_stats")
     ctx.call("pk_set_render_state", first_sample, 0.0)
     ctx.call("pk_sync")

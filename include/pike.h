@@ -259,10 +259,11 @@ int pk_set_accumulation(pk_ctx* ctx, int mode);
  * receive their contributions in the same order).  Applies to the persistent
  * and 8-wide traversal modes without per-kernel timing. */
 int pk_set_frame_overlap(pk_ctx* ctx, int overlap);
-/* Frames of pk_render_frame in flight: 2 (the default) renders consecutive
- * frames on two sets of queues and streams so one frame's kernels fill the
- * idle time of the other's; accumulation and postprocessing stay in frame
- * order and images are bit-identical to 1 (one frame at a time).  Every
+/* Frames of pk_render_frame in flight, 1 to 4 (the default): with 2 or more,
+ * consecutive frames render on separate sets of queues and streams so one
+ * frame's kernels fill the idle time of another's; accumulation and
+ * postprocessing stay in frame order and images are bit-identical to 1 (one
+ * frame at a time).  Every
  * other call (passes, uploads, reads, pk_sync) first waits for the frames in
  * flight; pk_set_render_state, pk_set_camera and pk_read_display_async do not.
  * pk_read_color returns the colour buffer of the last frame rendered. */

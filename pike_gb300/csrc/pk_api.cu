@@ -233,7 +233,7 @@ int pk_configure(pk_ctx* c, uint32_t width, uint32_t height, uint32_t batch) {
     kernel_grids(c->sms, c->cap, &c->g_trace, &c->g_compact, &c->g_shade, &c->g_trace_wide);
     for (int i = 0; i < 3; i++) c->mq[i].alloc(2 * (size_t)c->cap);
     alloc_slot(c, 0);
-    release_slot(c->slot[1]);  // sized again on first use
+    for (int k = 1; k < MAX_IN_FLIGHT; k++) release_slot(c->slot[k]);  // sized again on first use
     c->next_slot = c->last_slot = 0;
     c->accum.alloc(c->npix);
     c->display.alloc(c->npix);
@@ -840,15 +840,15 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
 }
 
 // pk_render_frame.  A frame's launches are captured once per slot into a CUDA
-// graph and replayed (the sequence only reads device-side counts).  With two
-// frames in flight, frames alternate between the slots' streams: each waits
+// graph and replayed (the sequence only reads device-side counts).  With
+// several frames in flight, frames take the slots in turn, each on its stream: each waits
 // for the API stream, takes the render state by value, replays its graph,
 // then accumulates and postprocesses after the previous frame did (the
 // accumulation and display buffers are shared) and after the last
 // asynchronous display read.  With per-kernel timing the launches are issued
 // directly on the API stream.
 static void render_frame(pk_ctx* c, uint32_t bounces) {
-  const bool piped = c->in_flight == 2 && !c->timing;
+  const bool piped = c->in_flight > 1 && !c->timing;
   const int k = piped ? c->next_slot : 0;
   FrameSlot& fs = c->slot[k];
   if (fs.cap != c->cap) alloc_slot(c, k);
@@ -902,7 +902,7 @@ static void render_frame(pk_ctx* c, uint32_t bounces) {
     check(cudaEventRecord(fs.ev_done, st), "cudaEventRecord");
     c->tail_pending = true;
     fs.busy = true;
-    c->next_slot ^= 1;
+    c->next_slot = (c->next_slot + 1) % c->in_flight;
   }
   c->last_slot = k;
   c->samples_next++;
@@ -955,10 +955,10 @@ int pk_read_counters(pk_ctx* c, uint32_t out8[8]) {
     Counters h;
     check(cudaStreamSynchronize(c->stream), "sync");
     check(cudaMemcpy(&h, c->slot[c->last_slot].ctr.p, sizeof(h), cudaMemcpyDeviceToHost), "D2H");
-    const int other = c->last_slot ^ 1;
-    if (c->slot[other].ctr.p) {
+    for (int k = 0; k < MAX_IN_FLIGHT; k++) {
+      if (k == c->last_slot || !c->slot[k].ctr.p) continue;
       Counters o;
-      check(cudaMemcpy(&o, c->slot[other].ctr.p, sizeof(o), cudaMemcpyDeviceToHost), "D2H");
+      check(cudaMemcpy(&o, c->slot[k].ctr.p, sizeof(o), cudaMemcpyDeviceToHost), "D2H");
       h.rays_traced += o.rays_traced;
       h.err |= o.err;
     }
@@ -1131,7 +1131,7 @@ int pk_set_frame_overlap(pk_ctx* c, int on) {
 
 int pk_set_frames_in_flight(pk_ctx* c, int n) {
   return guarded(c, [&]() {
-    if (n != 1 && n != 2) return fail(c, PK_ERR_ARG, "frames in flight must be 1 or 2");
+    if (n < 1 || n > MAX_IN_FLIGHT) return fail(c, PK_ERR_ARG, "frames in flight must be 1 to 4");
     c->in_flight = n;
     c->next_slot = 0;
     c->invalidate_graph();

@@ -12,6 +12,7 @@
 namespace pk {
 
 constexpr uint32_t MAX_BOUNCES = 16;
+constexpr int MAX_IN_FLIGHT = 4;  // frame slots
 constexpr int N_KINDS = 8;
 enum Kind { K_CAMERA = 0, K_TRACE, K_COMPACT, K_SHADE, K_SHADOW, K_ACCUM, K_POST, K_OTHER };
 
@@ -20,8 +21,8 @@ struct EventPair {
   cudaEvent_t a, b;
 };
 
-// The transient state of one frame of pk_render_frame.  Two slots let two
-// frames be in flight: each renders on its own stream (plus a side stream for
+// The transient state of one frame of pk_render_frame.  Several slots let
+// several frames be in flight: each renders on its own stream (plus a side stream for
 // its shadow traversals) from its own counters, camera, colour buffer and
 // queues; the scene, BVH, environment, accumulation and display buffers are
 // shared.  Slot 0 is also the state of the pass-by-pass API.
@@ -72,7 +73,7 @@ struct pk_ctx {
   cudaStream_t copy = nullptr;    // pk_read_display_async
   cudaEvent_t ev_api = nullptr, ev_tail = nullptr, ev_read = nullptr;
   bool overlap = true;            // shadow traversal beside the next closest-hit traversal
-  int in_flight = 2;              // frames of pk_render_frame in flight (1 or 2)
+  int in_flight = pk::MAX_IN_FLIGHT;  // frames of pk_render_frame in flight (1..MAX_IN_FLIGHT)
   int next_slot = 0, last_slot = 0;
   bool tail_pending = false;      // ev_tail: accumulate/postprocess of the last pipelined frame
   bool read_pending = false;      // ev_read: the last asynchronous display read
@@ -83,10 +84,9 @@ struct pk_ctx {
   unsigned g_trace = 1, g_compact = 1, g_shade = 1, g_trace_wide = 1;  // persistent grid sizes
   int trace_mode = pk::TRACE_PERSISTENT;
   unsigned long long state_version = 1;
-  pk::FrameSlot slot[2];
+  pk::FrameSlot slot[pk::MAX_IN_FLIGHT];
   void invalidate_graph() {
-    slot[0].drop_graph();
-    slot[1].drop_graph();
+    for (pk::FrameSlot& s : slot) s.drop_graph();
     state_version++;
   }
   // render state for the next frame (pk_set_render_state / pk_set_camera);

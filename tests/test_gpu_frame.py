@@ -206,12 +206,12 @@ def _stepped_frames(pair: Pair, src, frames: int, bounces: int):
 
 
 def test_frames_in_flight_bit_identical(oracle, pk_built):
-    """Two frames in flight (the default) against one at a time: the same
+    """Four (the default) and two frames in flight against one at a time: the same
     display after every frame, accumulation, colour of the last frame, counters
     and ray totals; the pass API afterwards starts from the host's render state."""
     src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
     runs = {}
-    for n in (2, 1):
+    for n in (4, 2, 1):
         pair = Pair(src, oracle)
         pair.ctx.call("pk_set_frames_in_flight", n)
         pair.ctx.call("pk_reset_stats")
@@ -221,13 +221,15 @@ def test_frames_in_flight_bit_identical(oracle, pk_built):
         runs[n] = (disp, pair.image("accum").copy(), pair.image("color").copy(), pair.counters(), s.copy())
         c = pair.counters()
         assert c["samples"] == 5 and c["err"] == 0
-    (d2, a2, c2, k2, s2), (d1, a1, c1, k1, s1) = runs[2], runs[1]
-    for f in range(5):
-        assert np.array_equal(d2[f], d1[f]), f"display after frame {f}"
+    d1, a1, c1, k1, s1 = runs[1]
     assert len({d.tobytes() for d in d1}) == 5  # the camera moved: every frame differs
-    assert_bits_equal(a2, a1, "accumulation")
-    assert_bits_equal(c2, c1, "colour of the last frame")
-    assert k2 == k1 and np.array_equal(s2, s1)
+    for n in (4, 2):
+        dn, an, cn, kn, sn = runs[n]
+        for f in range(5):
+            assert np.array_equal(dn[f], d1[f]), f"{n} in flight: display after frame {f}"
+        assert_bits_equal(an, a1, f"{n} in flight: accumulation")
+        assert_bits_equal(cn, c1, f"{n} in flight: colour of the last frame")
+        assert kn == k1 and np.array_equal(sn, s1)
     # the oracle renders the same stepped sequence
     P = pair.P.r
     P.set_render_state(0)
@@ -257,3 +259,4 @@ def test_passes_after_frames_in_flight(oracle, pk_built):
     c.call("pk_accumulate")
     assert a.counters()["samples"] == 3  # passes do not advance the sample index
     assert_bits_equal(a.image("accum"), want, "passes after frames in flight")
+
