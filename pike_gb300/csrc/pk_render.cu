@@ -1059,12 +1059,13 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 
 // Out-of-line calls for the batch megakernel: inlining both traversals, the
 // whole shade_hit body and the camera into one loop overflows the instruction
-// cache (ncu: most warps stalled waiting for instructions).
-template <bool ANY, int BLOCK, int SSTACK>
-__device__ __noinline__ void batch_trace(const SceneDev& sc, float4 o, float4 d, float& t, int& idx, uint32_t& bary,
-                                         int (*sstack)[BLOCK], uint32_t* err) {
+// cache (ncu: most warps stalled waiting for instructions).  One traversal
+// copy serves closest and shadow rays.
+template <int BLOCK, int SSTACK>
+__device__ __noinline__ void batch_trace(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
+                                         uint32_t& bary, int (*sstack)[BLOCK], uint32_t* err) {
   uint32_t nf = 0, nt = 0;
-  traverse<ANY, false, BLOCK, SSTACK>(sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf, nt);
+  traverse_rt<false, BLOCK, SSTACK>(any, sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf, nt);
 }
 __device__ __noinline__ bool batch_shade(const SceneDev& sc, const EnvDev& env, float theta, int32_t samples,
                                          uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr, V3& em, bool& eb,
@@ -1157,7 +1158,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
       float t;
       int idx;
       uint32_t bary;
-      batch_trace<false, BLOCK, SSTACK>(S.sc, o4, d4, t, idx, bary, sstack, err);
+      batch_trace<BLOCK, SSTACK>(false, S.sc, o4, d4, t, idx, bary, sstack, err);
       float cr = 0.0f, cg = 0.0f, cb = 0.0f;
       bool next = false;
       if (idx < 0) {
@@ -1176,7 +1177,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch(const BatchScene* __restrict__ 
           float ts;
           int is;
           uint32_t bs;
-          batch_trace<true, BLOCK, SSTACK>(S.sc, so, sd, ts, is, bs, sstack, err);
+          batch_trace<BLOCK, SSTACK>(true, S.sc, so, sd, ts, is, bs, sstack, err);
           if (is < 0) {
             const V3 e = env_color(S.env, S.theta, v3(sd.x, sd.y, sd.z));
             cr += e.x * st.x; cg += e.y * st.y; cb += e.z * st.z;

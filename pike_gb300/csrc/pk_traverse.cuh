@@ -71,12 +71,14 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
 }
 
 // BLOCK threads per block share `sstack` (SSTACK entries per thread in shared
-// memory, STACK_LOCAL more in local memory).
-template <bool ANY, bool COUNT, int BLOCK = TRACE_THREADS, int SSTACK = STACK_SMEM>
-__device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
-                                         float dz, float& best_t, int& best_i, uint32_t& best_b,
-                                         int (*sstack)[BLOCK], uint32_t* err, uint32_t& nfetch,
-                                         uint32_t& ntest) {
+// memory, STACK_LOCAL more in local memory).  ANY: any hit (trace_shadow.wgsl)
+// rather than closest hit; a constant at every inlined call site, a run-time
+// value where one out-of-line copy serves both.
+template <bool COUNT, int BLOCK, int SSTACK>
+__device__ __forceinline__ void traverse_rt(const bool ANY, const SceneDev& sc, float ox, float oy, float oz,
+                                            float dx, float dy, float dz, float& best_t, int& best_i,
+                                            uint32_t& best_b, int (*sstack)[BLOCK], uint32_t* err,
+                                            uint32_t& nfetch, uint32_t& ntest) {
   const float eps = ANY ? 1e-7f : 1e-8f;
   const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
   int lstack[STACK_LOCAL];
@@ -139,6 +141,14 @@ __device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy,
     --sp;
     cur = sp < SSTACK ? sstack[sp][tid] : lstack[sp - SSTACK];
   }
+}
+template <bool ANY, bool COUNT, int BLOCK = TRACE_THREADS, int SSTACK = STACK_SMEM>
+__device__ __forceinline__ void traverse(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy,
+                                         float dz, float& best_t, int& best_i, uint32_t& best_b,
+                                         int (*sstack)[BLOCK], uint32_t* err, uint32_t& nfetch,
+                                         uint32_t& ntest) {
+  traverse_rt<COUNT, BLOCK, SSTACK>(ANY, sc, ox, oy, oz, dx, dy, dz, best_t, best_i, best_b, sstack, err, nfetch,
+                                    ntest);
 }
 
 }  // namespace pk
