@@ -195,7 +195,9 @@ __device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y 
 __device__ __forceinline__ V3 cross(V3 a, V3 b) {
   return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-__device__ __forceinline__ V3 normalize(V3 a) {
+// Called, not inlined (an IEEE square root and three IEEE quotients at a
+// dozen shading sites), for the same instruction-cache reason as sin_.
+static __device__ __noinline__ V3 normalize(V3 a) {
   const float l = sqrtf(dot(a, a));
   return v3(a.x / l, a.y / l, a.z / l);
 }
