@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
     ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
+    ap.add_argument("--profile-case", choices=["wide", "adjoint", "batch"],
+                    help="run one small case of a form kernel (for ncu captures) and exit")
     ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
     ap.add_argument("--no-overlap", action="store_true",
@@ -344,6 +346,48 @@ def warm_graphs(ctx, first_sample: int, B: int):
     ctx.call("pk_set_render_state", first_sample, 0.0)
     ctx.call("pk_render_frames", 4, B)
     ctx.call("pk_sync")
+
+
+def profile_case(name: str, local: int = 0):
+    """One small invocation of a form kernel, for ncu captures (a few seconds,
+    well under a GB on the device): `wide` = icosphere7 + box (327,690
+    triangles) at 480x270, 8 bounces, 8-wide traversal; `adjoint` = icosphere6
+    + box at 256x256, 4 spp, depth 4, one render and one adjoint; `batch` = 16
+    requests over 2 scenes (9,998 / 327,690 triangles), half the batching
+    workload's resolutions, <= 4 spp, block 128, stack 16, chunk 4, rendered
+    twice (the second launch is the one to capture)."""
+    from pike_gb300 import _lib, synth
+    if name == "wide":
+        src = synth.displaced_sphere_scene(subdivisions=7, width=480, height=270)
+        ctx, _ = setup_context(src, local)
+        ctx.call("pk_set_trace_mode", _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE)
+        ctx.call("pk_set_camera", camera_struct(src))
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_render_frames", 1, 8)
+        ctx.call("pk_sync")
+    elif name == "adjoint":
+        import torch
+        from pike_gb300.diff import DiffScene
+        src = synth.displaced_sphere_scene(subdivisions=6, width=256, height=256, env_size=(64, 32))
+        scene = DiffScene(src, 256, 256, spp=4, depth=4, device=local)
+        albedo, rough, env = scene.source_params(env_size=(256, 128), sun=20.0)
+        img = scene.render(albedo, rough, env, seed=0)
+        scene.backward(albedo, rough, env, torch.ones_like(img), seed=0)
+        torch.cuda.synchronize()
+    else:
+        from pike_gb300.batch import Batch, random_requests, scene_context
+        srcs = [synth.small_scene(n_boxes=833), synth.displaced_sphere_scene(subdivisions=7, width=16, height=16)]
+        ctxs = [scene_context(x, local) for x in srcs]
+        reqs = random_requests(16, 2, seed=7)
+        for r in reqs:
+            r.width, r.height, r.spp = max(64, r.width // 2), max(64, r.height // 2), min(r.spp, 4)
+        b = Batch(ctxs)
+        b.set_requests(reqs)
+        b.set_config(128, 16, 4)
+        b.render(1)
+        b.reset()
+        b.render(1)
+    print(json.dumps({"profile_case": name, "ok": True}))
 
 
 def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
@@ -799,6 +843,9 @@ def gpu_arm(args):
 
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return 0
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)
