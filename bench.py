@@ -805,7 +805,9 @@ def gpu_arm(args):
         achieved = alg_bytes_launch / (trace_ms / 1000.0) / 1e9
         traffic = profiled_traffic()
         total_ms = sum(v["ms"] for v in kt.values())
-        launches_per_frame = 4 * B + 4
+        # k_set_state, k_camera, per bounce {closest trace, compaction, shade, shadow trace},
+        # k_accumulate, k_postprocess, k_end_frame
+        launches_per_frame = 4 * B + 5
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
