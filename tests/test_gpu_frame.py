@@ -260,3 +260,38 @@ def test_passes_after_frames_in_flight(oracle, pk_built):
     assert a.counters()["samples"] == 3  # passes do not advance the sample index
     assert_bits_equal(a.image("accum"), want, "passes after frames in flight")
 
+
+
+def test_frames_in_flight_across_reconfigure_env_and_switches(oracle, pk_built):
+    """Frames in flight, then a new resolution, a new environment and changes
+    of the number in flight between frames: every accumulation equals the one
+    of the same sequence rendered one frame at a time."""
+    src = synth.displaced_sphere_scene(subdivisions=5, width=128, height=96, env_size=(256, 128))
+    env2 = np.ascontiguousarray(np.roll(np.asarray(src.env_rgbe, np.uint8), 37, axis=1))
+    results = {}
+    for piped in (False, True):
+        pair = Pair(src, oracle)
+        c = pair.ctx
+        c.call("pk_set_frames_in_flight", 4 if piped else 1)
+        c.call("pk_set_render_state", 0, 0.0)
+        c.call("pk_render_frames", 3, 6)
+        first = pair.image("accum").copy()
+        c.call("pk_configure", 96, 64, 96 * 64)  # new queues and slot buffers while frames may be in flight
+        c.call("pk_set_camera", camera_struct(src.camera_state()))
+        if piped:
+            c.call("pk_set_frames_in_flight", 3)
+        c.call("pk_set_render_state", 0, 0.0)
+        c.call("pk_render_frames", 5, 6)
+        second = np.zeros((64, 96, 4), np.float32)
+        c.call("pk_read_accum", ptr(second))
+        c.call("pk_env_build", ptr(env2), env2.shape[1], env2.shape[0])
+        if piped:
+            c.call("pk_set_frames_in_flight", 2)
+        c.call("pk_render_frames", 3, 6)
+        third = np.zeros((64, 96, 4), np.float32)
+        c.call("pk_read_accum", ptr(third))
+        results[piped] = (first, second, third, pair.counters())
+    for k, name in enumerate(("before", "after reconfigure", "after a new environment")):
+        assert_bits_equal(results[True][k], results[False][k], name)
+    assert results[True][3]["samples"] == results[False][3]["samples"] == 8
+    assert results[True][3]["err"] == 0
