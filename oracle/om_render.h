@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "om_math.h"
+#include "om_render64.h"
 
 namespace om {
 
@@ -93,6 +94,27 @@ struct Renderer {
   CameraState cam{};
   float exposure = 1.0f, saturation = 1.0f;
   Stats trace_stats, shadow_stats;
+  // FP64 companion (om_render64.h): per-ray FP64 throughput of the ray,
+  // hit and miss buffers (3 doubles per slot), the frame's FP64 colour, its
+  // running mean (accumulate.wgsl in double) and Welford moments of the
+  // per-frame colour since set_track64.
+  bool track64 = false;
+  std::vector<double> ray64, hit64, miss64, color64, accum64, mean64, m2_64;
+  uint64_t frames64 = 0;
+  void alloc64() {
+    ray64.assign(3 * ray_buffer.size(), 0.0);
+    hit64.assign(3 * hit_buffer.size(), 0.0);
+    miss64.assign(3 * miss_buffer.size(), 0.0);
+    color64.assign(4 * (size_t)W * H, 0.0);
+    accum64.assign(4 * (size_t)W * H, 0.0);
+    mean64.assign(4 * (size_t)W * H, 0.0);
+    m2_64.assign(4 * (size_t)W * H, 0.0);
+    frames64 = 0;
+  }
+  void set_track64(bool on) {
+    track64 = on;
+    if (on) alloc64();
+  }
 
   void configure(uint32_t w, uint32_t h, uint32_t batch) {
     W = w; H = h; B = batch;
@@ -103,6 +125,7 @@ struct Renderer {
     ray_buffer.assign(3 * (size_t)B, DeferredRay{});
     miss_buffer.assign(2 * (size_t)B, DeferredRay{});
     hit_buffer.assign((size_t)B, Hit{});
+    if (track64) alloc64();
   }
   static uint32_t round_up(uint32_t n, uint32_t m) { return (n + m - 1) / m * m; }
 
@@ -158,7 +181,12 @@ struct Renderer {
     });
     for (uint32_t gid = 0; gid < n; gid++) {
       if (!valid[gid]) continue;
-      if (gid < ray_buffer.size()) ray_buffer[gid] = out[gid]; else overflow |= 1;
+      if (gid < ray_buffer.size()) {
+        ray_buffer[gid] = out[gid];
+        if (track64) ray64[3 * gid] = ray64[3 * gid + 1] = ray64[3 * gid + 2] = 1.0;
+      } else {
+        overflow |= 1;
+      }
       num_rays++;
     }
   }
@@ -281,9 +309,11 @@ struct Renderer {
       if (res[j].index != -1) {
         uint32_t k = num_hits++;
         if (k < hit_buffer.size()) hit_buffer[k] = Hit{res[j].t, res[j].index, res[j].bary, ray_buffer[j]}; else overflow |= 2;
+        if (track64 && k < hit_buffer.size()) copy64(&hit64[3 * (size_t)k], &ray64[3 * (size_t)j]);
       } else {
         uint32_t k = num_misses++;
         if (k < miss_buffer.size()) miss_buffer[k] = ray_buffer[j]; else overflow |= 4;
+        if (track64 && k < miss_buffer.size()) copy64(&miss64[3 * (size_t)k], &ray64[3 * (size_t)j]);
       }
     }
   }
@@ -307,6 +337,7 @@ struct Renderer {
       if (res[j].index == -1) {
         uint32_t k = num_misses++;
         if (k < miss_buffer.size()) miss_buffer[k] = ray_buffer[off + j]; else overflow |= 4;
+        if (track64 && k < miss_buffer.size()) copy64(&miss64[3 * (size_t)k], &ray64[3 * ((size_t)off + j)]);
       }
     }
   }
@@ -506,6 +537,7 @@ struct Renderer {
   }
   struct ShadeOut {
     bool bounce = false, shadow = false, emit = false;
+    bool passthru = false, diffuse = false;  // the branches taken (read by shade_one64)
     DeferredRay bounce_ray, shadow_ray;
     float add[4];
     uint32_t pixel = 0;
@@ -529,6 +561,7 @@ struct Renderer {
       DeferredRay r = hit.ray;
       r.o[0] = ao.x; r.o[1] = ao.y; r.o[2] = ao.z;
       out.bounce = true; out.bounce_ray = r;
+      out.passthru = true;
       return out;
     }
     if (dot(si.emission, v3(1.0f, 1.0f, 1.0f)) > 0.0f) {
@@ -548,6 +581,7 @@ struct Renderer {
     if (h.rand() > f) {
       bs = sample_lambert(h);
       bsdf = eval_lambert(si, bs);
+      out.diffuse = true;
     } else {
       bs = Sample{reflect(neg(si.wo), m), 0.0f};
       bs.pdf = specular_pdf(si, m);
@@ -583,22 +617,189 @@ struct Renderer {
     num_rays = 0; num_shadow = 0;   // ShadeHitPass.generateCommands: clearNumRays
     const uint32_t n = num_hits;
     std::vector<ShadeOut> res(n);
+    std::vector<Shade64> r64(track64 ? n : 0);
     parallel_for(n, nthreads, [&](size_t b, size_t e, int) {
-      for (size_t j = b; j < e; j++) res[j] = shade_one((uint32_t)j);
+      for (size_t j = b; j < e; j++) {
+        res[j] = shade_one((uint32_t)j);
+        if (track64) r64[j] = shade_one64((uint32_t)j, res[j]);
+      }
     });
     const uint32_t off = shadow_offset();
     for (uint32_t j = 0; j < n; j++) {
       const ShadeOut& o = res[j];
-      if (o.emit) add_color(o.pixel, o.add);
+      if (o.emit) {
+        add_color(o.pixel, o.add);
+        if (track64) add_color64(o.pixel, r64[j].add);
+      }
       if (o.bounce) {
         uint32_t k = num_rays++;
         if (k < ray_buffer.size()) ray_buffer[k] = o.bounce_ray; else overflow |= 1;
+        if (track64 && k < ray_buffer.size()) copy64(&ray64[3 * (size_t)k], r64[j].bounce);
       }
       if (o.shadow) {
         uint32_t k = num_shadow++ + off;
         if (k < ray_buffer.size()) ray_buffer[k] = o.shadow_ray; else overflow |= 1;
+        if (track64 && k < ray_buffer.size()) copy64(&ray64[3 * (size_t)k], r64[j].shadow);
       }
     }
+  }
+
+  // ---------------- FP64 companion (om_render64.h) ----------------
+  static void copy64(double* d, const double* s) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
+  void add_color64(uint32_t idx, const double* c) {
+    if ((size_t)idx >= (size_t)W * H) return;
+    double* p = &color64[4 * (size_t)idx];
+    p[0] += c[0]; p[1] += c[1]; p[2] += c[2]; p[3] += 1.0;
+  }
+  void texel64(int32_t layer, double u, double v, double* c) const {
+    const int32_t R = atlas_res;
+    const int32_t nl = (int32_t)(layers.size() / (4 * (size_t)R * R));
+    const int32_t l = layer < 0 ? 0 : (layer >= nl ? nl - 1 : layer);
+    auto at = [&](int32_t i, int32_t j, double* t) {
+      i = ((i % R) + R) % R;
+      j = ((j % R) + R) % R;
+      const uint8_t* p = &layers[4 * (((size_t)l * R + (size_t)j) * R + (size_t)i)];
+      for (int k = 0; k < 4; k++) t[k] = (double)p[k] / 255.0;
+    };
+    if (R == 1) { at(0, 0, c); return; }
+    const double x = u * R - 0.5, y = v * R - 0.5;
+    const double x0 = std::floor(x), y0 = std::floor(y);
+    const double fx = x - x0, fy = y - y0;
+    const int32_t i0 = (int32_t)x0, j0 = (int32_t)y0;
+    double t00[4], t10[4], t01[4], t11[4];
+    at(i0, j0, t00);
+    at(i0 + 1, j0, t10);
+    at(i0, j0 + 1, t01);
+    at(i0 + 1, j0 + 1, t11);
+    for (int k = 0; k < 4; k++) c[k] = mixd(mixd(t00[k], t10[k], fx), mixd(t01[k], t11[k], fx), fy);
+  }
+  SI64 surface64(const Hit& hit) const {
+    SI64 si;
+    const D3 rd = d3f(hit.ray.d);
+    const int32_t* tri = &tri4[4 * (size_t)hit.index];
+    const double u = unorm16d(hit.bary, 0), v = unorm16d(hit.bary, 1);
+    const D3 bary = d3(1.0 - u - v, u, v);
+    D3 tg[3], bt[3], nm[3];
+    double uvx[3], uvy[3];
+    for (int k = 0; k < 3; k++) {
+      const uint32_t* a = &attrs4[4 * (size_t)tri[k]];
+      tg[k] = d3(snorm8d(a[0], 0), snorm8d(a[0], 1), snorm8d(a[0], 2));
+      bt[k] = d3(snorm8d(a[1], 0), snorm8d(a[1], 1), snorm8d(a[1], 2));
+      nm[k] = d3(snorm8d(a[2], 0), snorm8d(a[2], 1), snorm8d(a[2], 2));
+      uvx[k] = snorm16d(a[3], 0);
+      uvy[k] = snorm16d(a[3], 1);
+    }
+    const D3 T = normalize(matvec(tg[0], tg[1], tg[2], bary));
+    const D3 Bt = normalize(matvec(bt[0], bt[1], bt[2], bary));
+    const D3 N = normalize(matvec(nm[0], nm[1], nm[2], bary));
+    const double tu = uvx[0] * bary.x + uvx[1] * bary.y + uvx[2] * bary.z;
+    const double tv = uvy[0] * bary.x + uvy[1] * bary.y + uvy[2] * bary.z;
+    const int32_t* mat = &mat4[4 * (size_t)tri[3]];
+    double nrm[4], dif[4], mr[4], em[4];
+    texel64(mat[2], tu, tv, nrm);
+    const D3 map_normal = mul(sub(d3(nrm[0], nrm[1], nrm[2]), d3(0.5, 0.5, 0.0)), d3(2.0, 2.0, 1.0));
+    si.normal = normalize(matvec(T, Bt, N, map_normal));
+    si.n = si.normal;
+    onb64(si.normal, &si.b1, &si.b2);
+    si.wo = vecmat(neg(rd), si.b1, si.b2, si.n);
+    texel64(mat[0], tu, tv, dif);
+    si.base = d3(dif[0], dif[1], dif[2]);
+    si.opacity = dif[3];
+    texel64(mat[1], tu, tv, mr);
+    si.metallic = mr[2];
+    si.alpha = mr[1] * mr[1];
+    texel64(mat[3], tu, tv, em);
+    si.emission = d3(em[0], em[1], em[2]);
+    si.spec = d3(mixd(1.0, si.base.x, si.metallic), mixd(1.0, si.base.y, si.metallic), mixd(1.0, si.base.z, si.metallic));
+    return si;
+  }
+  double pdf_texel64(int32_t x, int32_t y) const {
+    if (x < 0 || y < 0 || x >= (int32_t)env_w || y >= (int32_t)env_h) return 0.0;
+    return (double)env_pdf[(size_t)x + (size_t)env_w * (size_t)y];
+  }
+  static double acos_clamped(double y) { return std::acos(y < -1.0 ? -1.0 : (y > 1.0 ? 1.0 : y)); }
+  double env_pdf_dir64(D3 dir) const {
+    const double a = 1.0 + (double)env_theta + std::atan2(dir.z, dir.x) / TAU_D;
+    const double u = a - std::trunc(a);
+    const double v = acos_clamped(dir.y) / PI_D;
+    const int32_t cx = (int32_t)(u * (double)env_w), cy = (int32_t)(v * (double)env_h);
+    return pdf_texel64(cx, cy) / std::sin(v * PI_D);
+  }
+  Sample64 sample_env64(Hash& h, const SI64& si) const {
+    const uint32_t nb = (uint32_t)(env_bins2.size() / 2);
+    const int32_t idx = (int32_t)(h.hash() % nb);
+    const int32_t h0 = env_bins2[2 * idx], h1 = env_bins2[2 * idx + 1];
+    const int32_t ci = (int32_t)(h.hash() % (uint32_t)(h1 - h0)) + h0;
+    const int32_t cx = env_coords2[2 * (size_t)ci], cy = env_coords2[2 * (size_t)ci + 1];
+    const double u = -(double)env_theta + (0.5 + cx) / (double)env_w;
+    const double v = (0.5 + cy) / (double)env_h;
+    const double theta = u * TAU_D, phi = v * PI_D, sp = std::sin(phi);
+    const D3 dir = d3(std::cos(theta) * sp, std::cos(phi), std::sin(theta) * sp);
+    return Sample64{vecmat(dir, si.b1, si.b2, si.n), pdf_texel64(cx, cy) / sp};
+  }
+  D3 env_color64(D3 dir) const {
+    const double u = (double)env_theta + std::atan2(dir.z, dir.x) / TAU_D;
+    const double v = acos_clamped(dir.y) / PI_D;
+    int32_t x = (int32_t)std::floor(u * (double)env_w), y = (int32_t)std::floor(v * (double)env_h);
+    x = ((x % (int32_t)env_w) + (int32_t)env_w) % (int32_t)env_w;
+    y = ((y % (int32_t)env_h) + (int32_t)env_h) % (int32_t)env_h;
+    const uint8_t* c = &env_rgbe[4 * ((size_t)y * env_w + (size_t)x)];
+    const double p = std::ldexp(1.0, (int)c[3] - 128);
+    return d3((double)c[0] / 255.0 * p, (double)c[1] / 255.0 * p, (double)c[2] / 255.0 * p);
+  }
+  struct Shade64 { double bounce[3] = {0, 0, 0}, shadow[3] = {0, 0, 0}, add[3] = {0, 0, 0}; };
+  // shade_hit.wgsl:407-483 in FP64 along the branches the FP32 shading took
+  Shade64 shade_one64(uint32_t tid, const ShadeOut& o) const {
+    Shade64 r;
+    const Hit& hit = hit_buffer[tid];
+    const double* ctp = &hit64[3 * (size_t)tid];
+    if (o.passthru) { copy64(r.bounce, ctp); return r; }
+    const uint32_t mask = f2u(hit.ray.tp[3]);
+    const uint32_t color_idx = mask & 0x0fffffffu;
+    if (!o.emit && (mask & 0xf0000000u) == 0x10000000u) return r;
+    Hash h;
+    h.seed = (tid * 1973u + color_idx * 9277u + (uint32_t)samples * 26699u) | 1u;
+    h.seed = h.hash();
+    (void)h.rand();  // opacity
+    const SI64 si = surface64(hit);
+    if (o.emit) {
+      const double att = fmaxd(dot(si.normal, matvec(si.b1, si.b2, si.n, si.wo)), 0.0);
+      r.add[0] = 50.0 * si.emission.x * ctp[0] * att;
+      r.add[1] = 50.0 * si.emission.y * ctp[1] * att;
+      r.add[2] = 50.0 * si.emission.z * ctp[2] * att;
+      return r;
+    }
+    const double g1 = (double)h.rand(), g2 = (double)h.rand();
+    const D3 m = sample_ggx64(si, g1, g2);
+    const double f = mixd(schlick64(fmaxd(dot(si.wo, m), 0.0), 1.5), 1.0, si.metallic);
+    (void)h.rand();  // lobe choice (o.diffuse)
+    Sample64 bs;
+    D3 bsdf;
+    if (o.diffuse) {
+      const double l1 = (double)h.rand(), l2 = (double)h.rand();
+      bs = sample_lambert64(l1, l2);
+      bsdf = eval_lambert64(si, bs);
+    } else {
+      bs.wi = reflect(neg(si.wo), m);
+      bs.pdf = specular_pdf64(si, m);
+      bsdf = eval_specular64(si, bs);
+    }
+    if (o.bounce) {
+      const double w = sample_env_light ? power_heuristic64(bs.pdf, env_pdf_dir64(matvec(si.b1, si.b2, si.n, bs.wi))) : 1.0;
+      r.bounce[0] = bsdf.x * ctp[0] * w;
+      r.bounce[1] = bsdf.y * ctp[1] * w;
+      r.bounce[2] = bsdf.z * ctp[2] * w;
+    }
+    if (sample_env_light) {
+      const Sample64 es = sample_env64(h, si);
+      if (o.shadow) {
+        const D3 sc = material_sample64(si, es, f);
+        r.shadow[0] = sc.x * ctp[0];
+        r.shadow[1] = sc.y * ctp[1];
+        r.shadow[2] = sc.z * ctp[2];
+      }
+    }
+    return r;
   }
 
   // ---------------- shade_miss.wgsl ----------------
@@ -627,6 +828,12 @@ struct Renderer {
       const DeferredRay& r = miss_buffer[j];
       float c[4] = {res[j].x * r.tp[0], res[j].y * r.tp[1], res[j].z * r.tp[2], 1.0f};
       add_color(f2u(r.tp[3]) & 0x0fffffffu, c);
+      if (track64) {
+        const D3 e = env_color64(d3f(r.d));
+        const double* t = &miss64[3 * (size_t)j];
+        const double c64[3] = {e.x * t[0], e.y * t[1], e.z * t[2]};
+        add_color64(f2u(r.tp[3]) & 0x0fffffffu, c64);
+      }
     }
   }
 
@@ -639,6 +846,19 @@ struct Renderer {
       const float* c = &color[4 * i];
       for (int k = 0; k < 3; k++) a[k] = (fmax_(c[k], 0.0f) + a[k] * s) / s1;
       a[3] = 1.0f;
+    }
+    if (track64) {
+      frames64++;
+      const double sd = (double)samples, sd1 = (double)samples + 1.0;
+      for (size_t i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) {
+          const size_t q = 4 * i + k;
+          const double x = fmaxd(color64[q], 0.0);
+          accum64[q] = (x + accum64[q] * sd) / sd1;
+          const double delta = x - mean64[q];
+          mean64[q] += delta / (double)frames64;
+          m2_64[q] += delta * (x - mean64[q]);
+        }
     }
   }
   static V3 rrt_odt_fit(V3 v) {
@@ -685,6 +905,7 @@ struct Renderer {
     // RenderState.generateCommands: clearColorBuffer + header upload {samples, theta, 0, 0, 0};
     // then tick() clears the colour buffer and, per batch, hits/misses and ray counts.
     std::fill(color.begin(), color.end(), 0.0f);
+    if (track64) std::fill(color64.begin(), color64.end(), 0.0);
     num_hits = num_misses = num_rays = 0;
     num_shadow = 0;
   }

@@ -297,6 +297,19 @@ void or_brute_rays(void* p, const float* rays8, size_t n, int any_hit, uint32_t*
 }
 void or_set_canonical(void* p, int on) { ((Renderer*)p)->canonical = on != 0; }
 
+// FP64 companion (om_render64.h): which = 0 the FP64 accumulation
+// (accumulate.wgsl in double), 1 the mean and 2 the sum of squared deviations
+// of the per-frame FP64 colours since or_set_track64; W*H*4 doubles.
+void or_set_track64(void* p, int on) { ((Renderer*)p)->set_track64(on != 0); }
+uint64_t or_frames64(void* p) { return ((Renderer*)p)->frames64; }
+int or_read64(void* p, int which, double* out) {
+  Renderer* r = (Renderer*)p;
+  const std::vector<double>* v = which == 0 ? &r->accum64 : which == 1 ? &r->mean64 : which == 2 ? &r->m2_64 : nullptr;
+  if (!v || !r->track64) return 1;
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+  return 0;
+}
+
 // Differentiable path tracer (pk_diff.cu) in binary64: image and gradient.
 static DiffScene diff_scene(void* p, const float* cam12, const double* albedo, const double* rough,
                             const double* metal, uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h,

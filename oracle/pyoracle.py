@@ -46,6 +46,10 @@ def lib():
             getattr(_lib, name).argtypes = [C.c_void_p]
         _lib.or_tick.argtypes = [C.c_void_p, C.c_uint32]
         _lib.or_set_threads.argtypes = [C.c_void_p, C.c_int]
+        _lib.or_set_track64.argtypes = [C.c_void_p, C.c_int]
+        _lib.or_frames64.argtypes = [C.c_void_p]
+        _lib.or_frames64.restype = C.c_uint64
+        _lib.or_read64.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     return _lib
 
 
@@ -291,6 +295,29 @@ class Renderer:
         lib().or_diff_grad(*self._diff_args(cam12, albedo, rough, metal, env, spp, depth, seed, W, H), _p(d), _p(ga),
                            _p(gr), _p(ge))
         return ga, gr, ge
+
+    def set_track64(self, on: bool = True):
+        """FP64 companion: every ray also carries an FP64 throughput and every
+        contribution is recomputed in FP64 along the same paths (om_render64.h)."""
+        lib().or_set_track64(self.p, C.c_int(1 if on else 0))
+
+    def _read64(self, which: int) -> np.ndarray:
+        out = np.zeros((self.h, self.w, 4), np.float64)
+        if lib().or_read64(self.p, C.c_int(which), _p(out)):
+            raise RuntimeError("FP64 companion is off")
+        return out
+
+    def accum64(self) -> np.ndarray:
+        """accumulate.wgsl's running mean of the FP64 per-frame colours."""
+        return self._read64(0)
+
+    def std64(self) -> np.ndarray:
+        """Per-pixel sample standard deviation of the FP64 per-frame colours."""
+        n = int(lib().or_frames64(self.p))
+        return np.sqrt(self._read64(2) / max(n - 1, 1))
+
+    def frames64(self) -> int:
+        return int(lib().or_frames64(self.p))
 
     def set_canonical(self, on: bool = True):
         """Trace by testing every triangle (min (t, slot)): the 8-wide traversal's answer."""
