@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
     ap.add_argument("--profile-case", choices=["wide", "adjoint", "batch"],
                     help="run one small case of a form kernel (for ncu captures) and exit")
-    ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4],
+    ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4, 5, 6, 7, 8],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
     ap.add_argument("--no-overlap", action="store_true",
                     help="serial frames: no shadow traversal beside the next bounce's closest-hit traversal")

@@ -12,7 +12,7 @@
 namespace pk {
 
 constexpr uint32_t MAX_BOUNCES = 16;
-constexpr int MAX_IN_FLIGHT = 4;  // frame slots
+constexpr int MAX_IN_FLIGHT = 8;  // frame slots
 constexpr int N_KINDS = 8;
 enum Kind { K_CAMERA = 0, K_TRACE, K_COMPACT, K_SHADE, K_SHADOW, K_ACCUM, K_POST, K_OTHER };
 
@@ -73,7 +73,7 @@ struct pk_ctx {
   cudaStream_t copy = nullptr;    // pk_read_display_async
   cudaEvent_t ev_api = nullptr, ev_tail = nullptr, ev_read = nullptr;
   bool overlap = true;            // shadow traversal beside the next closest-hit traversal
-  int in_flight = pk::MAX_IN_FLIGHT;  // frames of pk_render_frame in flight (1..MAX_IN_FLIGHT)
+  int in_flight = 4;  // frames of pk_render_frame in flight (1..MAX_IN_FLIGHT)
   int next_slot = 0, last_slot = 0;
   bool tail_pending = false;      // ev_tail: accumulate/postprocess of the last pipelined frame
   bool read_pending = false;      // ev_read: the last asynchronous display read
