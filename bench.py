@@ -344,7 +344,7 @@ def warm_graphs(ctx, first_sample: int, B: int):
     """Replays every frame slot once (a counting or timing frame re-captures a
     slot's graph), so no capture falls inside a timed region."""
     ctx.call("pk_set_render_state", first_sample, 0.0)
-    ctx.call("pk_render_frames", 4, B)
+    ctx.call("pk_render_frames", 8, B)  # up to eight slots
     ctx.call("pk_sync")
 
 
