@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--trace-mode", default="persistent", choices=["persistent", "chunked", "wide"],
                     help="traversal scheduling (identical results): persistent lanes with refill, or 32-ray chunks")
     ap.add_argument("--no-forms", action="store_true", help="skip the forms blocks (wide BVH, adjoint, batching)")
-    ap.add_argument("--profile-case", choices=["wide", "adjoint", "batch"],
+    ap.add_argument("--profile-case", choices=["wide", "wide_soup", "adjoint", "batch"],
                     help="run one small case of a form kernel (for ncu captures) and exit")
     ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4, 5, 6, 7, 8],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
@@ -355,10 +355,14 @@ def profile_case(name: str, local: int = 0):
     + box at 256x256, 4 spp, depth 4, one render and one adjoint; `batch` = 16
     requests over 2 scenes (9,998 / 327,690 triangles), half the batching
     workload's resolutions, <= 4 spp, block 128, stack 16, chunk 4, rendered
-    twice (the second launch is the one to capture)."""
+    twice (the second launch is the one to capture); `wide_soup` = the
+    8,388,608-triangle soup at 480x270 through the 8-wide traversal."""
     from pike_gb300 import _lib, synth
-    if name == "wide":
-        src = synth.displaced_sphere_scene(subdivisions=7, width=480, height=270)
+    if name in ("wide", "wide_soup"):
+        if name == "wide":
+            src = synth.displaced_sphere_scene(subdivisions=7, width=480, height=270)
+        else:
+            src = synth.triangle_soup_scene(width=480, height=270)
         ctx, _ = setup_context(src, local)
         ctx.call("pk_set_trace_mode", _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE)
         ctx.call("pk_set_camera", camera_struct(src))
