@@ -6,17 +6,19 @@
  * `generateCommands(commandEncoder)` method (render/passes/*.js), sequenced by
  * PikeRenderer.tick() (render/pike.js:120-162).  Each entry point below names
  * the reference interface it replaces.  A JavaScript host binds them through
- * N-API; the Python package pike_gb300 binds them through
- * ctypes.
+ * an N-API addon; the Python package pike_gb300 binds them through ctypes.
  *
  * Conventions
  *  - Every function returns a status: PK_OK (0) or an error code; the message
  *    of the last failure on a context is returned by pk_last_error().
  *  - The library owns all device memory.  Host input pointers are read before
  *    the call returns; output pointers must hold the documented element counts.
- *  - A context is single-threaded and enqueues on one CUDA stream.  Pass entry
- *    points enqueue work and return; pk_sync() waits and reports device-side
- *    error flags (queue/stack overflow, bounded-wait timeouts) as PK_ERR_DEVICE.
+ *  - A context is single-threaded.  Uploads, passes and reads enqueue on its
+ *    stream; pk_render_frame renders up to pk_set_frames_in_flight frames
+ *    concurrently on further streams of its own, and every other call orders
+ *    itself after them.  Entry points enqueue work and return; pk_sync() waits
+ *    and reports device-side error flags (queue/stack overflow, bounded-wait
+ *    timeouts) as PK_ERR_DEVICE.
  *  - Results are bit-identical to the CPU oracle's restatement of the reference
  *    (IEEE binary32, no FMA contraction, built-ins defined in pk_math.cuh).
  */
