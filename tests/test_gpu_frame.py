@@ -295,3 +295,18 @@ def test_frames_in_flight_across_reconfigure_env_and_switches(oracle, pk_built):
         assert_bits_equal(results[True][k], results[False][k], name)
     assert results[True][3]["samples"] == results[False][3]["samples"] == 8
     assert results[True][3]["err"] == 0
+
+
+def test_frame_scheduling_arguments(oracle, pk_built):
+    src = synth.small_scene(width=32, height=32)
+    pair = Pair(src, oracle)
+    c = pair.ctx
+    for bad in (0, 9, -1):
+        with pytest.raises(_lib.PikeError) as e:
+            c.call("pk_set_frames_in_flight", bad)
+        assert e.value.code == _lib.PK_ERR_ARG
+    for n in (1, 8):
+        c.call("pk_set_frames_in_flight", n)
+        c.call("pk_set_frame_overlap", n == 8)
+        fused_frames(pair, 9, 3)  # more frames than slots
+        assert pair.counters()["samples"] == 9 and pair.counters()["err"] == 0
