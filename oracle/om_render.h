@@ -909,15 +909,25 @@ struct Renderer {
     num_hits = num_misses = num_rays = 0;
     num_shadow = 0;
   }
+  // pike.js:133-154: W*H pixels in batches of B, each with its own counters,
+  // camera invocationOffset j*B and bounces; one colour buffer per frame.
   void tick(uint32_t bounces) {
     begin_frame();
-    pass_camera();
-    for (uint32_t i = 0; i < bounces; i++) {
-      pass_trace();
-      pass_shade_hit();
-      pass_trace_shadow();
-      pass_shade_miss();
+    const uint32_t nbatch = (uint32_t)(((uint64_t)W * H + B - 1) / B);
+    const uint32_t saved = cam.invocation_offset;
+    for (uint32_t j = 0; j < nbatch; j++) {
+      num_hits = num_misses = num_rays = 0;
+      num_shadow = 0;
+      cam.invocation_offset = j * B;
+      pass_camera();
+      for (uint32_t i = 0; i < bounces; i++) {
+        pass_trace();
+        pass_shade_hit();
+        pass_trace_shadow();
+        pass_shade_miss();
+      }
     }
+    cam.invocation_offset = saved;
     pass_accumulate();
     pass_postprocess();
     samples++;

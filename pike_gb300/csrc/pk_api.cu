@@ -787,47 +787,58 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
     if (forked) check(cudaStreamWaitEvent(st, fs.ev_shadow, 0), "cudaStreamWaitEvent");
     forked = false;
   };
-  const uint32_t nb = std::min(bounces, MAX_BOUNCES);
+  // tick() renders W*H pixels in batches of BATCH_SIZE (pk_configure's batch;
+  // pike.js:133-154), each with its own counters, camera offset and bounces.
+  const uint32_t nbatch = (uint32_t)(((uint64_t)c->npix + c->B - 1) / c->B);
+  const uint64_t steps = (uint64_t)nbatch * bounces;
+  const uint32_t nb = (uint32_t)std::min<uint64_t>(steps, MAX_BOUNCES);
   // RenderState.generateCommands + tick(): clear colour, hit/miss and ray counts
   check(cudaMemsetAsync(fs.color.p, 0, fs.color.bytes(), st), "memset");
   check(cudaMemsetAsync(&fs.ctr.p->num_hits, 0, 16, st), "memset");
   check(cudaMemsetAsync(fs.tickets.p, 0, fs.tickets.bytes(), st), "memset");
   check(cudaMemsetAsync(fs.tiles.p, 0, (size_t)std::max(nb, 1u) * (2 * c->ct + c->st) * 8, st), "memset");
-  fs.cur = 0;
-  c->timed(K_CAMERA, [&]() { launch_camera(L, fs.R(0), c->cap); });
-  for (uint32_t b = 0; b < bounces; b++) {
-    const uint32_t slot = b % MAX_BOUNCES;
-    if (b && slot == 0) {
-      join();  // the shadow traversal in flight still uses its slot's ticket
-      check(cudaMemsetAsync(fs.tickets.p, 0, fs.tickets.bytes(), st), "memset");
-      check(cudaMemsetAsync(fs.tiles.p, 0, fs.tiles.bytes(), st), "memset");
+  uint64_t seq = 0;  // (batch, bounce) steps so far: their ticket and tile slots
+  for (uint32_t batch = 0; batch < nbatch; batch++) {
+    if (batch) {
+      join();  // the previous batch's shadow traversal still reads its counts
+      check(cudaMemsetAsync(&fs.ctr.p->num_hits, 0, 16, st), "memset");  // clearNumHitsAndMisses, clearNumRays
     }
-    c->timed(K_TRACE, [&]() {
-      launch_trace(L, false, true, c->counting, &fs.ctr.p->num_rays, fs.R(fs.cur), fs.hrec.p, fs.hflags.p,
-                   fs.ticket(slot, 0));
-    });
-    join();
-    c->timed(K_COMPACT, [&]() {
-      launch_compact_trace(L, false, fs.hflags.p, fs.hit_list.p, fs.R(fs.cur), c->M(), fs.ticket(slot, 1),
-                           c->tiles_compact(slot, k), ov ? fs.hrec.p : nullptr);
-    });
-    c->timed(K_SHADE, [&]() {
-      launch_shade(L, fs.hit_list.p, fs.hrec.p, fs.R(fs.cur), fs.R(fs.cur ^ 1), fs.S(), fs.ticket(slot, 2),
-                   c->tiles_shade(slot, k));
-    });
-    fs.cur ^= 1;
-    if (ov) {
-      check(cudaEventRecord(fs.ev_shaded, st), "cudaEventRecord");
-      check(cudaStreamWaitEvent(fs.side, fs.ev_shaded, 0), "cudaStreamWaitEvent");
-      launch_trace(Ls, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
-                   fs.ticket(slot, 3));
-      check(cudaEventRecord(fs.ev_shadow, fs.side), "cudaEventRecord");
-      forked = true;
-    } else {
-      c->timed(K_SHADOW, [&]() {
-        launch_trace(L, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
-                     fs.ticket(slot, 3));
+    fs.cur = 0;
+    c->timed(K_CAMERA, [&]() { launch_camera(L, fs.R(0), c->cap, (int64_t)batch * c->B); });
+    for (uint32_t b = 0; b < bounces; b++, seq++) {
+      const uint32_t slot = (uint32_t)(seq % MAX_BOUNCES);
+      if (seq && slot == 0) {
+        join();  // the shadow traversal in flight still uses its slot's ticket
+        check(cudaMemsetAsync(fs.tickets.p, 0, fs.tickets.bytes(), st), "memset");
+        check(cudaMemsetAsync(fs.tiles.p, 0, fs.tiles.bytes(), st), "memset");
+      }
+      c->timed(K_TRACE, [&]() {
+        launch_trace(L, false, true, c->counting, &fs.ctr.p->num_rays, fs.R(fs.cur), fs.hrec.p, fs.hflags.p,
+                     fs.ticket(slot, 0));
       });
+      join();
+      c->timed(K_COMPACT, [&]() {
+        launch_compact_trace(L, false, fs.hflags.p, fs.hit_list.p, fs.R(fs.cur), c->M(), fs.ticket(slot, 1),
+                             c->tiles_compact(slot, k), ov ? fs.hrec.p : nullptr);
+      });
+      c->timed(K_SHADE, [&]() {
+        launch_shade(L, fs.hit_list.p, fs.hrec.p, fs.R(fs.cur), fs.R(fs.cur ^ 1), fs.S(), fs.ticket(slot, 2),
+                     c->tiles_shade(slot, k));
+      });
+      fs.cur ^= 1;
+      if (ov) {
+        check(cudaEventRecord(fs.ev_shaded, st), "cudaEventRecord");
+        check(cudaStreamWaitEvent(fs.side, fs.ev_shaded, 0), "cudaStreamWaitEvent");
+        launch_trace(Ls, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
+                     fs.ticket(slot, 3));
+        check(cudaEventRecord(fs.ev_shadow, fs.side), "cudaEventRecord");
+        forked = true;
+      } else {
+        c->timed(K_SHADOW, [&]() {
+          launch_trace(L, true, true, c->counting, &fs.ctr.p->num_shadow, fs.S(), nullptr, fs.sflags.p,
+                       fs.ticket(slot, 3));
+        });
+      }
     }
   }
   join();

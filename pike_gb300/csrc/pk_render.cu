@@ -52,13 +52,15 @@ __device__ __forceinline__ void camera_ray(const CamState& cam, uint32_t px, uin
   org = add(dof, eo);
 }
 
+// offset >= 0 replaces the camera's invocationOffset (tick()'s batch j passes
+// j * BATCH_SIZE, pike.js:146).
 __global__ void __launch_bounds__(128) k_camera(const CamState* __restrict__ camp, Counters* __restrict__ ctr,
-                                                RayQ R, uint32_t n_threads, uint32_t capacity) {
+                                                RayQ R, uint32_t n_threads, uint32_t capacity, int64_t offset) {
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= n_threads) return;
   const CamState cam = *camp;
   const uint32_t W = cam.dims_mask >> 16, H = cam.dims_mask & 0xffffu;
-  const uint32_t idx = gid + cam.invocation_offset;
+  const uint32_t idx = gid + (offset >= 0 ? (uint32_t)offset : cam.invocation_offset);
   const uint32_t px = idx % W, py = idx / W;
   if (px >= W || py >= H) return;
   V3 org, dir;
@@ -1266,9 +1268,9 @@ void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact
       std::max(1u, std::min((unsigned)(sms * std::max(w, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
 }
 
-void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads) {
+void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads, int64_t offset) {
   if (n_threads == 0) return;
-  k_camera<<<grid_for(n_threads, 128), 128, 0, L.stream>>>(L.cam, L.ctr, R, n_threads, L.capacity);
+  k_camera<<<grid_for(n_threads, 128), 128, 0, L.stream>>>(L.cam, L.ctr, R, n_threads, L.capacity, offset);
 }
 
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,

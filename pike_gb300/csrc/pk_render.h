@@ -34,7 +34,8 @@ struct LaunchCtx {
   bool defer_miss = false;
 };
 
-void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads);
+// offset >= 0: invocation offset of the rays (else the camera state's own)
+void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads, int64_t offset = -1);
 // Kernels that claim work through an atomic ticket take it as `ticket`; the
 // look-back kernels also take a zeroed tile-state array (one word per tile).
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,

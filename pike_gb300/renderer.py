@@ -50,8 +50,8 @@ class PikeRenderer:
             self.lastDraw = time.perf_counter()
         enc = self.device.createCommandEncoder()
         rs.generateCommands(enc)
-        if self.fused and self.BATCH_SIZE >= self.resolution[0] * self.resolution[1]:
-            # the whole tick in one call (misses shaded inside the traversal kernels)
+        if self.fused:
+            # the whole tick in one call: every batch, misses shaded inside the traversal kernels
             self.cameraPass.setCameraState(dict(self.camera, invocationOffset=0))
             self.device.ctx.call("pk_set_camera", self.cameraPass.cameraState)
             self.device.ctx.call("pk_render_frame", self.numBounces)

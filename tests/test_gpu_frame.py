@@ -310,3 +310,18 @@ def test_frame_scheduling_arguments(oracle, pk_built):
         c.call("pk_set_frame_overlap", n == 8)
         fused_frames(pair, 9, 3)  # more frames than slots
         assert pair.counters()["samples"] == 9 and pair.counters()["err"] == 0
+
+
+@pytest.mark.parametrize("batch,bounces", [(512, 3), (500, 8)])
+def test_fused_multi_batch_matches_oracle(oracle, pk_built, batch, bounces):
+    """tick() over several pixel batches (pike.js:133-154) in one
+    pk_render_frame: 1500 pixels in batches of 512, and of 500 (the camera
+    dispatch rounds up to 512 invocations, so 12 pixels of each next batch are
+    traced twice, as in the reference), 3 and 8 bounces (24 steps wrap the 16
+    per-step ticket slots)."""
+    src = synth.small_scene(width=50, height=30)
+    pair = Pair(src, oracle, batch=batch)
+    fused_frames(pair, 2, bounces)
+    oracle_frames(pair, 2, bounces)
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), f"batch {batch}")
+    assert pair.counters()["err"] == 0
