@@ -60,8 +60,8 @@ def parse():
                     help="run one small case of a form kernel (for ncu captures) and exit")
     ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4, 5, 6, 7, 8],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
-    ap.add_argument("--no-overlap", action="store_true",
-                    help="serial frames: no shadow traversal beside the next bounce's closest-hit traversal")
+    ap.add_argument("--overlap", choices=["auto", "on", "off"], default="auto",
+                    help="shadow traversal beside the next bounce's closest-hit traversal (auto: with one frame in flight)")
     ap.add_argument("--precision", action="store_true",
                     help="also run form (1)'s 8.4M-triangle soup workload (adds about a minute)")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
@@ -717,7 +717,7 @@ def gpu_arm(args):
     if args.node_records == 32:
         mode |= _lib.PK_TRACE_COMPACT_RECORDS
     ctx.call("pk_set_trace_mode", mode)
-    ctx.call("pk_set_frame_overlap", 0 if args.no_overlap else 1)
+    ctx.call("pk_set_frame_overlap", {"auto": _lib.PK_OVERLAP_AUTO, "on": 1, "off": 0}[args.overlap])
     ctx.call("pk_set_frames_in_flight", args.frames_in_flight)
     cam = camera_struct(src)
     ctx.call("pk_set_camera", cam)
@@ -820,7 +820,8 @@ def gpu_arm(args):
                        "bounces": B, "env": "2048x1024 RGBE8", "spp_mpix_per_s": spp_mpix,
                        "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
                        "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}", "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
-                       "frame_overlap": not args.no_overlap and args.trace_mode != "chunked",
+                       "frame_overlap": args.trace_mode != "chunked" and (
+                           args.overlap == "on" or (args.overlap == "auto" and args.frames_in_flight == 1)),
                        "frames_in_flight": args.frames_in_flight,
                        "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
                        "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},

@@ -255,11 +255,14 @@ int pk_read_stats(pk_ctx* ctx, uint64_t out10[10]);
 #define PK_ACCUM_RUNNING_MEAN 0
 #define PK_ACCUM_COMPENSATED 1
 int pk_set_accumulation(pk_ctx* ctx, int mode);
-/* overlap != 0 (the default) lets pk_render_frame run each bounce's shadow
- * traversal concurrently with the next bounce's closest-hit traversal on a
- * second stream of its graph; images are bit-identical either way (pixels
- * receive their contributions in the same order).  Applies to the persistent
- * and 8-wide traversal modes without per-kernel timing. */
+/* overlap = 1 lets pk_render_frame run each bounce's shadow traversal
+ * concurrently with the next bounce's closest-hit traversal on a second stream
+ * of its graph, 0 runs them in sequence, PK_OVERLAP_AUTO (the default) does
+ * the former only when one frame is in flight (several frames in flight
+ * already fill the shadow traversals' tails).  Images are bit-identical either
+ * way (pixels receive their contributions in the same order).  Applies to the
+ * persistent and 8-wide traversal modes without per-kernel timing. */
+#define PK_OVERLAP_AUTO (-1)
 int pk_set_frame_overlap(pk_ctx* ctx, int overlap);
 /* Frames of pk_render_frame in flight, 1 to 8 (4 by default): with 2 or more,
  * consecutive frames render on separate sets of queues and streams so one

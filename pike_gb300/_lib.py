@@ -22,6 +22,7 @@ PK_BVH_BINNED = 1
 PK_ACCUM_RUNNING_MEAN, PK_ACCUM_COMPENSATED = 0, 1
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
 PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE, PK_TRACE_EXACT = 0, 1, 2, 4, 8
+PK_OVERLAP_AUTO = -1
 
 
 class PikeError(RuntimeError):

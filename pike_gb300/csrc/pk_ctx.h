@@ -72,7 +72,7 @@ struct pk_ctx {
   cudaStream_t stream = nullptr;  // the API stream: uploads, passes, readbacks, serial frames
   cudaStream_t copy = nullptr;    // pk_read_display_async
   cudaEvent_t ev_api = nullptr, ev_tail = nullptr, ev_read = nullptr;
-  bool overlap = true;            // shadow traversal beside the next closest-hit traversal
+  int overlap = PK_OVERLAP_AUTO;  // shadow traversal beside the next closest-hit traversal
   int in_flight = 4;  // frames of pk_render_frame in flight (1..MAX_IN_FLIGHT)
   int next_slot = 0, last_slot = 0;
   bool tail_pending = false;      // ev_tail: accumulate/postprocess of the last pipelined frame

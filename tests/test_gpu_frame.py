@@ -161,12 +161,14 @@ def test_counting_kernels_match_oracle_counts(oracle, pk_built):
 @pytest.mark.parametrize("mode,bounces", [(_lib.PK_TRACE_PERSISTENT, 8), (_lib.PK_TRACE_PERSISTENT, 20),
                                           (_lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE, 8)])
 def test_frame_overlap_is_bit_identical(oracle, pk_built, mode, bounces):
-    """Shadow traversal of bounce b beside the closest-hit traversal of b+1 (the
-    default) against the serial frame; 20 bounces wrap the 16 per-bounce
-    ticket slots.  The persistent binary mode is also checked against the oracle."""
+    """Shadow traversal of bounce b beside the closest-hit traversal of b+1
+    against the serial frame, one frame at a time (where the default turns it
+    on) and four in flight; 20 bounces wrap the 16 per-bounce ticket slots.
+    The persistent binary mode is also checked against the oracle."""
     src = synth.displaced_sphere_scene(subdivisions=6, width=160, height=90, env_size=(512, 256))
     pair = Pair(src, oracle)
     pair.ctx.call("pk_set_trace_mode", mode)  # after the BVH: the 8-wide tree is built from it
+    pair.ctx.call("pk_set_frames_in_flight", 1)  # PK_OVERLAP_AUTO: overlapped
     fused_frames(pair, 2, bounces)
     on = pair.image("accum").copy()
     assert pair.counters()["err"] == 0
@@ -174,6 +176,11 @@ def test_frame_overlap_is_bit_identical(oracle, pk_built, mode, bounces):
     pair.ctx.call("pk_write_accum", ptr(np.zeros_like(on)))
     fused_frames(pair, 2, bounces)
     assert_bits_equal(pair.image("accum"), on, "serial vs overlapped frame")
+    pair.ctx.call("pk_set_frames_in_flight", 4)
+    pair.ctx.call("pk_set_frame_overlap", 1)
+    pair.ctx.call("pk_write_accum", ptr(np.zeros_like(on)))
+    fused_frames(pair, 2, bounces)
+    assert_bits_equal(pair.image("accum"), on, "overlapped frames in flight")
     if mode == _lib.PK_TRACE_PERSISTENT:
         oracle_frames(pair, 2, bounces)
         assert_bits_equal(on, pair.P.r.accum(), "overlapped frame vs oracle")
@@ -307,7 +314,7 @@ def test_frame_scheduling_arguments(oracle, pk_built):
         assert e.value.code == _lib.PK_ERR_ARG
     for n in (1, 8):
         c.call("pk_set_frames_in_flight", n)
-        c.call("pk_set_frame_overlap", n == 8)
+        c.call("pk_set_frame_overlap", 1 if n == 8 else _lib.PK_OVERLAP_AUTO)
         fused_frames(pair, 9, 3)  # more frames than slots
         assert pair.counters()["samples"] == 9 and pair.counters()["err"] == 0
 
