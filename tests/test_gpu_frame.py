@@ -332,3 +332,26 @@ def test_fused_multi_batch_matches_oracle(oracle, pk_built, batch, bounces):
     oracle_frames(pair, 2, bounces)
     assert_bits_equal(pair.image("accum"), pair.P.r.accum(), f"batch {batch}")
     assert pair.counters()["err"] == 0
+
+
+@pytest.mark.parametrize("mode", [_lib.PK_TRACE_PERSISTENT, _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_WIDE,
+                                  _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_EXACT])
+def test_scheduling_combinations_are_bit_identical(oracle, pk_built, mode):
+    """Pixel batches (500 of 1500 pixels) x three frames in flight x forced
+    overlap, against one frame at a time without overlap, for every
+    persistent traversal; the reference traversal also against the oracle."""
+    src = synth.small_scene(width=50, height=30)
+    out = []
+    for in_flight, overlap in ((1, 0), (3, 1)):
+        pair = Pair(src, oracle, batch=500)
+        c = pair.ctx
+        c.call("pk_set_trace_mode", mode)
+        c.call("pk_set_frames_in_flight", in_flight)
+        c.call("pk_set_frame_overlap", overlap)
+        fused_frames(pair, 5, 6)
+        assert pair.counters()["err"] == 0
+        out.append(pair.image("accum").copy())
+    assert_bits_equal(out[1], out[0], "scheduled vs plain")
+    if mode == _lib.PK_TRACE_PERSISTENT:
+        oracle_frames(pair, 5, 6)
+        assert_bits_equal(out[1], pair.P.r.accum(), "scheduled vs oracle")
