@@ -61,7 +61,8 @@ def parse():
     ap.add_argument("--frames-in-flight", type=int, default=4, choices=[1, 2, 3, 4, 5, 6, 7, 8],
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order)")
     ap.add_argument("--overlap", choices=["auto", "on", "off"], default="auto",
-                    help="shadow traversal beside the next bounce's closest-hit traversal (auto: with one frame in flight)")
+                    help="shadow traversal beside the next bounce's closest-hit traversal "
+                         "(auto: with one frame in flight or below 2^20 pixels)")
     ap.add_argument("--precision", action="store_true",
                     help="also run form (1)'s 8.4M-triangle soup workload (adds about a minute)")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
@@ -821,7 +822,8 @@ def gpu_arm(args):
                        "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
                        "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}", "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
                        "frame_overlap": args.trace_mode != "chunked" and (
-                           args.overlap == "on" or (args.overlap == "auto" and args.frames_in_flight == 1)),
+                           args.overlap == "on" or (args.overlap == "auto" and (
+                               args.frames_in_flight == 1 or src.width * src.height < (1 << 20)))),
                        "frames_in_flight": args.frames_in_flight,
                        "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
                        "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},

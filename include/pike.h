@@ -258,8 +258,9 @@ int pk_set_accumulation(pk_ctx* ctx, int mode);
 /* overlap = 1 lets pk_render_frame run each bounce's shadow traversal
  * concurrently with the next bounce's closest-hit traversal on a second stream
  * of its graph, 0 runs them in sequence, PK_OVERLAP_AUTO (the default) does
- * the former only when one frame is in flight (several frames in flight
- * already fill the shadow traversals' tails).  Images are bit-identical either
+ * the former when one frame is in flight or the ray queue holds fewer than
+ * 2^20 rays (several large frames in flight already fill the shadow
+ * traversals' tails).  Images are bit-identical either
  * way (pixels receive their contributions in the same order).  Applies to the
  * persistent and 8-wide traversal modes without per-kernel timing. */
 #define PK_OVERLAP_AUTO (-1)

@@ -778,10 +778,12 @@ int pk_postprocess(pk_ctx* c) {
 static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bounces, bool tail) {
   FrameSlot& fs = c->slot[k];
   LaunchCtx L = c->launch(k, st);
-  // PK_OVERLAP_AUTO: overlap when frames render one at a time (with several
-  // in flight they already fill the shadow tails; measured 2596-2599 with vs
-  // 2610-2612 Mrays/s without at four frames, +19% with at one)
-  const bool want = c->overlap == PK_OVERLAP_AUTO ? c->in_flight == 1 : c->overlap != 0;
+  // PK_OVERLAP_AUTO: overlap when frames render one at a time or are small
+  // (below 2^20 rays); several large frames in flight already fill the shadow
+  // tails (1080p, four frames: 2596-2599 Mrays/s with, 2610-2612 without; one
+  // frame: +19% with; the batching workload's small requests one at a time
+  // through four frames in flight: 644 ms with, 708 ms without)
+  const bool want = c->overlap == PK_OVERLAP_AUTO ? (c->in_flight == 1 || c->cap < (1u << 20)) : c->overlap != 0;
   const bool ov = want && !c->timing && (c->trace_mode & (pk::TRACE_PERSISTENT | pk::TRACE_WIDE)) != 0;
   L.defer_miss = ov;
   LaunchCtx Ls = L;
