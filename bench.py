@@ -116,6 +116,14 @@ class Dist:
             self.dist.destroy_process_group()
 
 
+def replica_throughput(D: Dist, rays_local: float, ms_local: float):
+    """Whole-job Mrays/s of N replicas: every rank's rays over the slowest
+    rank's time (max over ranks); returns (value, ms_max) on every rank."""
+    ms_max = D.max(ms_local)
+    rays_total = D.sum(float(rays_local))
+    return rays_total / (ms_max / 1000.0) / 1e6, ms_max
+
+
 class Clocks:
     """nvidia-smi samples (every 200 ms) while the timed region runs."""
 
@@ -216,7 +224,7 @@ def cpu_run(src, bounces: int, seconds: float, threads: int):
         r.reset_stats()
         r.set_render_state(frames)
         t = time.perf_counter()
-        r.tick(bounces)
+        r.tick_batch(bounces)  # the band only
         elapsed += time.perf_counter() - t
         s = r.stats()
         rays += s["trace_rays"] + s["shadow_rays"]
@@ -764,9 +772,7 @@ def gpu_arm(args):
     st = read_stats(ctx)
     rays_local = st["rays_traced"]
     D.barrier()
-    ms_max = D.max(ms)
-    rays_total = D.sum(float(rays_local))
-    value = rays_total / (ms_max / 1000.0) / 1e6
+    value, ms_max = replica_throughput(D, rays_local, ms)
     npix = src.width * src.height
     spp_mpix = world * args.steps * npix / (ms_max / 1000.0) / 1e6
 

@@ -116,15 +116,18 @@ struct Renderer {
     if (on) alloc64();
   }
 
+  // Queues hold the camera dispatch of a batch, rounded up to 128 invocations
+  // (camera.wgsl's workgroup size), as the GPU's do.
   void configure(uint32_t w, uint32_t h, uint32_t batch) {
     W = w; H = h; B = batch;
+    const size_t cap = round_up(B, 128);
     color.assign(4 * (size_t)W * H, 0.0f);
     temp.assign(4 * (size_t)W * H, 0.0f);
     display.assign(4 * (size_t)W * H, 0.0f);
     display8.assign(4 * (size_t)W * H, 0);
-    ray_buffer.assign(3 * (size_t)B, DeferredRay{});
-    miss_buffer.assign(2 * (size_t)B, DeferredRay{});
-    hit_buffer.assign((size_t)B, Hit{});
+    ray_buffer.assign(3 * cap, DeferredRay{});
+    miss_buffer.assign(2 * cap, DeferredRay{});
+    hit_buffer.assign(cap, Hit{});
     if (track64) alloc64();
   }
   static uint32_t round_up(uint32_t n, uint32_t m) { return (n + m - 1) / m * m; }
@@ -291,7 +294,7 @@ struct Renderer {
   }
   void pass_trace() {
     num_hits = 0; num_misses = 0;   // TracePass.generateCommands: clearNumHitsAndMisses
-    const uint32_t n = num_rays;
+    const uint32_t n = std::min<uint32_t>(num_rays, shadow_offset());
     std::vector<TravResult> res(n);
     parallel_for(n, nthreads, [&](size_t b, size_t e, int) {
       std::vector<int32_t> stack;
@@ -319,7 +322,8 @@ struct Renderer {
   }
   uint32_t shadow_offset() const { return (uint32_t)(ray_buffer.size() / 2); }
   void pass_trace_shadow() {
-    const uint32_t n = num_shadow, off = shadow_offset();
+    const uint32_t off = shadow_offset();
+    const uint32_t n = std::min<uint32_t>(num_shadow, (uint32_t)(ray_buffer.size() - off));
     std::vector<TravResult> res(n);
     parallel_for(n, nthreads, [&](size_t b, size_t e, int) {
       std::vector<int32_t> stack;
@@ -615,7 +619,7 @@ struct Renderer {
   }
   void pass_shade_hit() {
     num_rays = 0; num_shadow = 0;   // ShadeHitPass.generateCommands: clearNumRays
-    const uint32_t n = num_hits;
+    const uint32_t n = std::min<uint32_t>(num_hits, (uint32_t)hit_buffer.size());
     std::vector<ShadeOut> res(n);
     std::vector<Shade64> r64(track64 ? n : 0);
     parallel_for(n, nthreads, [&](size_t b, size_t e, int) {
@@ -816,7 +820,7 @@ struct Renderer {
     return v3(r * p, g * p, b * p);
   }
   void pass_shade_miss() {
-    const uint32_t n = num_misses;
+    const uint32_t n = std::min<uint32_t>(num_misses, (uint32_t)miss_buffer.size());
     std::vector<V3> res(n);
     parallel_for(n, nthreads, [&](size_t b, size_t e, int) {
       for (size_t j = b; j < e; j++) {
@@ -908,6 +912,21 @@ struct Renderer {
     if (track64) std::fill(color64.begin(), color64.end(), 0.0);
     num_hits = num_misses = num_rays = 0;
     num_shadow = 0;
+  }
+  // One batch of tick() at the camera's own invocationOffset (a band of the
+  // frame: the bounded CPU sample of the benchmark).
+  void tick_batch(uint32_t bounces) {
+    begin_frame();
+    pass_camera();
+    for (uint32_t i = 0; i < bounces; i++) {
+      pass_trace();
+      pass_shade_hit();
+      pass_trace_shadow();
+      pass_shade_miss();
+    }
+    pass_accumulate();
+    pass_postprocess();
+    samples++;
   }
   // pike.js:133-154: W*H pixels in batches of B, each with its own counters,
   // camera invocationOffset j*B and bounces; one colour buffer per frame.

@@ -203,6 +203,7 @@ void or_shade_miss(void* p) { ((Renderer*)p)->pass_shade_miss(); }
 void or_accumulate(void* p) { ((Renderer*)p)->pass_accumulate(); }
 void or_postprocess(void* p) { ((Renderer*)p)->pass_postprocess(); }
 void or_tick(void* p, uint32_t bounces) { ((Renderer*)p)->tick(bounces); }
+void or_tick_batch(void* p, uint32_t bounces) { ((Renderer*)p)->tick_batch(bounces); }
 
 // samples, num_hits, num_misses, num_rays, num_shadow, overflow
 void or_counters(void* p, uint32_t* out6) {

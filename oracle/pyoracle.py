@@ -45,6 +45,7 @@ def lib():
                      "or_reset_stats", "or_clear_color", "or_clear_hits_misses", "or_clear_rays"):
             getattr(_lib, name).argtypes = [C.c_void_p]
         _lib.or_tick.argtypes = [C.c_void_p, C.c_uint32]
+        _lib.or_tick_batch.argtypes = [C.c_void_p, C.c_uint32]
         _lib.or_set_threads.argtypes = [C.c_void_p, C.c_int]
         _lib.or_set_track64.argtypes = [C.c_void_p, C.c_int]
         _lib.or_frames64.argtypes = [C.c_void_p]
@@ -215,7 +216,12 @@ class Renderer:
         raise AttributeError(name)
 
     def tick(self, bounces: int):
+        """pike.js tick(): every pixel batch of the frame."""
         lib().or_tick(self.p, bounces)
+
+    def tick_batch(self, bounces: int):
+        """One batch of tick() at the camera's own invocationOffset."""
+        lib().or_tick_batch(self.p, bounces)
 
     def counters(self):
         c = np.zeros(6, np.uint32)
