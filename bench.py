@@ -11,9 +11,12 @@ steps.  Inputs are synthetic (seeded generators of that shape).
 
 Metric: Mrays/s (closest-hit + shadow rays traced per second, whole job),
 with spp*Mpix/s alongside.  `value` is device time (CUDA events on the
-library's stream) with the scene resident in HBM; `e2e` runs the same steps
-through the C ABI with the per-step render state and camera uploaded from
-pinned host memory and the 8-bit image read back into pinned host memory.
+library's API stream, which waits for every frame in flight) with the scene
+resident in HBM; `e2e` runs the same steps through the C ABI with the
+per-step render state and camera (56 bytes, handed to the device as launch
+parameters of the frame's state kernel) and every frame's 8-bit image read
+back asynchronously into pinned host memory.  Frames render four at a time
+in flight (pk_set_frames_in_flight), bit-identical to one at a time.
 
 --impl reference times the CPU restatement of the reference path (the oracle;
 the reference itself is JavaScript + WGSL on WebGPU and cannot run here) on
