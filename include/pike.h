@@ -310,7 +310,9 @@ int pk_read_display_async(pk_ctx* ctx, uint8_t* out8);
 #define PK_TRACE_EXACT 8
 int pk_set_trace_mode(pk_ctx* ctx, int mode);
 /* Elementwise evaluation of the library's built-in definitions on the GPU
- * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)). */
+ * (fn 0 sin, 1 cos, 2 tan, 3 atan2(x, y), 4 acos, 5 exp2, 6 log2, 7 pow(x, y)),
+ * and of the integer decodes on bit-cast integer inputs (fn 8 the node-box
+ * snorm16, 9 snorm8, 10 unorm8, 11 unorm16, 12 the attribute snorm16). */
 int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);
 
 /* ---- form (3): differentiable rendering (no reference counterpart) -------

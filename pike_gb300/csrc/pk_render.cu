@@ -85,8 +85,7 @@ __device__ __forceinline__ V3 env_color(const EnvDev& env, float theta, V3 dir) 
   x = ((x % env.w) + env.w) % env.w;
   y = ((y % env.h) + env.h) % env.h;
   const uchar4 cc = env.rgbe[(size_t)y * env.w + x];
-  const float r = (float)cc.x / 255.0f, g = (float)cc.y / 255.0f, b = (float)cc.z / 255.0f,
-              a = (float)cc.w / 255.0f;
+  const float r = unorm8(cc.x), g = unorm8(cc.y), b = unorm8(cc.z), a = unorm8(cc.w);
   const float p = pow_(2.0f, a * 255.0f - 128.0f);
   return v3(r * p, g * p, b * p);
 }
@@ -604,7 +603,7 @@ __device__ __forceinline__ float4 texel_at(const SceneDev& sc, int l, int i, int
   i = ((i % R) + R) % R;
   j = ((j % R) + R) % R;
   const uchar4 t = __ldg(sc.layers + ((size_t)l * R + (size_t)j) * R + (size_t)i);
-  return make_float4((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f, (float)t.w / 255.0f);
+  return make_float4(unorm8(t.x), unorm8(t.y), unorm8(t.z), unorm8(t.w));
 }
 // textureSampleLevel(atlas, linear + repeat sampler, uv, layer, 0) on rgba8unorm
 // layers (shade_hit.wgsl:184-197): a 1x1 layer returns its texel; larger ones
@@ -1031,6 +1030,10 @@ __global__ void k_math(int fn, const float* __restrict__ x, const float* __restr
     case 6: r = log2_(a); break;
     case 7: r = pow_(a, b); break;
     case 8: r = snorm16_decode(__float_as_int(a)); break;
+    case 9: r = snorm8(__float_as_int(a)); break;     // integer inputs, bit-cast
+    case 10: r = unorm8((uint32_t)__float_as_int(a)); break;
+    case 11: r = unorm16((uint32_t)__float_as_int(a)); break;
+    case 12: r = snorm16(__float_as_int(a)); break;
     default: r = __int_as_float(0x7fc00000);
   }
   out[i] = r;

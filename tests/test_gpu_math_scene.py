@@ -165,3 +165,19 @@ def test_bvh_soup_matches_oracle(ctx, oracle):
 @pytest.mark.slow
 def test_bvh_full_sphere_matches_oracle(ctx, oracle):
     _bvh_case(ctx, oracle, synth.displaced_sphere_scene(subdivisions=8, width=8, height=8, env_size=(64, 32)))
+
+
+@pytest.mark.parametrize("fn,lo,hi,div,signed", [(9, -128, 127, 127.0, True), (10, 0, 255, 255.0, False),
+                                                 (11, 0, 65535, 65535.0, False),
+                                                 (12, -32768, 32767, 32767.0, True)])
+def test_integer_decodes_all_values(ctx, fn, lo, hi, div, signed):
+    """snorm8, unorm8, unorm16 and snorm16 decode with a reciprocal product and
+    one FMA; each must equal the IEEE quotient (max(v / d, -1) when signed)
+    for every value of its domain."""
+    v = np.arange(lo, hi + 1, dtype=np.int32)
+    got = np.zeros(v.size, np.float32)
+    ctx.call("pk_math_eval", fn, ptr(v.view(np.float32)), None, ptr(got), v.size)
+    want = v.astype(np.float32) / np.float32(div)
+    if signed:
+        want = np.maximum(want, np.float32(-1.0))
+    assert_bits_equal(got, want, f"decode fn {fn}")
