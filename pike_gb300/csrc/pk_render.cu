@@ -769,9 +769,10 @@ constexpr int SHADE_THREADS = 128;
 // main (:407-483).  Tiles of SHADE_THREADS hits are claimed in order; bounce
 // and shadow rays are written at their stable ranks found by a block scan plus
 // decoupled look-back, so slot order equals the serial order of the reference.
-// 10 resident blocks per SM (<= 48 registers): more shading warps in flight to
+// 12 resident blocks per SM (<= 40 registers): more shading warps in flight to
 // cover the attribute/texel/env gathers; some registers spill to L1 (1080p
-// frame: 2583 Mrays/s at 10 blocks, 2540 at 8, 2558 at 12).
+// frame, paired runs: 3007-3013 Mrays/s at 12 blocks, 2943-2946 at 10, 2926
+// at 8, 2990 at 14, 2992 at 16).
 // shade_hit.wgsl:407-483 for one hit: the hit record of slot `r` (its
 // position in the hit list, which seeds the RNG) on ray (o4, d4, t4).
 // Returns whether the surface emits (emission contribution in em); eb/es with
@@ -851,7 +852,7 @@ __device__ __forceinline__ bool shade_one(const SceneDev& sc, const EnvDev& env,
   return emitted;
 }
 
-__global__ void __launch_bounds__(SHADE_THREADS, 10) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+__global__ void __launch_bounds__(SHADE_THREADS, 12) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                           const uint32_t* __restrict__ hit_list,
                                                           const uint4* __restrict__ hrec, RayQ Rin, RayQ Rout,
                                                           RayQ S, uint32_t capacity, float4* __restrict__ color,
