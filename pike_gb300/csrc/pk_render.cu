@@ -1088,11 +1088,12 @@ __device__ __noinline__ void batch_camera(const CamState& cam, uint32_t px, uint
   camera_ray(cam, px, py, W, H, samples, org, dir);
 }
 
-// 32 resident warps per SM (64 registers, a few spilled): the loop stalls
+// 40 resident warps per SM (48 registers, some spilled): the loop stalls
 // mostly on instruction fetch and memory latency, and more warps hide both
-// (653 ms at 24 warps, 572 at 32, 577 at 40 on the 64-request batch).
+// (64-request batch with the current shading code: 481 ms at 32 warps, 425 at
+// 40, 434 at 48, 489 at 64).
 template <int BLOCK, int SSTACK>
-__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) k_batch(const BatchScene* __restrict__ scenes, int nscenes,
+__global__ void __launch_bounds__(BLOCK, 1280 / BLOCK) k_batch(const BatchScene* __restrict__ scenes, int nscenes,
                                                  const BatchReq* __restrict__ reqs, int nreq,
                                                  unsigned long long total, int chunk,
                                                  unsigned long long* __restrict__ counter,
