@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (!have && !exhausted) {
         j = base + (uint32_t)__popc(idle & ltmask);
         if (j < n) {
-          const float4 o = R.o[j], d = R.d[j];
+          const float4 o = __ldcs(R.o + j), d = __ldcs(R.d + j);  // read once
           ox = o.x; oy = o.y; oz = o.z;
           dx = d.x; dy = d.y; dz = d.z;
           if (EXACT) { ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz); }
@@ -322,11 +322,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
     if (fin) {
       const bool hit = best_i != -1;
       if (hit) {
-        if (!ANY) hrec[j] = make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u);
+        if (!ANY) __stcs(hrec + j, make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u));
         if (!(ANY && FUSED)) atomicOr(flags + (j >> 5), 1u << (j & 31u));
         if (COUNT) nhit += 1;
       } else if (FUSED) {
-        const float4 tpv = R.t[j];
+        const float4 tpv = __ldcs(R.t + j);
         const V3 e = env_color(env, theta, v3(dx, dy, dz));
         fused_miss<ANY>(color, npix, hrec, j, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y,
                         e.z * tpv.z, defer, &ctr->err);
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
       if (!have && !exhausted) {
         j = base + (uint32_t)__popc(idle & ltmask);
         if (j < n) {
-          const float4 o = R.o[j], d = R.d[j];
+          const float4 o = __ldcs(R.o + j), d = __ldcs(R.d + j);  // read once
           ox = o.x; oy = o.y; oz = o.z;
           dx = d.x; dy = d.y; dz = d.z;
           ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz);
@@ -470,11 +470,11 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
     if (fin) {
       const bool hit = best_i != -1;
       if (hit) {
-        if (!ANY) hrec[j] = make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u);
+        if (!ANY) __stcs(hrec + j, make_uint4(__float_as_uint(best_t), (uint32_t)best_i, best_b, 0u));
         if (!(ANY && FUSED)) atomicOr(flags + (j >> 5), 1u << (j & 31u));
         if (COUNT) nhit += 1;
       } else if (FUSED) {
-        const float4 tpv = R.t[j];
+        const float4 tpv = __ldcs(R.t + j);
         const V3 e = env_color(env, theta, v3(dx, dy, dz));
         fused_miss<ANY>(color, npix, hrec, j, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y,
                         e.z * tpv.z, defer, &ctr->err);
@@ -880,13 +880,13 @@ __global__ void __launch_bounds__(SHADE_THREADS, 12) k_shade(SceneDev sc, EnvDev
     uint32_t j = 0;
     uint4 hr = make_uint4(0u, 0u, 0u, 0u);
     bool valid = r < nh;
-    if (valid) {
-      j = hit_list[r];
-      if (j < capacity) hr = hrec[j];
+    if (valid) {  // hit list, hit records and rays are read once: streaming loads
+      j = __ldcs(hit_list + r);
+      if (j < capacity) hr = __ldcs(hrec + j);
       if (j >= capacity || hr.y >= sc.n_tris) { atomicOr(&ctr->err, ERR_QUEUE); valid = false; }
     }
     if (valid) {
-      const float4 o4 = Rin.o[j], d4 = Rin.d[j], t4 = Rin.t[j];
+      const float4 o4 = __ldcs(Rin.o + j), d4 = __ldcs(Rin.d + j), t4 = __ldcs(Rin.t + j);
       V3 em;
       if (shade_one(sc, env, theta, samples, r, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd, st))
         add_color(color, npix, __float_as_uint(t4.w) & 0x0fffffffu, em.x, em.y, em.z, 1.0f, &ctr->err);
