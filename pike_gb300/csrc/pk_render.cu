@@ -897,11 +897,19 @@ __global__ void __launch_bounds__(SHADE_THREADS, 12) k_shade(SceneDev sc, EnvDev
     __syncthreads();
     const uint32_t pb = unpack_a(s_excl) + ea, ps = unpack_b(s_excl) + es2;
     if (eb) {
-      if (pb < capacity) { Rout.o[pb] = bo; Rout.d[pb] = bd; Rout.t[pb] = bt; }
+      if (pb < capacity) {  // read once by the next traversal: streaming stores
+        __stcs(Rout.o + pb, bo);
+        __stcs(Rout.d + pb, bd);
+        __stcs(Rout.t + pb, bt);
+      }
       else atomicOr(&ctr->err, ERR_QUEUE);
     }
     if (es) {
-      if (ps < capacity) { S.o[ps] = so; S.d[ps] = sd; S.t[ps] = st; }
+      if (ps < capacity) {
+        __stcs(S.o + ps, so);
+        __stcs(S.d + ps, sd);
+        __stcs(S.t + ps, st);
+      }
       else atomicOr(&ctr->err, ERR_QUEUE);
     }
     if (tile == ntiles - 1 && threadIdx.x == 0) {
