@@ -3,7 +3,7 @@
  *
  * The reference drives its passes from JavaScript through WebGPU: pass objects
  * with a `static async create(device, ...)` factory and a
- * `generateCommands(commandEncoder)` method (render/passes/*.js), sequenced by
+ * `generateCommands(commandEncoder)` method (the files of render/passes), sequenced by
  * PikeRenderer.tick() (render/pike.js:120-162).  Each entry point below names
  * the reference interface it replaces.  A JavaScript host binds them through
  * an N-API addon; the Python package pike_gb300 binds them through ctypes.
