@@ -313,6 +313,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
           best_i = base + i;
           best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
         }
+        // any hit only reports whether some triangle is hit: stop at the first
+        // (the counting variant tests the whole leaf, as trace_shadow.wgsl does)
+        if (ANY && !COUNT && best_i != -1) break;
       }
       if (ANY && best_i != -1) { fin = true; break; }
       if (sp == 0) { fin = true; break; }
@@ -463,6 +466,7 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
           best_i = base + i;
           best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
         }
+        if (ANY && !COUNT && best_i != -1) break;  // any hit: the first is enough
       }
       if (ANY && best_i != -1) { fin = true; break; }
       if (!wide_pop(sstack, sdist, lstack, ldist, tid, sp, best_t, cur)) { fin = true; break; }
