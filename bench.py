@@ -15,8 +15,12 @@ library's API stream, which waits for every frame in flight) with the scene
 resident in HBM; `e2e` runs the same steps through the C ABI with the
 per-step render state and camera (56 bytes, handed to the device as launch
 parameters of the frame's state kernel) and every frame's 8-bit image read
-back asynchronously into pinned host memory.  Frames render four at a time
-in flight (pk_set_frames_in_flight), bit-identical to one at a time.
+back asynchronously into pinned host memory, timed by the host clock from the
+first call to the return of the final pk_sync.  Frames render four at a time
+in flight (pk_set_frames_in_flight), bit-identical to one at a time.  The
+roofline line adds an L2 fraction against an L2 read peak measured in the
+same run (pk_probe_read_bandwidth).  The `forms` block includes the
+8,388,608-triangle soup (the precision workload) unless --no-precision.
 
 --impl reference times the CPU restatement of the reference path (the oracle;
 the reference itself is JavaScript + WGSL on WebGPU and cannot run here) on
@@ -66,8 +70,8 @@ def parse():
     ap.add_argument("--overlap", choices=["auto", "on", "off"], default="auto",
                     help="shadow traversal beside the next bounce's closest-hit traversal "
                          "(auto: with one frame in flight or below 2^20 pixels)")
-    ap.add_argument("--precision", action="store_true",
-                    help="also run form (1)'s 8.4M-triangle soup workload (adds about a minute)")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip form (1)'s 8.4M-triangle soup workload (part of the default run)")
     ap.add_argument("--node-records", type=int, default=64, choices=[32, 64],
                     help="inner-node record size (identical results): decoded float boxes (64) or snorm16 (32)")
     return ap.parse_args()
@@ -198,6 +202,21 @@ def profiled_traffic():
     return None
 
 
+def l2_peak(ctx) -> dict:
+    """L2 read-bandwidth peak from the library's probe kernel
+    (pk_probe_read_bandwidth): 128-bit L2-only loads from every SM over a
+    buffer read 40 times, at 32 and 64 MB (both inside the 129 MB L2); the
+    larger rate is the denominator."""
+    import ctypes as C
+    rates = {}
+    for mb in (32, 64):
+        g = C.c_float(0.0)
+        ctx.call("pk_probe_read_bandwidth", mb << 20, 40, C.byref(g))
+        rates[f"{mb}MB"] = float(g.value)
+    return {"gbs": max(rates.values()), "rates": rates,
+            "source": "measured in this run: pk_probe_read_bandwidth (L2-resident read, 32/64 MB x 40)"}
+
+
 def make_scene(args):
     from pike_gb300 import synth
     return synth.displaced_sphere_scene(subdivisions=args.subdivisions, width=args.width, height=args.height,
@@ -205,10 +224,16 @@ def make_scene(args):
 
 
 # ---------------------------------------------------------------- CPU (oracle)
-def cpu_run(src, bounces: int, seconds: float, threads: int):
+def cpu_band_rows(src) -> int:
+    """Rows of the CPU sample's band: a tenth of the image, in its middle."""
+    return max(1, src.height // 10)
+
+
+def cpu_run(src, bounces: int, seconds: float, threads: int, warmup: int = 1):
     """The CPU restatement on a bounded band of the frame: frames of a batch of
     rows in the middle of the image (the reference's BATCH_SIZE/invocationOffset
-    mechanism, pike.js:133-147), repeated until `seconds` of rendering."""
+    mechanism, pike.js:133-147), `warmup` untimed band frames, then repeated
+    until `seconds` of rendering."""
     from oracle import pyoracle
     t0 = time.perf_counter()
     pos, attrs = pyoracle.flatten(src)
@@ -216,12 +241,15 @@ def cpu_run(src, bounces: int, seconds: float, threads: int):
     bvh = pyoracle.BVH(pos, src.tris)
     bvh_s = time.perf_counter() - t0
     env = pyoracle.Env(src.env_rgbe)
-    rows = max(1, src.height // 10)
+    rows = cpu_band_rows(src)
     batch = src.width * rows
     r = pyoracle.Renderer(src.width, src.height, batch=batch, threads=threads)
     r.set_scene(bvh, attrs, idx, layers)
     r.set_env(env)
     r.set_camera(src.camera_state(invocation_offset=(src.height // 2 - rows // 2) * src.width))
+    for w in range(max(warmup, 0)):  # untimed: pages in the tables, spins up the worker threads
+        r.set_render_state(1_000_000 + w)
+        r.tick_batch(bounces)
     frames, rays, elapsed = 0, 0, 0.0
     while elapsed < seconds or frames == 0:
         r.reset_stats()
@@ -236,6 +264,24 @@ def cpu_run(src, bounces: int, seconds: float, threads: int):
             "sample": f"{frames} frame(s) of a {src.width}x{rows}-pixel band ({batch} pixels, {bounces} bounces)"}
 
 
+def bench_config(args, src, world: int) -> dict:
+    """The workload description both arms print (identical keys and values):
+    what is rendered, how the GPU arm schedules it, and which band the CPU
+    sample renders."""
+    rows = cpu_band_rows(src)
+    return {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
+            "bounces": args.bounces, "env": "2048x1024 RGBE8", "parallelism": f"replicas{world}",
+            "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
+            "frame_overlap": args.trace_mode != "chunked" and (
+                args.overlap == "on" or (args.overlap == "auto" and (
+                    args.frames_in_flight == 1 or src.width * src.height < (1 << 20)))),
+            "frames_in_flight": args.frames_in_flight,
+            "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
+            "cpu_sample": f"CPU arm and cpu_baseline: band of {rows} rows x {src.width} (rows "
+                          f"{src.height // 2 - rows // 2}..{src.height // 2 - rows // 2 + rows - 1}) per frame, "
+                          f"same scene, camera and bounces; Mrays/s is per ray traced"}
+
+
 def reference_arm(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -243,18 +289,16 @@ def reference_arm(args):
     src = make_scene(args)
     threads = os.cpu_count() or 1
     per_step = max(args.cpu_seconds / max(args.steps, 1), 0.5)
-    for _ in range(args.warmup):
-        pass  # the CPU restatement has no warm-up state beyond the scene build
-    res = cpu_run(src, args.bounces, per_step * args.steps, threads)
+    res = cpu_run(src, args.bounces, per_step * args.steps, threads, warmup=max(args.warmup, 1))
     value = res["mrays"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * res["seconds"] / res["frames"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
-                   "bounces": args.bounces, "bvh_build_s": res["bvh_s"],
-                   "note": "CPU restatement of the reference path (oracle); the reference is JavaScript+WGSL "
-                           "on WebGPU, which cannot run on this machine"},
+        "config": bench_config(args, src, dist_env()[1]),
+        "measured": {"bvh_build_s": res["bvh_s"], "band_frames": res["frames"], "warmup_band_frames": max(args.warmup, 1),
+                     "note": "CPU restatement of the reference path (oracle); the reference is JavaScript+WGSL "
+                             "on WebGPU, which cannot run on this machine"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": res["sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -779,34 +823,39 @@ def gpu_arm(args):
     npix = src.width * src.height
     spp_mpix = world * args.steps * npix / (ms_max / 1000.0) / 1e6
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: host wall clock from
+    # before the first call to after pk_sync has waited for the last frame and
+    # the last image copy (device events bracket the same loop for reference)
     e2e_steps = args.steps
     img = ctx.pinned((src.height, src.width, 4), "uint8")
     h2d = C.sizeof(cam) + 8
     ctx.call("pk_reset_stats")
     D.barrier()
     ctx.call("pk_sync")
+    t_host0 = time.perf_counter()
     ctx.timer_start()
     for s in range(e2e_steps):
         ctx.call("pk_set_render_state", first_sample + s, 0.0)
         ctx.call("pk_set_camera", cam)
         ctx.call("pk_render_frame", B)
         ctx.call("pk_read_display_async", img.array.ctypes.data_as(C.c_void_p))
-    e2e_ms = ctx.timer_stop()
+    e2e_dev_ms = ctx.timer_stop()
+    ctx.call("pk_sync")
+    e2e_ms = 1000.0 * (time.perf_counter() - t_host0)
     e2e_rays = read_stats(ctx)["rays_traced"]
     e2e_ms_max = D.max(e2e_ms)
     e2e_value = D.sum(float(e2e_rays)) / (e2e_ms_max / 1000.0) / 1e6
     img.free()
-    ctx.call("pk_sync")
     forms = None
     if rank == 0 and args.trace_mode != "wide" and not args.no_forms:
         forms = {"wide_bvh": wide_form(ctx, args, B, first_sample, mode)}
         forms["adjoint"] = adjoint_form(args, local)
         forms["batching"] = batch_form(args, local)
         forms["binned_bvh"] = binned_form(ctx, args, B, first_sample, bvh_ms)
-        if args.precision:
+        if not args.no_precision:
             forms["precision_soup"] = precision_form(args, local)
 
+    l2 = l2_peak(ctx) if rank == 0 else None
     if rank == 0:
         peak, peak_kind = load_peak_hbm()
         tr = kt["trace"]
@@ -819,6 +868,9 @@ def gpu_arm(args):
         achieved = alg_bytes_launch / (trace_ms / 1000.0) / 1e9
         traffic = profiled_traffic()
         total_ms = sum(v["ms"] for v in kt.values())
+        measured = {"spp_mpix_per_s": spp_mpix, "spp_per_s": spp_mpix / (npix / 1e6),
+                    "rays_per_step": rays_local / args.steps, "bvh_build_ms": bvh_ms,
+                    "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}}
         # k_set_state, k_camera, per bounce {closest trace, compaction, shade, shadow trace},
         # k_accumulate, k_postprocess, k_end_frame
         launches_per_frame = 4 * B + 5
@@ -826,23 +878,24 @@ def gpu_arm(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "triangles": src.n_tris, "resolution": f"{src.width}x{src.height}",
-                       "bounces": B, "env": "2048x1024 RGBE8", "spp_mpix_per_s": spp_mpix,
-                       "spp_per_s": spp_mpix / (npix / 1e6), "rays_per_step": rays_local / args.steps,
-                       "bvh_build_ms": bvh_ms, "parallelism": f"replicas{world}", "trace_mode": args.trace_mode, "node_record_bytes": args.node_records,
-                       "frame_overlap": args.trace_mode != "chunked" and (
-                           args.overlap == "on" or (args.overlap == "auto" and (
-                               args.frames_in_flight == 1 or src.width * src.height < (1 << 20)))),
-                       "frames_in_flight": args.frames_in_flight,
-                       "l2": "working set > L2 (BVH+triangles 150 MB, ray queues 400 MB); no flush between steps",
-                       "kernel_share": {k: round(v["ms"] / total_ms, 4) for k, v in kt.items() if total_ms}},
+            "config": bench_config(args, src, world),
+            "measured": measured,
             "roofline": {"bound": "hbm", "kernel": "closest-hit traversal (trace.wgsl + fused shade_miss)", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
-                         "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes_launch,
+                         "peak_l2": l2["gbs"] if l2 else None,
+                         "frac_l2": achieved / l2["gbs"] if l2 and l2["gbs"] else None,
+                         "peak_l2_source": l2["source"] if l2 else None,
+                         "traffic": traffic,
+                         "traffic_source": "carried over: profiles/trace_closest_dram.txt, an ncu capture of this "
+                                           "workload's closest-hit launches (dram__bytes_read.sum + "
+                                           "dram__bytes_write.sum per launch); not measured in this run",
+                         "algorithmic_bytes_per_launch": alg_bytes_launch,
                          "launch_ms": trace_ms,
                          "bytes_model": f"{node_bytes}*node_fetch + 52*tri_test + 48*ray + 64*hit + 48*miss"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": src.width * src.height * 4, "steps": e2e_steps},
+                    "d2h_bytes_per_step": src.width * src.height * 4, "steps": e2e_steps,
+                    "timing": "host perf_counter around the calls plus the final pk_sync",
+                    "device_ms": e2e_dev_ms},
             "gpu_launches": launches_per_frame * args.steps,
             "clocks": clk,
             "counts_per_frame": counts,
@@ -850,7 +903,7 @@ def gpu_arm(args):
         if forms:
             line["forms"] = forms
         if world == 1 and not args.no_cpu_baseline:
-            res = cpu_run(src, B, args.cpu_seconds, os.cpu_count() or 1)
+            res = cpu_run(src, B, args.cpu_seconds, os.cpu_count() or 1, warmup=1)
             line["cpu_baseline"] = {"value": res["mrays"], "unit": UNIT, "cores": os.cpu_count() or 1,
                                     "kind": "port", "sample": res["sample"], "bvh_build_s": res["bvh_s"]}
         print(json.dumps(line))

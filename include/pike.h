@@ -188,7 +188,12 @@ int pk_render_frames(pk_ctx* ctx, uint32_t frames, uint32_t bounces);
  * float4 each (xyz used, normalised frame); hits4: n * {t bits, triangle index
  * or 0xffffffff, bary_mask, 0}; hit_index: the indices of the rays that hit,
  * increasing; n_hits: one u32 (device).  Runs on the context's stream and
- * returns when the results are written. */
+ * returns when the results are written.  Always traverses the drop-in's
+ * snorm16 node records, whatever pk_set_trace_mode selected.  Any hit reports
+ * the closest triangle of the first leaf that has a hit, as trace_shadow.wgsl
+ * does (its :154-158); the render passes' any-hit traversal only needs
+ * visibility and stops at the first accepted triangle of that leaf (same
+ * occluded/unoccluded answer, possibly another triangle). */
 int pk_cast_rays(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit, uint32_t* hits4,
                  uint32_t* hit_index, uint32_t* n_hits);
 /* pk_cast_rays without any device allocation.  No counterpart in the reference.
@@ -199,10 +204,11 @@ int pk_cast_rays(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t
  * makes no cudaMalloc/cudaFree call: its scratch is a 132,352-byte static
  * device array that every GPU loading the library keeps until the process
  * exits.  Limit: at most 1,048,576 rays per call (more returns PK_ERR_ARG).
- * The first call on a device looks up that array's address, so make it before
- * any stream capture.  All calls share the array (each call re-zeroes what must
- * start at zero): calls that overlap on the GPU race.  Same arguments and
- * results as pk_cast_rays. */
+ * pk_create looks up that array's device address (with the context's device
+ * current) and the context keeps it, so it lives as long as the context.  All
+ * calls share the array (each call re-zeroes what must start at zero): calls
+ * that overlap on the GPU race.  Same arguments and results as pk_cast_rays;
+ * like it, the call synchronises the context's stream before it returns. */
 int pk_cast_rays_noalloc(pk_ctx* ctx, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
                          uint32_t* hits4, uint32_t* hit_index, uint32_t* n_hits);
 
@@ -279,6 +285,12 @@ int pk_read_timing(pk_ctx* ctx, float out16[16]);
 /* CUDA events on the context's stream: op 0 records the start event, op 1
  * records the stop event, waits for it and returns the elapsed milliseconds. */
 int pk_stream_timer(pk_ctx* ctx, int op, float* ms);
+/* Read-bandwidth probe for the roofline denominators (no reference
+ * counterpart): reads a zero-filled device buffer of `bytes` reps times with
+ * 128-bit L2-only loads from every SM (after one untimed pass) and returns GB/s.
+ * A buffer well inside the 129 MB L2 measures the L2 read rate.  Allocates the
+ * buffer for the duration of the call. */
+int pk_probe_read_bandwidth(pk_ctx* ctx, uint64_t bytes, uint32_t reps, float* gbs);
 /* Page-locked host memory for the asynchronous readback below. */
 int pk_host_alloc(pk_ctx* ctx, size_t bytes, void** out);
 int pk_host_free(pk_ctx* ctx, void* p);

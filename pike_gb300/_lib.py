@@ -90,7 +90,8 @@ def load(path: str = LIB_PATH):
         "pk_read_display": [_P, _P, _P], "pk_set_counting": [_P, C.c_int], "pk_reset_stats": [_P],
         "pk_read_stats": [_P, _P], "pk_set_timing": [_P, C.c_int], "pk_read_timing": [_P, _P],
         "pk_math_eval": [_P, C.c_int, _P, _P, _P, u32],
-        "pk_stream_timer": [_P, C.c_int, C.POINTER(C.c_float)], "pk_host_alloc": [_P, C.c_size_t, C.POINTER(_P)],
+        "pk_stream_timer": [_P, C.c_int, C.POINTER(C.c_float)],
+        "pk_probe_read_bandwidth": [_P, C.c_uint64, u32, C.POINTER(C.c_float)], "pk_host_alloc": [_P, C.c_size_t, C.POINTER(_P)],
         "pk_host_free": [_P, _P], "pk_read_display_async": [_P, _P],
         "pk_cast_rays": [_P, _P, _P, u32, C.c_int, _P, _P, _P],
         "pk_cast_rays_noalloc": [_P, _P, _P, u32, C.c_int, _P, _P, _P],

@@ -172,6 +172,7 @@ int pk_create(pk_ctx** out, int device) {
     }
     c->ctr.alloc(1);
     c->cam.alloc(1);
+    c->cast_scratch = noalloc_scratch_address();
     check(cudaMemsetAsync(c->ctr.p, 0, sizeof(Counters), c->stream), "memset");
     check(cudaStreamSynchronize(c->stream), "sync");
     return PK_OK;

@@ -105,7 +105,7 @@ int pk_batch_create(pk_batch** out, pk_ctx* const* scenes, uint32_t n_scenes) {
         return bfail(b, PK_ERR_STATE, "every scene needs a BVH, materials and an environment");
       const LaunchCtx L = c->launch();
       b->ctxs.push_back(c);
-      b->scenes.push_back(BatchScene{L.scene, L.env, 0.0f});
+      b->scenes.push_back(BatchScene{c->dropin_scene(), L.env, 0.0f});
     }
     check(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device), "attr");
     check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");

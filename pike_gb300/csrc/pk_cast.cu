@@ -6,7 +6,6 @@
 
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/pike.h"
 #include "pk_ctx.h"
@@ -111,6 +110,7 @@ int cast_enqueue(pk_ctx* c, const float4* o4, const float4* d4, uint32_t n, int 
   check(cudaMemsetAsync(s.tickets, 0, 16, stream), "memset");
   if (cast_tiles(n)) check(cudaMemsetAsync(s.tiles, 0, cast_tiles(n) * 8, stream), "memset");
   LaunchCtx L = c->launch();
+  L.scene = c->dropin_scene();  // the drop-in's records whatever the trace mode
   const unsigned warps = (unsigned)((n + 31) / 32);
   const unsigned grid = std::max(1u, std::min(L.trace_blocks, (warps + CAST_THREADS / 32 - 1) / (CAST_THREADS / 32)));
   if (n) {
@@ -172,25 +172,20 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_TILES_OFF + NOALLOC_TILES * 8;  // 132,
 
 static __device__ __align__(256) unsigned char g_cast_scratch[NOALLOC_BYTES];
 
-std::mutex g_scratch_mu;
-constexpr int MAX_DEVICES = 256;
-void* g_scratch_addr[MAX_DEVICES] = {};
+}  // namespace
 
 // The array's device address on the current device.  In host code the name
-// g_cast_scratch is only a host-side stand-in, so the address is looked up once
-// per device (with that device current) and cached.
-unsigned char* noalloc_scratch(int device) {
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (device < 0 || device >= MAX_DEVICES) throw CudaError("pk_cast_rays_noalloc: device id out of range");
-  if (!g_scratch_addr[device]) {
-    void* p = nullptr;
-    check(cudaGetSymbolAddress(&p, g_cast_scratch), "cudaGetSymbolAddress(g_cast_scratch)");
-    g_scratch_addr[device] = p;
-  }
-  return static_cast<unsigned char*>(g_scratch_addr[device]);
+// g_cast_scratch is only a host-side stand-in, not a device address, so
+// pk_create looks the address up once, with the context's device current, and
+// keeps it in the context: it stays valid exactly as long as the context's
+// other device memory (a device reset invalidates both; the next pk_create
+// looks it up again).
+void* noalloc_scratch_address() {
+  void* p = nullptr;
+  check(cudaGetSymbolAddress(&p, g_cast_scratch), "cudaGetSymbolAddress(g_cast_scratch)");
+  return p;
 }
 
-}  // namespace
 }  // namespace pk
 
 extern "C" int pk_cast_rays_noalloc(pk_ctx* c, const float* ray_o4, const float* ray_d4, uint32_t n, int any_hit,
@@ -207,7 +202,8 @@ extern "C" int pk_cast_rays_noalloc(pk_ctx* c, const float* ray_o4, const float*
       c->err = "pk_cast_rays_noalloc: at most 1048576 rays per call (the size of its static scratch)";
       return PK_ERR_ARG;
     }
-    unsigned char* base = noalloc_scratch(c->device);
+    if (!c->cast_scratch) { c->err = "pk_cast_rays_noalloc: scratch address not set up"; return PK_ERR_STATE; }
+    unsigned char* base = static_cast<unsigned char*>(c->cast_scratch);
     const CastScratch s{reinterpret_cast<uint32_t*>(base), reinterpret_cast<uint32_t*>(base + NOALLOC_FLAGS_OFF),
                         reinterpret_cast<unsigned long long*>(base + NOALLOC_TILES_OFF)};
     cast_enqueue(c, reinterpret_cast<const float4*>(ray_o4), reinterpret_cast<const float4*>(ray_d4), n, any_hit,

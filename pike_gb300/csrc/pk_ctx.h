@@ -57,6 +57,10 @@ struct FrameSlot {
   }
 };
 
+// Device address of pk_cast_rays_noalloc's static scratch array on the
+// current device (pk_cast.cu).
+void* noalloc_scratch_address();
+
 }  // namespace pk
 
 struct pk_ctx {
@@ -153,6 +157,7 @@ struct pk_ctx {
   float kind_n[pk::N_KINDS] = {0};
   unsigned long long frames = 0;
   unsigned long long diff_rays = 0;  // rays of the last differentiable render / adjoint
+  void* cast_scratch = nullptr;  // pk_cast_rays_noalloc's static scratch on this device (set by pk_create)
 
   RayQ R(int i) { return slot[0].R(i); }
   RayQ S() { return slot[0].S(); }
@@ -188,6 +193,18 @@ struct pk_ctx {
     L.shade_blocks = g_shade;
     L.trace_mode = trace_mode;
     return L;
+  }
+  // The drop-in's traversal records (the reference's snorm16 boxes and root),
+  // whatever the trace mode.  The ray-query, batch and differentiable kernels
+  // use the drop-in's box test and strict `<` hit test, which are defined on
+  // these records only; PK_TRACE_EXACT's outward-rounded records need the
+  // slack and (t, slot) ties of the exact traversal.
+  pk::SceneDev dropin_scene() {
+    pk::SceneDev s = launch().scene;
+    s.inner = inner.p;
+    s.inner32 = compact_nodes ? inner32.p : nullptr;
+    s.root = root;
+    return s;
   }
   cudaEvent_t take_event() {
     if (!event_pool.empty()) {

@@ -340,7 +340,7 @@ extern "C" int pk_diff_render(pk_ctx* c, const pk_diff_camera* cam, const pk_dif
     check(cudaMemsetAsync(rays.p, 0, 8, c->stream), "memset");
     const uint32_t n = c->W * c->H;
     k_diff_forward<<<(n + DIFF_THREADS - 1) / DIFF_THREADS, DIFF_THREADS, 0, c->stream>>>(
-        c->launch().scene, dc, dp, c->W, c->H, reinterpret_cast<float4*>(image4), err.p, rays.p);
+        c->dropin_scene(), dc, dp, c->W, c->H, reinterpret_cast<float4*>(image4), err.p, rays.p);
     check(cudaGetLastError(), "k_diff_forward");
     uint32_t herr = 0;
     unsigned long long hr = 0;
@@ -375,7 +375,7 @@ extern "C" int pk_diff_backward(pk_ctx* c, const pk_diff_camera* cam, const pk_d
     if (smem > 48 * 1024)
       check(cudaFuncSetAttribute(k_diff_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
     k_diff_adjoint<<<(n + DIFF_THREADS - 1) / DIFF_THREADS, DIFF_THREADS, smem, c->stream>>>(
-        c->launch().scene, dc, dp, c->W, c->H, reinterpret_cast<const float4*>(d_image4), g_albedo3, g_roughness,
+        c->dropin_scene(), dc, dp, c->W, c->H, reinterpret_cast<const float4*>(d_image4), g_albedo3, g_roughness,
         g_env_rgb, err.p, rays.p);
     check(cudaGetLastError(), "k_diff_adjoint");
     uint32_t herr = 0;

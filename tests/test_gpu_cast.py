@@ -85,3 +85,24 @@ def test_focus_distance_matches_raycaster(oracle, pk_built):
         assert np.float64(t.value).view(np.uint64) == np.float64(want[i]).view(np.uint64), i
         assert fd.value == 1.0 - 1.0 / t.value
     assert (want < 1e6).any() and (want == 1e6).any()
+
+
+@pytest.mark.parametrize("mode_name", ["PK_TRACE_EXACT", "PK_TRACE_WIDE", "PK_TRACE_COMPACT_RECORDS"])
+def test_cast_rays_ignore_the_trace_mode(oracle, pk_built, mode_name):
+    """Ray queries traverse the drop-in's records whatever the context's trace
+    mode selects for the render passes: after switching the mode (which builds
+    the outward-rounded binary records or the 8-wide BVH) the hits still equal
+    the oracle's trace.wgsl / trace_shadow.wgsl answers bit for bit."""
+    from pike_gb300 import _lib
+    src = synth.displaced_sphere_scene(subdivisions=5, width=16, height=16, env_size=(64, 32))
+    pair = Pair(src, oracle)
+    pair.ctx.call("pk_set_trace_mode", _lib.PK_TRACE_PERSISTENT | getattr(_lib, mode_name))
+    o, d = query_rays(src, 50_000, 21)
+    rays8 = np.concatenate([o, d], axis=1)
+    for any_hit in (False, True):
+        hits, idx = cast(pair.ctx, o, d, any_hit)
+        ref = pair.P.r.trace_rays(rays8, any_hit=any_hit)
+        hit = ref[:, 1] != 0xFFFFFFFF
+        assert np.array_equal(hits[:, 1], ref[:, 1])
+        assert np.array_equal(hits[hit, 0], ref[hit, 0])
+        assert np.array_equal(idx, np.flatnonzero(hit).astype(np.uint32))

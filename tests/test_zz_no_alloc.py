@@ -66,6 +66,30 @@ def test_noalloc_matches_allocating_query_twice(pk_built):
         assert np.array_equal(i, i_ref)
 
 
+def test_noalloc_leaves_device_memory_unchanged(pk_built):
+    """Free device memory is the same before and after each call (after a
+    warm-up call): device memory the entry point kept would show as a drop."""
+    torch = pytest.importorskip("torch")
+    ctx = _scene_context()
+    n = 300_000
+    o, d = _rays(n, 13)
+    to, td = torch.from_numpy(o).cuda(), torch.from_numpy(d).cuda()
+    hits = torch.zeros((n, 4), dtype=torch.int32, device="cuda")
+    idx = torch.zeros((n,), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    args = [C.c_void_p(to.data_ptr()), C.c_void_p(td.data_ptr()), n, 0, C.c_void_p(hits.data_ptr()),
+            C.c_void_p(idx.data_ptr()), C.c_void_p(cnt.data_ptr())]
+    torch.cuda.synchronize()
+    ctx.call("pk_cast_rays_noalloc", *args)  # warm-up
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        ctx.call("pk_cast_rays_noalloc", *args)
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0
+    assert int(cnt.item()) > 0
+
+
 def test_noalloc_rejects_more_rays_than_its_scratch(pk_built):
     torch = pytest.importorskip("torch")
     ctx = _scene_context()
