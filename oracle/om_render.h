@@ -99,6 +99,12 @@ struct Renderer {
   // running mean (accumulate.wgsl in double) and Welford moments of the
   // per-frame colour since set_track64.
   bool track64 = false;
+  // With share_texels, the FP64 evaluation takes the texel indices of the
+  // two nearest-texel lookups (envPdf's pdf texel for the bounce MIS weight,
+  // envColor's texel on a miss) from the FP32 evaluation, and keeps its own
+  // FP64 arithmetic everywhere else.  A texel choice is a discontinuous
+  // function of the direction: near a texel boundary any rounding flips it.
+  bool share_texels = false;
   std::vector<double> ray64, hit64, miss64, color64, accum64, mean64, m2_64;
   uint64_t frames64 = 0;
   void alloc64() {
@@ -111,9 +117,25 @@ struct Renderer {
     m2_64.assign(4 * (size_t)W * H, 0.0);
     frames64 = 0;
   }
-  void set_track64(bool on) {
+  void set_track64(bool on, bool shared_texels = false) {
     track64 = on;
+    share_texels = on && shared_texels;
     if (on) alloc64();
+  }
+  // envPdf's (shade_hit.wgsl:202-210) and envColor's (shade_miss.wgsl:37-43)
+  // texel indices as the FP32 passes compute them for direction d.
+  void pdf_texel_index32(V3 dir, int32_t* cx, int32_t* cy) const {
+    float a = 1.0f + env_theta + atan2_(dir.z, dir.x) / TAU_F;
+    float u = a - std::trunc(a);
+    float v = acos_(dir.y) * INV_PI_F;
+    *cx = f2i(u * (float)env_w);
+    *cy = f2i(v * (float)env_h);
+  }
+  void color_texel_index32(V3 dir, int32_t* x, int32_t* y) const {
+    float u = env_theta + atan2_(dir.z, dir.x) / TAU_F;
+    float v = acos_(dir.y) * INV_PI_F;
+    *x = f2i(std::floor(u * (float)env_w));
+    *y = f2i(std::floor(v * (float)env_h));
   }
 
   // Queues hold the camera dispatch of a batch, rounded up to 128 invocations
@@ -722,11 +744,13 @@ struct Renderer {
     return (double)env_pdf[(size_t)x + (size_t)env_w * (size_t)y];
   }
   static double acos_clamped(double y) { return std::acos(y < -1.0 ? -1.0 : (y > 1.0 ? 1.0 : y)); }
-  double env_pdf_dir64(D3 dir) const {
+  // texel32: the FP32 direction whose texel is used (share_texels), or null
+  double env_pdf_dir64(D3 dir, const V3* texel32 = nullptr) const {
     const double a = 1.0 + (double)env_theta + std::atan2(dir.z, dir.x) / TAU_D;
     const double u = a - std::trunc(a);
     const double v = acos_clamped(dir.y) / PI_D;
-    const int32_t cx = (int32_t)(u * (double)env_w), cy = (int32_t)(v * (double)env_h);
+    int32_t cx = (int32_t)(u * (double)env_w), cy = (int32_t)(v * (double)env_h);
+    if (texel32) pdf_texel_index32(*texel32, &cx, &cy);
     return pdf_texel64(cx, cy) / std::sin(v * PI_D);
   }
   Sample64 sample_env64(Hash& h, const SI64& si) const {
@@ -741,10 +765,11 @@ struct Renderer {
     const D3 dir = d3(std::cos(theta) * sp, std::cos(phi), std::sin(theta) * sp);
     return Sample64{vecmat(dir, si.b1, si.b2, si.n), pdf_texel64(cx, cy) / sp};
   }
-  D3 env_color64(D3 dir) const {
+  D3 env_color64(D3 dir, const V3* texel32 = nullptr) const {
     const double u = (double)env_theta + std::atan2(dir.z, dir.x) / TAU_D;
     const double v = acos_clamped(dir.y) / PI_D;
     int32_t x = (int32_t)std::floor(u * (double)env_w), y = (int32_t)std::floor(v * (double)env_h);
+    if (texel32) color_texel_index32(*texel32, &x, &y);
     x = ((x % (int32_t)env_w) + (int32_t)env_w) % (int32_t)env_w;
     y = ((y % (int32_t)env_h) + (int32_t)env_h) % (int32_t)env_h;
     const uint8_t* c = &env_rgbe[4 * ((size_t)y * env_w + (size_t)x)];
@@ -789,7 +814,10 @@ struct Renderer {
       bsdf = eval_specular64(si, bs);
     }
     if (o.bounce) {
-      const double w = sample_env_light ? power_heuristic64(bs.pdf, env_pdf_dir64(matvec(si.b1, si.b2, si.n, bs.wi))) : 1.0;
+      const V3 dir32 = v3(o.bounce_ray.d[0], o.bounce_ray.d[1], o.bounce_ray.d[2]);
+      const double w = sample_env_light ? power_heuristic64(bs.pdf, env_pdf_dir64(matvec(si.b1, si.b2, si.n, bs.wi),
+                                                                                  share_texels ? &dir32 : nullptr))
+                                        : 1.0;
       r.bounce[0] = bsdf.x * ctp[0] * w;
       r.bounce[1] = bsdf.y * ctp[1] * w;
       r.bounce[2] = bsdf.z * ctp[2] * w;
@@ -833,7 +861,8 @@ struct Renderer {
       float c[4] = {res[j].x * r.tp[0], res[j].y * r.tp[1], res[j].z * r.tp[2], 1.0f};
       add_color(f2u(r.tp[3]) & 0x0fffffffu, c);
       if (track64) {
-        const D3 e = env_color64(d3f(r.d));
+        const V3 dir32 = v3(r.d[0], r.d[1], r.d[2]);
+        const D3 e = env_color64(d3f(r.d), share_texels ? &dir32 : nullptr);
         const double* t = &miss64[3 * (size_t)j];
         const double c64[3] = {e.x * t[0], e.y * t[1], e.z * t[2]};
         add_color64(f2u(r.tp[3]) & 0x0fffffffu, c64);

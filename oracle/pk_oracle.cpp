@@ -301,7 +301,8 @@ void or_set_canonical(void* p, int on) { ((Renderer*)p)->canonical = on != 0; }
 // FP64 companion (om_render64.h): which = 0 the FP64 accumulation
 // (accumulate.wgsl in double), 1 the mean and 2 the sum of squared deviations
 // of the per-frame FP64 colours since or_set_track64; W*H*4 doubles.
-void or_set_track64(void* p, int on) { ((Renderer*)p)->set_track64(on != 0); }
+// on: 0 off, 1 FP64 evaluation, 2 FP64 evaluation with the FP32 texel choices
+void or_set_track64(void* p, int on) { ((Renderer*)p)->set_track64(on != 0, on == 2); }
 uint64_t or_frames64(void* p) { return ((Renderer*)p)->frames64; }
 int or_read64(void* p, int which, double* out) {
   Renderer* r = (Renderer*)p;

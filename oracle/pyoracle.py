@@ -302,10 +302,13 @@ class Renderer:
                            _p(gr), _p(ge))
         return ga, gr, ge
 
-    def set_track64(self, on: bool = True):
+    def set_track64(self, on: bool = True, share_texels: bool = False):
         """FP64 companion: every ray also carries an FP64 throughput and every
-        contribution is recomputed in FP64 along the same paths (om_render64.h)."""
-        lib().or_set_track64(self.p, C.c_int(1 if on else 0))
+        contribution is recomputed in FP64 along the same paths (om_render64.h).
+        share_texels: the two nearest-texel lookups (the env pdf texel of the
+        bounce MIS weight, the env texel of a miss) use the FP32 evaluation's
+        texel indices, isolating the arithmetic error from texel flips."""
+        lib().or_set_track64(self.p, C.c_int((2 if share_texels else 1) if on else 0))
 
     def _read64(self, which: int) -> np.ndarray:
         out = np.zeros((self.h, self.w, 4), np.float64)
