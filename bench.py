@@ -357,10 +357,11 @@ def read_timing(ctx):
     return {k: {"ms": float(t[i]), "launches": int(t[8 + i])} for i, k in enumerate(kinds)}
 
 
-def hit_agreement(ctx, mode_a: int, mode_b: int, bounces: int = 2):
+def hit_agreement(ctx, mode_a: int, mode_b: int, bounces: int = 2, full: bool = True):
     """Per-ray closest-hit agreement of two traversal modes on the pass path
     (camera rays, then bounce rays shaded from mode_b's hits): rays whose
-    {t, slot, barycentrics} differ, out of all rays traced."""
+    {t, slot, barycentrics} differ (full) or whose hit triangle id differs,
+    out of all rays traced."""
     import numpy as np
     from pike_gb300 import _lib
     from pike_gb300._lib import ptr
@@ -390,7 +391,8 @@ def hit_agreement(ctx, mode_a: int, mode_b: int, bounces: int = 2):
         ka, va = hit_rows(mode_a)
         kb, vb = hit_rows(mode_b)
         common, ia, ib = np.intersect1d(ka, kb, assume_unique=True, return_indices=True)
-        differ += (ka.size - common.size) + (kb.size - common.size) + int((va[ia] != vb[ib]).any(axis=1).sum())
+        cols = slice(0, 3) if full else slice(1, 2)
+        differ += (ka.size - common.size) + (kb.size - common.size) + int((va[ia, cols] != vb[ib, cols]).any(axis=1).sum())
         for name in ("shade_hit", "trace_shadow", "shade_miss"):
             ctx.call("pk_" + name)
     return total, differ
@@ -484,7 +486,7 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
     ctx.call("pk_render_frames", steps, B)
     ms = ctx.timer_stop()
     rays = read_stats(ctx)["rays_traced"]
-    total, differ = hit_agreement(ctx, plain_mode, wide_mode)
+    total, differ = hit_agreement(ctx, plain_mode, wide_mode, full=False)
     # the FP32 binary reference of form (1): same tree, outward-rounded FP32 boxes, (t, slot) ties
     exact_mode = _lib.PK_TRACE_PERSISTENT | _lib.PK_TRACE_EXACT
     etotal, ediffer = hit_agreement(ctx, exact_mode, wide_mode)
@@ -511,11 +513,14 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
             "closest_hit_launch_ms": tr["ms"] / max(tr["launches"], 1), "wide_build_ms": build_ms,
             "wide_nodes_per_ray": counts["closest_fetch"] / R, "tri_tests_per_ray": counts["closest_tests"] / R,
             "shadow_wide_nodes_per_ray": counts["shadow_fetch"] / max(counts["shadow_rays"], 1),
-            "node_bytes": 96,
+            "node_bytes": 80,
             "closest_hit_agreement": {"rays": total, "differ": differ, "fraction_equal": 1.0 - differ / max(total, 1),
+                                      "compared": "hit triangle id (the drop-in uses Moller-Trumbore, form (1) "
+                                                  "the watertight test)",
                                       "note": "camera + first bounce rays, pass path; differing rays are the "
-                                              "drop-in's truncated-box misses and t ties (the wide result "
-                                              "equals brute force, tests/test_gpu_wide.py)"},
+                                              "drop-in's truncated-box misses, t ties and edge hits where the "
+                                              "two triangle tests disagree (the wide result equals brute "
+                                              "force, tests/test_gpu_wide.py)"},
             "fp32_binary": {"value": erays / (ems / 1000.0) / 1e6, "unit": UNIT, "ms_per_step": ems / steps,
                             "node_bytes": 64,
                             "fetch_units_per_ray": ecounts["closest_fetch"] / max(ecounts["closest_rays"], 1),
@@ -705,6 +710,66 @@ def binned_form(ctx, args, B: int, first_sample: int, sweep_ms: float):
             "ms_per_step": ms / steps, "note": "binned SAH, 16 bins, leaves <= 8; frames differ from the reference's"}
 
 
+def alias_env_form(args, local: int):
+    """Form (1)'s alias-table environment sampling (PK_ENV_ALIAS) against the
+    reference's equal-mass histogram on the benchmark scene: the shade
+    kernel's launch time at 1920x1080 (pk_set_timing, one frame at a time),
+    and the per-pixel variance of 32 single-sample frames at 480x270 (relative
+    variance var/mean^2, averaged over lit pixels; same seeds in both modes)."""
+    import numpy as np
+    from pike_gb300 import _lib
+    from pike_gb300._lib import ptr
+    out = {"workload": "icosphere8+openbox, 2048x1024 env; shade timing at 1920x1080 (8 bounces), "
+                       "variance over 32 frames at 480x270"}
+    src = make_scene(args)
+    ctx, _ = setup_context(src, local)
+    ctx.call("pk_set_camera", camera_struct(src))
+    ctx.call("pk_set_frames_in_flight", 1)
+    B = args.bounces
+    for name, mode in (("histogram", _lib.PK_ENV_HISTOGRAM), ("alias", _lib.PK_ENV_ALIAS)):
+        ctx.call("pk_sync")
+        ctx.timer_start()
+        ctx.call("pk_set_env_sampling", mode)
+        build_ms = ctx.timer_stop()
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_render_frames", 2, B)
+        ctx.call("pk_reset_stats")
+        ctx.call("pk_set_timing", 1)
+        ctx.call("pk_set_render_state", 0, 0.0)
+        ctx.call("pk_render_frames", 4, B)
+        ctx.call("pk_sync")
+        kt = read_timing(ctx)
+        ctx.call("pk_set_timing", 0)
+        sh = kt["shade"]
+        out[name] = {"shade_launch_ms": sh["ms"] / max(sh["launches"], 1), "table_build_ms": build_ms}
+    ctx.close()
+    small = make_scene(argparse.Namespace(subdivisions=args.subdivisions, width=480, height=270, bounces=B))
+    ctx, _ = setup_context(small, local)
+    ctx.call("pk_set_camera", camera_struct(small))
+    frames = 32
+    for name, mode in (("histogram", _lib.PK_ENV_HISTOGRAM), ("alias", _lib.PK_ENV_ALIAS)):
+        ctx.call("pk_set_env_sampling", mode)
+        ctx.call("pk_set_render_state", 0, 0.0)
+        s1 = s2 = 0.0
+        col = np.zeros((small.height, small.width, 4), np.float32)
+        for _ in range(frames):
+            ctx.call("pk_render_frames", 1, B)
+            ctx.call("pk_read_color", ptr(col))
+            c = np.maximum(col[..., :3].astype(np.float64), 0.0)
+            s1 = s1 + c
+            s2 = s2 + c * c
+        m = s1 / frames
+        var = np.maximum(s2 / frames - m * m, 0.0) * frames / (frames - 1)
+        lit = m > 1e-6
+        out[name]["mean_relative_variance"] = float((var[lit] / m[lit] ** 2).mean())
+        out[name]["image_mean"] = float(m.mean())
+    ctx.close()
+    h, a = out["histogram"], out["alias"]
+    out["variance_ratio_alias_over_histogram"] = a["mean_relative_variance"] / h["mean_relative_variance"]
+    out["shade_time_ratio_alias_over_histogram"] = a["shade_launch_ms"] / h["shade_launch_ms"]
+    return out
+
+
 def precision_form(args, local: int):
     """Form (1)'s precision workload: the 8,388,608-triangle soup with the
     2048x1024 env at 1920x1080, depth 4: drop-in, FP32 binary reference and
@@ -742,8 +807,8 @@ def precision_form(args, local: int):
         rays = read_stats(ctx)["rays_traced"]
         R = max(cnt["closest_rays"], 1)
         # bytes per fetch unit: the drop-in counts three 20-byte reference nodes per
-        # inner step (one 64-byte record here), the wide traversal one 96-byte node
-        node_bytes = {"dropin": 20.0, "fp32_binary": 64.0 / 3.0, "wide": 96.0}[name]
+        # inner step (one 64-byte record here), the wide traversal one 80-byte node
+        node_bytes = {"dropin": 20.0, "fp32_binary": 64.0 / 3.0, "wide": 80.0}[name]
         out[name] = {"value": rays / (ms / 1000.0) / 1e6, "unit": UNIT, "ms_per_frame": ms / 4,
                      "structure_ms": prep_ms, "fetch_per_closest_ray": cnt["closest_fetch"] / R,
                      "tests_per_closest_ray": cnt["closest_tests"] / R,
@@ -753,8 +818,10 @@ def precision_form(args, local: int):
     wide, exact, plain = modes["wide"], modes["fp32_binary"], modes["dropin"]
     t, d = hit_agreement(ctx, exact, wide)
     out["agreement_fp32_binary_vs_wide"] = {"rays": t, "differ": d, "fraction_equal": 1.0 - d / max(t, 1)}
-    t, d = hit_agreement(ctx, plain, wide)
-    out["agreement_dropin_vs_wide"] = {"rays": t, "differ": d, "fraction_equal": 1.0 - d / max(t, 1)}
+    t, d = hit_agreement(ctx, plain, wide, full=False)
+    out["agreement_dropin_vs_wide"] = {"rays": t, "differ": d, "fraction_equal": 1.0 - d / max(t, 1),
+                                       "compared": "hit triangle id (t and barycentrics come from different "
+                                                   "triangle tests)"}
     ctx.close()
     return out
 
@@ -852,6 +919,7 @@ def gpu_arm(args):
         forms["adjoint"] = adjoint_form(args, local)
         forms["batching"] = batch_form(args, local)
         forms["binned_bvh"] = binned_form(ctx, args, B, first_sample, bvh_ms)
+        forms["alias_env"] = alias_env_form(args, local)
         if not args.no_precision:
             forms["precision_soup"] = precision_form(args, local)
 
@@ -861,7 +929,7 @@ def gpu_arm(args):
         tr = kt["trace"]
         trace_ms = tr["ms"] / max(tr["launches"], 1)
         R, H = counts["closest_rays"], counts["closest_hits"]
-        node_bytes = 96 if args.trace_mode == "wide" else 20
+        node_bytes = 80 if args.trace_mode == "wide" else 20
         alg_bytes_frame = (node_bytes * counts["closest_fetch"] + 52 * counts["closest_tests"] + 48 * R + 64 * H
                            + 48 * (R - H))
         alg_bytes_launch = alg_bytes_frame / B

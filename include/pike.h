@@ -135,10 +135,12 @@ int pk_bvh_upload(pk_ctx* ctx, const int32_t* nodes5, uint32_t n_nodes, const in
                   uint32_t n_leaf_tris, const float* verts4, uint32_t n_verts);
 /* n_nodes, n_leaf_tris, and the normaliser {center x,y,z, scale} (only set by pk_bvh_build). */
 int pk_bvh_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* n_leaf_tris, double norm4[4]);
-/* Size (8-wide nodes, levels) and records (24 floats per node, the layout of
- * pk_wide.h) of the wide BVH; PK_ERR_STATE before PK_TRACE_WIDE was set. */
+/* Size (8-wide nodes, levels) and records of the compressed wide BVH (no
+ * reference counterpart; the layout of pike_gb300/csrc/pk_wide.h): nodes20 =
+ * 20 floats per node, tris12 (optional) = 12 floats per triangle record in the
+ * wide BVH's order; PK_ERR_STATE before PK_TRACE_WIDE was set. */
 int pk_wide_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* depth);
-int pk_wide_download(pk_ctx* ctx, float* nodes24);
+int pk_wide_download(pk_ctx* ctx, float* nodes20, float* tris12);
 int pk_bvh_download(pk_ctx* ctx, int32_t* nodes5, int32_t* tri4_leaf, float* verts4);
 
 /* ---- environment (row E) --------------------------------------------------
@@ -261,6 +263,21 @@ int pk_read_stats(pk_ctx* ctx, uint64_t out10[10]);
 #define PK_ACCUM_RUNNING_MEAN 0
 #define PK_ACCUM_COMPENSATED 1
 int pk_set_accumulation(pk_ctx* ctx, int mode);
+/* Environment light sampling of the shade pass: PK_ENV_HISTOGRAM is
+ * env_sampler.js's equal-mass luminance histogram (env_sampler.js:74-157,
+ * sampleEnv shade_hit.wgsl:213-227; the default, bit-exact with the
+ * reference); PK_ENV_ALIAS draws texels from a Walker/Vose alias table with
+ * probability proportional to their radiance, normalised in FP64 (the
+ * precision form; no reference counterpart).  The alias mode makes the same
+ * two hash draws and uses its own pdf texture for envPdf (shade_hit.wgsl:
+ * 202-210), so MIS stays consistent.  pk_env_alias_download returns the
+ * table (per texel {keep threshold, alias}: keep the uniformly drawn texel
+ * when the next 32-bit random number is below the threshold, always when it
+ * is 0xffffffff) and the pdf texture, W*H entries each. */
+#define PK_ENV_HISTOGRAM 0
+#define PK_ENV_ALIAS 1
+int pk_set_env_sampling(pk_ctx* ctx, int mode);
+int pk_env_alias_download(pk_ctx* ctx, uint32_t* table2, float* pdf);
 /* overlap = 1 lets pk_render_frame run each bounce's shadow traversal
  * concurrently with the next bounce's closest-hit traversal on a second stream
  * of its graph, 0 runs them in sequence, PK_OVERLAP_AUTO (the default) does

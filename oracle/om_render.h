@@ -249,19 +249,75 @@ struct Renderer {
     *bary = pack2x16unorm(u, v);
     return dist > eps ? dist : MAX_T;
   }
+  // The watertight test of form (1) (Woop, Benthin & Wald, JCGT 2013), the
+  // device's wt_setup / wt_test restated: kz = axis of largest |d| (first of
+  // equals), kx, ky cyclic after it and swapped when d[kz] < 0; shear
+  // S = (d[kx]/d[kz], d[ky]/d[kz], 1/d[kz]); an edge function exactly 0 is
+  // recomputed in double; t = T/det accepted when t > eps; (u, v) = (V, W)/det.
+  struct WtRay { int kx, ky, kz; float sx, sy, sz; float o[3]; };
+  static WtRay wt_setup(V3 o, V3 d) {
+    const float dv[3] = {d.x, d.y, d.z}, ov[3] = {o.x, o.y, o.z};
+    const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    int kz = 0;
+    float m = ax;
+    if (ay > m) { kz = 1; m = ay; }
+    if (az > m) kz = 2;
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    if (dv[kz] < 0.0f) std::swap(kx, ky);
+    WtRay w;
+    w.kx = kx; w.ky = ky; w.kz = kz;
+    w.sx = dv[kx] / dv[kz];
+    w.sy = dv[ky] / dv[kz];
+    w.sz = 1.0f / dv[kz];
+    w.o[0] = ov[kx]; w.o[1] = ov[ky]; w.o[2] = ov[kz];
+    return w;
+  }
+  float tri_hit_wt(const WtRay& r, const int32_t* tri, float eps, uint32_t* bary) const {
+    float p[3][3];
+    for (int k = 0; k < 3; k++) {
+      const V3 v = vert(tri[k]);
+      const float c[3] = {v.x, v.y, v.z};
+      p[k][0] = c[r.kx] - r.o[0];
+      p[k][1] = c[r.ky] - r.o[1];
+      p[k][2] = c[r.kz] - r.o[2];
+    }
+    const float Ax = p[0][0] - r.sx * p[0][2], Ay = p[0][1] - r.sy * p[0][2];
+    const float Bx = p[1][0] - r.sx * p[1][2], By = p[1][1] - r.sy * p[1][2];
+    const float Cx = p[2][0] - r.sx * p[2][2], Cy = p[2][1] - r.sy * p[2][2];
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+      U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+      V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+      W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return MAX_T;
+    const float det = U + V + W;
+    if (det == 0.0f) return MAX_T;
+    const float Az = r.sz * p[0][2], Bz = r.sz * p[1][2], Cz = r.sz * p[2][2];
+    const float T = U * Az + V * Bz + W * Cz;
+    const float t = T / det;
+    if (!(t > eps)) return MAX_T;
+    *bary = pack2x16unorm(V / det, W / det);
+    return t;
+  }
   struct TravResult { float t; int32_t index; uint32_t bary; uint32_t fetch, tests, max_stack; };
-  // Order-independent answer: every triangle tested, closest = min (t, slot),
-  // any = some triangle accepted.  Used in place of intersect() when
-  // `canonical` is set (the reference of the 8-wide traversal).
+  // Order-independent answer: every triangle tested with the watertight test,
+  // closest = min (t, slot), any = some triangle accepted.  Used in place of
+  // intersect() when `canonical` is set (the reference of form (1)'s 8-wide
+  // and FP32 binary traversals).
   bool canonical = false;
   template <bool ANY>
   TravResult brute(V3 o, V3 d) const {
     const float eps = ANY ? 1e-7f : 1e-8f;
     TravResult r{MAX_T, -1, 0u, 0u, 0u, 0u};
     const size_t nt = tri4.size() / 4;
+    const WtRay wr = wt_setup(o, d);
     for (size_t k = 0; k < nt; k++) {
       uint32_t bary = 0u;
-      const float res = tri_hit(o, d, &tri4[4 * k], eps, &bary);
+      const float res = tri_hit_wt(wr, &tri4[4 * k], eps, &bary);
       if (res < r.t) {
         r.t = res;
         r.index = (int32_t)k;
@@ -466,13 +522,29 @@ struct Renderer {
     float sin_phi = sin_(phi);
     return pdf_texel(cx, cy) / sin_phi;
   }
+  // Alias-table sampling of the library's PK_ENV_ALIAS (no reference
+  // counterpart): per texel {keep threshold, alias}; env_pdf then holds the
+  // table's pdf texture.  Empty: the reference's histogram.
+  std::vector<uint32_t> env_alias2;
   Sample sample_env(Hash& h, const SI& si) const {
     float dx = (float)env_w, dy = (float)env_h;
-    uint32_t nb = (uint32_t)(env_bins2.size() / 2);
-    int32_t idx = (int32_t)(h.hash() % nb);
-    int32_t h0 = env_bins2[2 * idx], h1 = env_bins2[2 * idx + 1];
-    int32_t ci = (int32_t)(h.hash() % (uint32_t)(h1 - h0)) + h0;
-    int32_t cx = env_coords2[2 * (size_t)ci], cy = env_coords2[2 * (size_t)ci + 1];
+    int32_t cx, cy;
+    if (!env_alias2.empty()) {
+      const uint32_t n = env_w * env_h;
+      const uint32_t i = h.hash() % n;
+      const uint32_t thr = env_alias2[2 * (size_t)i], al = env_alias2[2 * (size_t)i + 1];
+      const uint32_t r = h.hash();
+      const uint32_t k = (thr == 0xffffffffu || r < thr) ? i : al;
+      cx = (int32_t)(k % env_w);
+      cy = (int32_t)(k / env_w);
+    } else {
+      uint32_t nb = (uint32_t)(env_bins2.size() / 2);
+      int32_t idx = (int32_t)(h.hash() % nb);
+      int32_t h0 = env_bins2[2 * idx], h1 = env_bins2[2 * idx + 1];
+      int32_t ci = (int32_t)(h.hash() % (uint32_t)(h1 - h0)) + h0;
+      cx = env_coords2[2 * (size_t)ci];
+      cy = env_coords2[2 * (size_t)ci + 1];
+    }
     float u = -env_theta + ((0.5f + (float)cx) / dx);
     float v = (0.5f + (float)cy) / dy;
     float theta = u * TAU_F;
@@ -481,6 +553,17 @@ struct Renderer {
     V3 dir = v3(cos_(theta) * sin_phi, cos_(phi), sin_(theta) * sin_phi);
     float pdf = pdf_texel(cx, cy) / sin_phi;
     return Sample{vecmat(dir, si.b1, si.b2, si.n), pdf};
+  }
+  // sampleEnv's direction for texel (cx, cy) (shade_hit.wgsl:218-224, before
+  // the ONB) and envPdf's texel index for that direction (:202-206).
+  void env_roundtrip(int32_t cx, int32_t cy, float* dir3, int32_t* ix, int32_t* iy) const {
+    const float dx = (float)env_w, dy = (float)env_h;
+    const float u = -env_theta + ((0.5f + (float)cx) / dx);
+    const float v = (0.5f + (float)cy) / dy;
+    const float theta = u * TAU_F, phi = v * PI_F, sin_phi = sin_(phi);
+    const V3 dir = v3(cos_(theta) * sin_phi, cos_(phi), sin_(theta) * sin_phi);
+    dir3[0] = dir.x; dir3[1] = dir.y; dir3[2] = dir.z;
+    pdf_texel_index32(dir, ix, iy);
   }
   static float lambert_pdf(V3 wi) { return fmax_(wi.z, 1e-7f) * INV_PI_F; }
   static Sample sample_lambert(Hash& h) {
@@ -699,11 +782,13 @@ struct Renderer {
     at(i0 + 1, j0 + 1, t11);
     for (int k = 0; k < 4; k++) c[k] = mixd(mixd(t00[k], t10[k], fx), mixd(t01[k], t11[k], fx), fy);
   }
-  SI64 surface64(const Hit& hit) const {
+  SI64 surface64(const Hit& hit) const { return surface64_at(hit.index, hit.bary, d3f(hit.ray.d)); }
+  // getSurfaceInteraction in double for triangle `index`, the stored
+  // (unorm16) barycentrics and ray direction rd
+  SI64 surface64_at(int32_t index, uint32_t bary_word, D3 rd) const {
     SI64 si;
-    const D3 rd = d3f(hit.ray.d);
-    const int32_t* tri = &tri4[4 * (size_t)hit.index];
-    const double u = unorm16d(hit.bary, 0), v = unorm16d(hit.bary, 1);
+    const int32_t* tri = &tri4[4 * (size_t)index];
+    const double u = unorm16d(bary_word, 0), v = unorm16d(bary_word, 1);
     const D3 bary = d3(1.0 - u - v, u, v);
     D3 tg[3], bt[3], nm[3];
     double uvx[3], uvy[3];

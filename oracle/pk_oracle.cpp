@@ -15,6 +15,7 @@
 
 #include "om_build.h"
 #include "om_render.h"
+#include "om_render_f64.h"
 #include "om_diff.h"
 
 using namespace om;
@@ -175,6 +176,7 @@ int or_set_env(void* p, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32
   r->env_bins2.assign(bins2, bins2 + 2 * nb);
   r->env_coords2.assign(coords2, coords2 + 2 * N);
   r->env_pdf.assign(pdf, pdf + N);
+  r->env_alias2.clear();  // a new environment samples by its histogram
   r->sample_env_light = true;
   return 0;
 }
@@ -301,6 +303,18 @@ void or_set_canonical(void* p, int on) { ((Renderer*)p)->canonical = on != 0; }
 // FP64 companion (om_render64.h): which = 0 the FP64 accumulation
 // (accumulate.wgsl in double), 1 the mean and 2 the sum of squared deviations
 // of the per-frame FP64 colours since or_set_track64; W*H*4 doubles.
+// sampleEnv's direction for texel (cx, cy) and envPdf's texel for it.
+void or_env_roundtrip(void* p, int32_t cx, int32_t cy, float* dir3, int32_t* idx2) {
+  ((Renderer*)p)->env_roundtrip(cx, cy, dir3, idx2, idx2 + 1);
+}
+// Alias-table environment sampling (table2: W*H {threshold, alias}; pdf: W*H
+// r32f replacing the histogram's pdf texture); n = 0 restores nothing (set a
+// new environment to return to the histogram).
+void or_set_env_alias(void* p, const uint32_t* table2, const float* pdf, size_t n) {
+  Renderer* r = (Renderer*)p;
+  r->env_alias2.assign(table2, table2 + 2 * n);
+  r->env_pdf.assign(pdf, pdf + n);
+}
 // on: 0 off, 1 FP64 evaluation, 2 FP64 evaluation with the FP32 texel choices
 void or_set_track64(void* p, int on) { ((Renderer*)p)->set_track64(on != 0, on == 2); }
 uint64_t or_frames64(void* p) { return ((Renderer*)p)->frames64; }
@@ -308,6 +322,23 @@ int or_read64(void* p, int which, double* out) {
   Renderer* r = (Renderer*)p;
   const std::vector<double>* v = which == 0 ? &r->accum64 : which == 1 ? &r->mean64 : which == 2 ? &r->m2_64 : nullptr;
   if (!v || !r->track64) return 1;
+  std::memcpy(out, v->data(), v->size() * sizeof(double));
+  return 0;
+}
+
+// The reference path rendered in binary64 end to end (om_render_f64.h), on
+// the scene, environment, camera and sample index of a configured renderer.
+void* or_render64_new(void* r) { return new Render64(*(Renderer*)r); }
+void or_render64_free(void* p) { delete (Render64*)p; }
+void or_render64_tick(void* p, uint32_t bounces) { ((Render64*)p)->tick(bounces); }
+uint64_t or_render64_frames(void* p) { return ((Render64*)p)->frames; }
+// which = 0 the running mean, 1 the mean and 2 the sum of squared deviations
+// of the per-frame colours, 3 the last frame's colour; W*H*4 doubles.
+int or_render64_read(void* p, int which, double* out) {
+  Render64* r = (Render64*)p;
+  const std::vector<double>* v = which == 0 ? &r->accum : which == 1 ? &r->mean : which == 2 ? &r->m2
+                               : which == 3 ? &r->color : nullptr;
+  if (!v) return 1;
   std::memcpy(out, v->data(), v->size() * sizeof(double));
   return 0;
 }

@@ -22,7 +22,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(_HERE, f) for f in ("pk_oracle.cpp", "om_math.h", "om_build.h", "om_render.h", "Makefile")]
+    srcs = [os.path.join(_HERE, f) for f in ("pk_oracle.cpp", "om_math.h", "om_build.h", "om_render.h", "om_render64.h",
+                                             "om_render_f64.h", "om_diff.h", "Makefile")]
     if force or not os.path.exists(_LIB) or max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(_LIB):
         subprocess.run(["make", "-s", "-C", _HERE, "-B", "liboracle.so"], check=True)
     return _LIB
@@ -51,6 +52,13 @@ def lib():
         _lib.or_frames64.argtypes = [C.c_void_p]
         _lib.or_frames64.restype = C.c_uint64
         _lib.or_read64.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        _lib.or_render64_new.restype = C.c_void_p
+        _lib.or_render64_new.argtypes = [C.c_void_p]
+        _lib.or_render64_free.argtypes = [C.c_void_p]
+        _lib.or_render64_tick.argtypes = [C.c_void_p, C.c_uint32]
+        _lib.or_render64_frames.argtypes = [C.c_void_p]
+        _lib.or_render64_frames.restype = C.c_uint64
+        _lib.or_render64_read.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     return _lib
 
 
@@ -328,6 +336,25 @@ class Renderer:
     def frames64(self) -> int:
         return int(lib().or_frames64(self.p))
 
+    def env_roundtrip(self, cx: int, cy: int):
+        """sampleEnv's direction for texel (cx, cy) and envPdf's texel index of it."""
+        d = np.zeros(3, np.float32)
+        i = np.zeros(2, np.int32)
+        lib().or_env_roundtrip(self.p, C.c_int32(cx), C.c_int32(cy), _p(d), _p(i))
+        return d, (int(i[0]), int(i[1]))
+
+    def set_env_alias(self, table2: np.ndarray, pdf: np.ndarray):
+        """Sample the environment from an alias table (the library's
+        PK_ENV_ALIAS) with its pdf texture in place of the histogram's."""
+        t = np.ascontiguousarray(table2, np.uint32)
+        p = np.ascontiguousarray(pdf, np.float32)
+        lib().or_set_env_alias(self.p, _p(t), _p(p), C.c_size_t(p.size))
+
+    def render64(self) -> "Render64":
+        """An independent binary64 renderer (om_render_f64.h) of this
+        renderer's scene, environment, camera and current sample index."""
+        return Render64(self)
+
     def set_canonical(self, on: bool = True):
         """Trace by testing every triangle (min (t, slot)): the 8-wide traversal's answer."""
         lib().or_set_canonical(self.p, C.c_int(1 if on else 0))
@@ -373,3 +400,40 @@ class Prepared:
         self.r.set_scene(self.bvh, self.attrs, self.mat_index, self.layers)
         self.r.set_env(self.env)
         self.r.set_camera(src.camera_state())
+
+
+class Render64:
+    """The reference path rendered in binary64 end to end (om_render_f64.h):
+    its own rays, hits, queues and branches from the same hash streams."""
+
+    def __init__(self, r: "Renderer"):
+        self.w, self.h = r.w, r.h
+        self.p = lib().or_render64_new(r.p)
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().or_render64_free(self.p)
+            self.p = None
+
+    def tick(self, bounces: int):
+        lib().or_render64_tick(self.p, C.c_uint32(bounces))
+
+    def frames(self) -> int:
+        return int(lib().or_render64_frames(self.p))
+
+    def _read(self, which: int) -> np.ndarray:
+        out = np.zeros((self.h, self.w, 4), np.float64)
+        lib().or_render64_read(self.p, C.c_int(which), _p(out))
+        return out
+
+    def accum(self) -> np.ndarray:
+        """accumulate.wgsl's running mean in double."""
+        return self._read(0)
+
+    def std(self) -> np.ndarray:
+        """Per-pixel sample standard deviation of the per-frame colours."""
+        return np.sqrt(self._read(2) / max(self.frames() - 1, 1))
+
+    def color(self) -> np.ndarray:
+        """The last frame's colour buffer (before accumulation)."""
+        return self._read(3)

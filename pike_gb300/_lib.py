@@ -20,6 +20,7 @@ PK_OK, PK_ERR_ARG, PK_ERR_CUDA, PK_ERR_STATE, PK_ERR_DEVICE, PK_ERR_UNSUPPORTED 
 PK_BVH_SWEEP = 0
 PK_BVH_BINNED = 1
 PK_ACCUM_RUNNING_MEAN, PK_ACCUM_COMPENSATED = 0, 1
+PK_ENV_HISTOGRAM, PK_ENV_ALIAS = 0, 1
 PK_QUEUE_RAYS, PK_QUEUE_SHADOW, PK_QUEUE_MISS = 0, 1, 2
 PK_TRACE_CHUNKED, PK_TRACE_PERSISTENT, PK_TRACE_COMPACT_RECORDS, PK_TRACE_WIDE, PK_TRACE_EXACT = 0, 1, 2, 4, 8
 PK_OVERLAP_AUTO = -1
@@ -66,7 +67,7 @@ def load(path: str = LIB_PATH):
         "pk_scene_upload": [_P, _P, u32, _P, _P, u32], "pk_scene_download": [_P, _P, _P],
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
         "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
-        "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P],
+        "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P, _P],
         "pk_diff_render": [_P, _P, _P, _P], "pk_diff_backward": [_P, _P, _P, _P, _P, _P, _P],
         "pk_diff_rays": [_P, _P],
         "pk_batch_create": [_P, _P, u32], "pk_batch_destroy": [_P], "pk_batch_set_requests": [_P, _P, u32],
@@ -74,6 +75,7 @@ def load(path: str = LIB_PATH):
         "pk_batch_autotune": [_P, C.c_uint64, _P], "pk_batch_render": [_P, u32], "pk_batch_reset": [_P],
         "pk_batch_read": [_P, u32, _P], "pk_batch_info": [_P, _P, _P, _P], "pk_batch_latencies": [_P, _P],
         "pk_set_accumulation": [_P, C.c_int],
+        "pk_set_env_sampling": [_P, C.c_int], "pk_env_alias_download": [_P, _P, _P],
         "pk_set_frame_overlap": [_P, C.c_int],
         "pk_set_frames_in_flight": [_P, C.c_int],
         "pk_bvh_build": [_P, C.c_int], "pk_bvh_upload": [_P, _P, u32, _P, u32, _P, u32],

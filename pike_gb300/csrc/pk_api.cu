@@ -379,19 +379,33 @@ int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32
 }
 
 // ---------------- BVH ----------------
-// The 8-wide compressed BVH from the binary nodes and triangle records.
-static int build_wide(pk_ctx* c) {
-  std::vector<int32_t> nodes(5 * (size_t)c->n_nodes);
-  std::vector<float> tris(12 * (size_t)c->n_leaf_tris);
+// Host copies of the binary nodes, leaf-ordered triangle indices and
+// normalised vertices (the inputs of form (1)'s structures).
+static void download_bvh_inputs(pk_ctx* c, std::vector<int32_t>& nodes, std::vector<int32_t>& tri4,
+                                std::vector<float>& verts) {
+  nodes.resize(5 * (size_t)c->n_nodes);
+  tri4.resize(4 * (size_t)c->n_leaf_tris);
+  verts.resize(4 * (size_t)c->bvh_verts);
   check(cudaMemcpyAsync(nodes.data(), c->nodes5.p, nodes.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
   if (c->n_leaf_tris)
-    check(cudaMemcpyAsync(tris.data(), c->tris.p, tris.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaMemcpyAsync(tri4.data(), c->tri4_leaf.p, tri4.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  if (c->bvh_verts)
+    check(cudaMemcpyAsync(verts.data(), c->verts4.p, verts.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
   check(cudaStreamSynchronize(c->stream), "sync");
+}
+
+// The compressed 8-wide BVH and its triangle records.
+static int build_wide(pk_ctx* c) {
+  std::vector<int32_t> nodes, tri4;
+  std::vector<float> verts;
+  download_bvh_inputs(c, nodes, tri4, verts);
   WideHost w;
   std::string why;
-  if (build_wide_bvh(nodes.data(), c->n_nodes, tris.data(), c->n_leaf_tris, w, why))
+  if (build_wide_bvh(nodes.data(), c->n_nodes, tri4.data(), c->n_leaf_tris, verts.data(), c->bvh_verts, w, why))
     return fail(c, PK_ERR_ARG, "wide BVH: " + why);
-  upload(c->wide, reinterpret_cast<const float4*>(w.nodes.data()), 6 * (size_t)w.n_nodes, c->stream);
+  upload(c->wide, reinterpret_cast<const float4*>(w.nodes.data()), 5 * (size_t)w.n_nodes, c->stream);
+  upload(c->wide_tris, reinterpret_cast<const float4*>(w.tris.data()), std::max<size_t>(w.tris.size() / 4, 1),
+         c->stream);
   check(cudaStreamSynchronize(c->stream), "sync");
   c->wide_nodes = w.n_nodes;
   c->wide_depth = w.max_depth;
@@ -400,20 +414,21 @@ static int build_wide(pk_ctx* c) {
   return PK_OK;
 }
 
-// Binary records with outward-rounded FP32 boxes for PK_TRACE_EXACT.
+// Binary records with outward-rounded FP32 boxes and the binary leaf order's
+// triangle records for PK_TRACE_EXACT.
 static int build_exact(pk_ctx* c) {
-  std::vector<int32_t> nodes(5 * (size_t)c->n_nodes);
-  std::vector<float> tris(12 * (size_t)c->n_leaf_tris);
-  check(cudaMemcpyAsync(nodes.data(), c->nodes5.p, nodes.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  if (c->n_leaf_tris)
-    check(cudaMemcpyAsync(tris.data(), c->tris.p, tris.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  check(cudaStreamSynchronize(c->stream), "sync");
-  std::vector<float> rec;
+  std::vector<int32_t> nodes, tri4;
+  std::vector<float> verts;
+  download_bvh_inputs(c, nodes, tri4, verts);
+  std::vector<float> rec, tris;
   int32_t root = 0;
   std::string why;
-  if (build_exact_binary(nodes.data(), c->n_nodes, tris.data(), c->n_leaf_tris, rec, root, why))
+  if (build_exact_binary(nodes.data(), c->n_nodes, tri4.data(), c->n_leaf_tris, verts.data(), c->bvh_verts, rec,
+                         tris, root, why))
     return fail(c, PK_ERR_ARG, "exact binary records: " + why);
   upload(c->exact, reinterpret_cast<const float4*>(rec.data()), rec.size() / 4, c->stream);
+  upload(c->exact_tris, reinterpret_cast<const float4*>(tris.data()), std::max<size_t>(tris.size() / 4, 1),
+         c->stream);
   check(cudaStreamSynchronize(c->stream), "sync");
   c->exact_root = root;
   c->exact_ready = true;
@@ -424,9 +439,13 @@ static int build_exact(pk_ctx* c) {
 static int finish_bvh(pk_ctx* c) {
   c->wide_ready = false;
   c->wide.release();
+  c->wide_tris.release();
   c->exact_ready = false;
   c->exact.release();
-  c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
+  c->exact_tris.release();
+  // at least 128 records, so that a traversal may stage the first records of
+  // any tree in shared memory without reading past the allocation
+  c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 128u));
   c->inner32.alloc(2 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
   DevBuf<int> root(1);
@@ -461,11 +480,13 @@ int pk_wide_info(pk_ctx* c, uint32_t* n_nodes, uint32_t* depth) {
   });
 }
 
-int pk_wide_download(pk_ctx* c, float* nodes24) {
+int pk_wide_download(pk_ctx* c, float* nodes20, float* tris12) {
   return guarded(c, [&]() {
     if (!c->wide_ready) return fail(c, PK_ERR_STATE, "no wide BVH");
-    if (!nodes24) return fail(c, PK_ERR_ARG, "null output");
-    check(cudaMemcpy(nodes24, c->wide.p, c->wide.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    if (!nodes20) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaMemcpy(nodes20, c->wide.p, 80 * (size_t)c->wide_nodes, cudaMemcpyDeviceToHost), "D2H");
+    if (tris12 && c->n_leaf_tris)
+      check(cudaMemcpy(tris12, c->wide_tris.p, 48 * (size_t)c->n_leaf_tris, cudaMemcpyDeviceToHost), "D2H");
     return PK_OK;
   });
 }
@@ -531,6 +552,30 @@ int pk_bvh_download(pk_ctx* c, int32_t* nodes5, int32_t* tri4_leaf, float* verts
 }
 
 // ---------------- env ----------------
+// The alias table of PK_ENV_ALIAS from the current environment's texels.
+static int build_alias(pk_ctx* c) {
+  const size_t N = (size_t)c->env_w * c->env_h;
+  std::vector<uint8_t> rgbe(4 * N);
+  check(cudaMemcpyAsync(rgbe.data(), c->rgbe.p, 4 * N, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  check(cudaStreamSynchronize(c->stream), "sync");
+  std::vector<uint32_t> table2;
+  std::vector<float> pdf;
+  std::string why;
+  if (!build_env_alias(rgbe.data(), c->env_w, c->env_h, table2, pdf, why))
+    return fail(c, PK_ERR_ARG, "alias table: " + why);
+  upload(c->env_alias, reinterpret_cast<const uint2*>(table2.data()), N, c->stream);
+  upload(c->alias_pdf, pdf.data(), N, c->stream);
+  check(cudaStreamSynchronize(c->stream), "sync");
+  c->alias_ready = true;
+  c->invalidate_graph();
+  return PK_OK;
+}
+// After an environment change: the alias table follows it.
+static int env_changed(pk_ctx* c) {
+  c->alias_ready = false;
+  return c->env_sampling == PK_ENV_ALIAS ? build_alias(c) : PK_OK;
+}
+
 static int env_set(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const int32_t* bins2, uint32_t nb,
                    const int32_t* coords2, const float* pdf) {
   upload(c->rgbe, rgbe, (size_t)w * h, c->stream);
@@ -541,7 +586,7 @@ static int env_set(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h, const
   c->env_w = w; c->env_h = h; c->env_nb = nb;
   c->env_ready = true;
   c->invalidate_graph();
-  return PK_OK;
+  return env_changed(c);
 }
 
 int pk_env_build(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h) {
@@ -558,6 +603,31 @@ int pk_env_build(pk_ctx* c, const uint8_t* rgbe, uint32_t w, uint32_t h) {
     c->env_w = w; c->env_h = h; c->env_nb = nb;
     c->env_ready = true;
     c->invalidate_graph();
+    return env_changed(c);
+  });
+}
+
+int pk_set_env_sampling(pk_ctx* c, int mode) {
+  return guarded(c, [&]() {
+    if (mode != PK_ENV_HISTOGRAM && mode != PK_ENV_ALIAS) return fail(c, PK_ERR_ARG, "unknown env sampling mode");
+    if (mode == PK_ENV_ALIAS && !c->alias_ready) {
+      if (!c->env_ready) return fail(c, PK_ERR_STATE, "PK_ENV_ALIAS needs an environment");
+      const int rc = build_alias(c);
+      if (rc != PK_OK) return rc;
+    }
+    c->env_sampling = mode;
+    c->invalidate_graph();
+    return PK_OK;
+  });
+}
+
+int pk_env_alias_download(pk_ctx* c, uint32_t* table2, float* pdf) {
+  return guarded(c, [&]() {
+    if (!c->alias_ready) return fail(c, PK_ERR_STATE, "no alias table: set PK_ENV_ALIAS first");
+    const size_t N = (size_t)c->env_w * c->env_h;
+    if (table2) check(cudaMemcpyAsync(table2, c->env_alias.p, 8 * N, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    if (pdf) check(cudaMemcpyAsync(pdf, c->alias_pdf.p, 4 * N, cudaMemcpyDeviceToHost, c->stream), "D2H");
+    check(cudaStreamSynchronize(c->stream), "sync");
     return PK_OK;
   });
 }

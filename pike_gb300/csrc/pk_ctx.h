@@ -133,8 +133,10 @@ struct pk_ctx {
   DevBuf<int4> inner32;
   DevBuf<double> node_box_d;  // exact double node bounds (pk_bvh_build only)
   bool compact_nodes = false;  // traverse 32-byte records (same boxes as the 64-byte ones)
-  DevBuf<float4> wide;         // 8-wide compressed BVH (built on first use of PK_TRACE_WIDE)
+  DevBuf<float4> wide;         // compressed 8-wide BVH nodes (built on first use of PK_TRACE_WIDE)
+  DevBuf<float4> wide_tris;    // its triangle records, in its own leaf order
   DevBuf<float4> exact;        // binary records with outward-rounded FP32 boxes (PK_TRACE_EXACT)
+  DevBuf<float4> exact_tris;   // triangle records of the binary leaf order (PK_TRACE_EXACT)
   int exact_root = 0;
   bool exact_ready = false;
   uint32_t wide_nodes = 0, wide_depth = 0;
@@ -147,6 +149,10 @@ struct pk_ctx {
   DevBuf<int2> bins, coords;
   DevBuf<float> pdf;
   bool env_ready = false;
+  int env_sampling = 0;       // PK_ENV_HISTOGRAM or PK_ENV_ALIAS
+  DevBuf<uint2> env_alias;    // PK_ENV_ALIAS: {keep threshold, alias} per texel
+  DevBuf<float> alias_pdf;    // and its pdf texture
+  bool alias_ready = false;
   // measurement
   bool counting = false;
   bool timing = false;
@@ -176,8 +182,11 @@ struct pk_ctx {
     const bool ex = (trace_mode & pk::TRACE_EXACT) && exact_ready;
     L.scene = pk::SceneDev{ex ? exact.p : inner.p, (compact_nodes && !ex) ? inner32.p : nullptr, tris.p, tri4_leaf.p,
                            attrs.p, mat4.p, layers.p, (int)n_layers, (int)atlas_res, ex ? exact_root : root,
-                       n_leaf_tris, n_verts, n_mats, wide_ready ? wide.p : nullptr};
-    L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, pdf.p, (int)env_w, (int)env_h, (int)env_nb, env_ready ? 1 : 0};
+                       n_leaf_tris, n_verts, n_mats, wide_ready ? wide.p : nullptr,
+                       (trace_mode & pk::TRACE_WIDE) && wide_ready ? wide_tris.p : (ex ? exact_tris.p : nullptr)};
+    const bool al = env_sampling == PK_ENV_ALIAS && alias_ready;
+    L.env = pk::EnvDev{rgbe.p, bins.p, coords.p, al ? alias_pdf.p : pdf.p, (int)env_w, (int)env_h, (int)env_nb,
+                       env_ready ? 1 : 0, al ? env_alias.p : nullptr};
     L.color = slot[k].color.p;
     L.accum = accum.p;
     L.display = display.p;

@@ -71,16 +71,19 @@ struct SceneDev {
   uint32_t n_tris;         // leaf-ordered triangles
   uint32_t n_verts;        // vertex attributes
   uint32_t n_mats;         // material index entries
-  const float4* wide;      // 6 float4 per 8-wide node (pk_wide.h); null unless built
+  const float4* wide;      // 5 float4 per compressed 8-wide node (pk_wide.h); null unless built
+  const float4* wtris;     // form (1) triangle records {v0, v1, v2, slot} (pk_wide.h): the 8-wide
+                           // BVH's order (PK_TRACE_WIDE) or the binary leaf order (PK_TRACE_EXACT)
 };
 
 struct EnvDev {
   const uchar4* rgbe;      // rgba8 texels, alpha = exponent
   const int2* bins;        // {h0, h1}
   const int2* coords;      // {x, y}, descending radiance
-  const float* pdf;        // r32f per texel
+  const float* pdf;        // r32f per texel (the alias table's when `alias` is set)
   int w, h, nb;
   int enabled;             // SAMPLE_ENV_LIGHT
+  const uint2* alias;      // PK_ENV_ALIAS: per texel {keep threshold, alias texel}; null: the histogram
 };
 
 // ---- decoupled look-back over tiles carrying two 31-bit counts ------------

@@ -170,7 +170,10 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
 // leaf is intersected as soon as the ray reaches it, so each ray visits the
 // same nodes in the same order as trace.wgsl's loop and gets the same hit.
 // Hit bits are set with atomicOr in a flag array zeroed before the launch.
-constexpr int REFILL_MIN = 16;
+#ifndef PK_REFILL_MIN
+#define PK_REFILL_MIN 16
+#endif
+constexpr int REFILL_MIN = PK_REFILL_MIN;
 
 // Box test of the exact binary records: like box_hit, with the far distance
 // widened by WIDE_SLACK (relative) so that rounding never drops a box.
@@ -199,6 +202,12 @@ __device__ __forceinline__ void inner_children_exact(const SceneDev& sc, int cur
 // 10 resident blocks per SM (<= 48 registers): with several frames in
 // flight this beats the unconstrained 55 registers (2607-2611 vs 2579-2581
 // Mrays/s at 1080p, paired runs) and 12 blocks (2494).
+// PK_TREELET > 0 stages the first PK_TREELET inner records (the top levels:
+// records are numbered breadth first) in shared memory per block; the inner
+// record array is allocated with at least TREELET_ALLOC records.
+#ifndef PK_TREELET
+#define PK_TREELET 0
+#endif
 template <bool ANY, bool FUSED, bool COUNT, bool EXACT>
 __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                               const uint32_t* __restrict__ countp, RayQ R,
@@ -206,6 +215,13 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
                                                               float4* __restrict__ color, uint32_t npix,
                                                               uint32_t* __restrict__ ticket, int defer) {
   __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+#if PK_TREELET > 0
+  __shared__ float4 s_tree[EXACT ? 1 : 4 * PK_TREELET];
+  const bool treelet = !EXACT && sc.inner32 == nullptr;
+  if (treelet)
+    for (int i = threadIdx.x; i < 4 * PK_TREELET; i += TRACE_THREADS) s_tree[i] = __ldg(sc.inner + i);
+  __syncthreads();
+#endif
   int lstack[STACK_LOCAL];
   const uint32_t n = *countp;
   const int lane = threadIdx.x & 31;
@@ -221,6 +237,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
   uint32_t j = 0;
   bool have = false, exhausted = false;
   float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, ix = 0.f, iy = 0.f, iz = 0.f;
+  WtRay wr{};  // EXACT: the watertight test's per-ray set-up
   float best_t = MAX_T;
   int best_i = -1;
   uint32_t best_b = 0u;
@@ -239,8 +256,12 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
           const float4 o = __ldcs(R.o + j), d = __ldcs(R.d + j);  // read once
           ox = o.x; oy = o.y; oz = o.z;
           dx = d.x; dy = d.y; dz = d.z;
-          if (EXACT) { ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz); }
-          else { ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz; }
+          if (EXACT) {
+            ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz);
+            wr = wt_setup(ox, oy, oz, dx, dy, dz);
+          } else {
+            ix = 1.0f / dx; iy = 1.0f / dy; iz = 1.0f / dz;
+          }
           best_t = MAX_T; best_i = -1; best_b = 0u;
           sp = 0;
           cur = sc.root;
@@ -265,6 +286,16 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
         lok = lh < MAX_T && lh <= lim;
         rok = rh < MAX_T && rh <= lim;
       } else {
+#if PK_TREELET > 0
+        if (treelet && cur < PK_TREELET) {
+          const float4 a = s_tree[4 * cur], b = s_tree[4 * cur + 1], c4 = s_tree[4 * cur + 2];
+          const float4 chf = s_tree[4 * cur + 3];
+          lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
+          rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
+          cl = __float_as_int(chf.x);
+          cr = __float_as_int(chf.y);
+        } else
+#endif
         inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
         lok = lh < best_t;
         rok = rh < best_t;
@@ -293,6 +324,18 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       const int base = (int)(word & 0x00ffffffu);
       for (int i = 0; i < size; i++) {
         if (COUNT) ntest += 1;
+        if (EXACT) {  // the watertight test of form (1), min (t, slot)
+          float t, u, v;
+          uint32_t slot;
+          if (wt_test(sc.wtris, (uint32_t)(base + i), wr, eps, t, u, v, slot) &&
+              (t < best_t || (t == best_t && (int)slot < best_i))) {
+            best_t = t;
+            best_i = (int)slot;
+            best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+          }
+          if (ANY && !COUNT && best_i != -1) break;
+          continue;
+        }
         const float4* tp = sc.tris + 3 * (size_t)(base + i);
         const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
         const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
@@ -308,7 +351,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
         if (v < 0.0f || u + v > 1.0f) continue;
         const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
         const float res = dist > eps ? dist : MAX_T;
-        if (res < best_t || (EXACT && res == best_t && base + i < best_i)) {
+        if (res < best_t) {
           best_t = res;
           best_i = base + i;
           best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
@@ -344,38 +387,47 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
   }
 }
 
-// Pops the next stack entry whose entry distance does not exceed the current
-// best hit (with the traversal's slack); false when none is left.
-__device__ __forceinline__ bool wide_pop(int (*sstack)[TRACE_THREADS], float (*sdist)[TRACE_THREADS], const int* lstack,
-                                         const float* ldist, int tid, int& sp, float best_t, int& cur) {
-  const float lim = best_t + best_t * WIDE_SLACK;
-  while (sp > 0) {
-    --sp;
-    const bool sm = sp < WIDE_STACK_SMEM;
-    const float dd = sm ? sdist[sp][tid] : ldist[sp - WIDE_STACK_SMEM];
-    if (dd <= lim) {
-      cur = sm ? sstack[sp][tid] : lstack[sp - WIDE_STACK_SMEM];
-      return true;
-    }
-  }
-  return false;
+// =====================================================================
+// Persistent traversal of the compressed 8-wide BVH (pk_wide.h), after
+// Ylitie, Karras & Laine (HPG 2017): the stack holds groups, not nodes.  A
+// node group {child_base, hits << 24 | imask} stands for the hit internal
+// children of one node, visited in the ray's octant order (lowest bit
+// first); a triangle group {tri_base, triangle bits} for its hit leaf
+// triangles.  Each step visits one child of the current node group (pushing
+// the rest of the group) and then tests the triangle group in hand; while
+// fewer than CW_POSTPONE lanes of the warp have triangles and this lane still
+// has nodes to visit, the triangle group is pushed instead and tested later,
+// which keeps lanes in the same phase.  Lanes take new rays as in k_trace_dyn.
+// Closest hit = min (t, slot) over accepted triangles, any hit = the first
+// accepted triangle: the answer does not depend on the visiting order.
+// =====================================================================
+constexpr int CW_STACK_SMEM = 16;   // group entries per thread in shared memory
+constexpr int CW_STACK_LOCAL = 16;  // overflow entries in local memory
+#ifndef PK_CW_POSTPONE
+#define PK_CW_POSTPONE 8
+#endif
+constexpr int CW_POSTPONE = PK_CW_POSTPONE;
+
+__device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
+  if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
+  else if (sp < CW_STACK_SMEM + CW_STACK_LOCAL) lstack[sp - CW_STACK_SMEM] = g;
+  else return false;
+  ++sp;
+  return true;
+}
+__device__ __forceinline__ uint2 cw_pop(uint2 (*sstack)[TRACE_THREADS], const uint2* lstack, int tid, int& sp) {
+  --sp;
+  return sp < CW_STACK_SMEM ? sstack[sp][tid] : lstack[sp - CW_STACK_SMEM];
 }
 
-// =====================================================================
-// Persistent traversal of the 8-wide compressed BVH: the lane scheduling and
-// outputs of k_trace_dyn; closest hit = min (t, slot) over accepted
-// triangles, any hit = the first accepted triangle.
-// =====================================================================
 template <bool ANY, bool FUSED, bool COUNT>
-__global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
-                                                               const uint32_t* __restrict__ countp, RayQ R,
-                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
-                                                               float4* __restrict__ color, uint32_t npix,
-                                                               uint32_t* __restrict__ ticket, int defer) {
-  __shared__ int sstack[WIDE_STACK_SMEM][TRACE_THREADS];
-  __shared__ float sdist[WIDE_STACK_SMEM][TRACE_THREADS];
-  int lstack[WIDE_STACK_LOCAL];
-  float ldist[WIDE_STACK_LOCAL];
+__global__ void __launch_bounds__(TRACE_THREADS) k_trace_cw(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+                                                             const uint32_t* __restrict__ countp, RayQ R,
+                                                             uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
+                                                             float4* __restrict__ color, uint32_t npix,
+                                                             uint32_t* __restrict__ ticket, int defer) {
+  __shared__ uint2 sstack[CW_STACK_SMEM][TRACE_THREADS];
+  uint2 lstack[CW_STACK_LOCAL];
   const uint32_t n = *countp;
   const int lane = threadIdx.x & 31;
   const int tid = threadIdx.x;
@@ -389,11 +441,14 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
   uint32_t nfetch = 0, ntest = 0, nhit = 0;
   uint32_t j = 0;
   bool have = false, exhausted = false;
-  float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, ix = 0.f, iy = 0.f, iz = 0.f;
+  float ox = 0.f, oy = 0.f, oz = 0.f, ix = 0.f, iy = 0.f, iz = 0.f;
+  WtRay wr{};
+  uint32_t oct = 0;
   float best_t = MAX_T;
   int best_i = -1;
   uint32_t best_b = 0u;
-  int sp = 0, cur = 0;
+  int sp = 0;
+  uint2 G = make_uint2(0u, 0u), T = make_uint2(0u, 0u);
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
     const uint32_t busy = __ballot_sync(0xffffffffu, have);
@@ -407,11 +462,13 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
         if (j < n) {
           const float4 o = __ldcs(R.o + j), d = __ldcs(R.d + j);  // read once
           ox = o.x; oy = o.y; oz = o.z;
-          dx = d.x; dy = d.y; dz = d.z;
-          ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz);
+          ix = wide_inverse(d.x); iy = wide_inverse(d.y); iz = wide_inverse(d.z);
+          oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+          wr = wt_setup(o.x, o.y, o.z, d.x, d.y, d.z);
           best_t = MAX_T; best_i = -1; best_b = 0u;
           sp = 0;
-          cur = 0;  // wide root
+          G = make_uint2(0u, (1u << (24u + oct)) | 1u);  // the root: slot 0 of a one-child group
+          T = make_uint2(0u, 0u);
           have = true;
         } else {
           exhausted = true;
@@ -421,55 +478,49 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
     if (!__any_sync(0xffffffffu, have)) break;
     if (!have) continue;
     bool fin = false;
-    // wide nodes: descend into the nearest hit child, push the others with
-    // their entry distances; pops skip entries that start beyond the best hit
-    while (cur >= 0) {
+    if (G.y > 0x00ffffffu) {  // visit the nearest remaining child of the node group
+      const uint32_t bit = (uint32_t)__ffs(G.y >> 24) - 1u;
+      const uint32_t slot = bit ^ oct;
+      const uint32_t node = G.x + (uint32_t)__popc(G.y & ((1u << slot) - 1u) & 0xffu);
+      G.y &= ~(1u << (24u + bit));
+      if (G.y > 0x00ffffffu && !cw_push(sstack, lstack, tid, sp, G)) {
+        atomicOr(&ctr->err, ERR_STACK);
+        fin = true;
+      }
       if (COUNT) nfetch += 1;
-      float d[8];
-      int c[8];
-      wide_children(sc.wide, cur, ox, oy, oz, ix, iy, iz, best_t, d, c);
-      // descend into the nearest hit child; push the other hit children (their
-      // codes differ from the nearest one's)
-      float dn = __int_as_float(0x7f800000);
-      int cn = 0;
-#pragma unroll
-      for (int k = 0; k < 8; k++)
-        if (d[k] < dn) { dn = d[k]; cn = c[k]; }
-      if (!(dn < __int_as_float(0x7f800000))) {
-        if (!wide_pop(sstack, sdist, lstack, ldist, tid, sp, best_t, cur)) { fin = true; break; }
-        continue;
-      }
-      bool over = false;
-#pragma unroll
-      for (int k = 7; k >= 0; k--) {
-        if (d[k] < __int_as_float(0x7f800000) && c[k] != cn) {
-          if (sp < WIDE_STACK_SMEM) { sstack[sp][tid] = c[k]; sdist[sp][tid] = d[k]; }
-          else if (sp < WIDE_STACK_SMEM + WIDE_STACK_LOCAL) { lstack[sp - WIDE_STACK_SMEM] = c[k]; ldist[sp - WIDE_STACK_SMEM] = d[k]; }
-          else over = true;
-          ++sp;
-        }
-      }
-      if (over) { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
-      cur = cn;
+      uint32_t cb, tb, im, ih, th;
+      cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
+      G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
+      T = make_uint2(tb, th);
+    } else {  // a triangle group taken from the stack
+      T = G;
+      G = make_uint2(0u, 0u);
     }
-    // leaves
-    while (!fin && cur < 0) {
-      const uint32_t word = (uint32_t)cur & 0x7fffffffu;
-      const int size = (int)(word >> 24);
-      const int base = (int)(word & 0x00ffffffu);
-      for (int i = 0; i < size; i++) {
-        if (COUNT) ntest += 1;
-        float res, u, v;
-        if (!tri_test(sc.tris, base + i, ox, oy, oz, dx, dy, dz, eps, res, u, v)) continue;
-        if (res < best_t || (res == best_t && base + i < best_i)) {
-          best_t = res;
-          best_i = base + i;
-          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
-        }
-        if (ANY && !COUNT && best_i != -1) break;  // any hit: the first is enough
+    while (!fin && T.y != 0u) {
+      if (G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
+        if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
+        T.y = 0u;
+        break;
       }
-      if (ANY && best_i != -1) { fin = true; break; }
-      if (!wide_pop(sstack, sdist, lstack, ldist, tid, sp, best_t, cur)) { fin = true; break; }
+      const uint32_t i = (uint32_t)__ffs(T.y) - 1u;
+      T.y &= T.y - 1u;
+      if (COUNT) ntest += 1;
+      float t, u, v;
+      uint32_t slot;
+      if (wt_test(sc.wtris, T.x + i, wr, eps, t, u, v, slot) &&
+          (t < best_t || (t == best_t && (int)slot < best_i))) {
+        best_t = t;
+        best_i = (int)slot;
+        best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        if (ANY && !COUNT) fin = true;  // any hit: the first is enough
+      }
+    }
+    if (!fin) {
+      if (ANY && best_i != -1) fin = true;
+      else if (G.y <= 0x00ffffffu) {
+        if (sp == 0) fin = true;
+        else G = cw_pop(sstack, lstack, tid, sp);
+      }
     }
     if (fin) {
       const bool hit = best_i != -1;
@@ -478,8 +529,8 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace_wide(SceneDev sc, EnvDe
         if (!(ANY && FUSED)) atomicOr(flags + (j >> 5), 1u << (j & 31u));
         if (COUNT) nhit += 1;
       } else if (FUSED) {
-        const float4 tpv = __ldcs(R.t + j);
-        const V3 e = env_color(env, theta, v3(dx, dy, dz));
+        const float4 tpv = __ldcs(R.t + j), d = __ldcs(R.d + j);
+        const V3 e = env_color(env, theta, v3(d.x, d.y, d.z));
         fused_miss<ANY>(color, npix, hrec, j, __float_as_uint(tpv.w) & 0x0fffffffu, e.x * tpv.x, e.y * tpv.y,
                         e.z * tpv.z, defer, &ctr->err);
       }
@@ -693,10 +744,20 @@ __device__ __forceinline__ float env_pdf_dir(const EnvDev& env, float theta, V3 
 }
 // sampleEnv (:213-227)
 __device__ __forceinline__ Sample sample_env(const EnvDev& env, float theta, Hash& h, const SI& si) {
-  const int idx = (int)(h.next() % (uint32_t)env.nb);
-  const int2 bin = __ldg(env.bins + idx);
-  const int ci = (int)(h.next() % (uint32_t)(bin.y - bin.x)) + bin.x;
-  const int2 cc = __ldg(env.coords + ci);
+  int2 cc;
+  if (env.alias) {  // PK_ENV_ALIAS: a uniform texel, kept or replaced by its alias (same two draws)
+    const uint32_t n = (uint32_t)env.w * (uint32_t)env.h;
+    const uint32_t i = h.next() % n;
+    const uint2 e = __ldg(env.alias + i);
+    const uint32_t r = h.next();
+    const uint32_t k = (e.x == 0xffffffffu || r < e.x) ? i : e.y;
+    cc = make_int2((int)(k % (uint32_t)env.w), (int)(k / (uint32_t)env.w));
+  } else {
+    const int idx = (int)(h.next() % (uint32_t)env.nb);
+    const int2 bin = __ldg(env.bins + idx);
+    const int ci = (int)(h.next() % (uint32_t)(bin.y - bin.x)) + bin.x;
+    cc = __ldg(env.coords + ci);
+  }
   const float u = -theta + ((0.5f + (float)cc.x) / (float)env.w);
   const float v = (0.5f + (float)cc.y) / (float)env.h;
   const float th = u * c::TAU;
@@ -1277,7 +1338,7 @@ void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact
                   unsigned* trace_wide) {
   int t = 0, c = 0, s = 0, w = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false, false>, TRACE_THREADS, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w, k_trace_wide<false, true, false>, TRACE_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w, k_trace_cw<false, true, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&s, k_shade, SHADE_THREADS, 0);
   const unsigned warps = (capacity + 31u) / 32u;
@@ -1302,7 +1363,7 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
 #define PK_TRACEW(A, F, C) \
-  k_trace_wide<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, \
+  k_trace_cw<A, F, C><<<grid, block, 0, L.stream>>>(L.scene, L.env, L.ctr, countp, R, hrec, flags, L.color, L.npix, \
                                                       ticket, defer)
     if (!any_hit) {
       if (fused) { if (count) PK_TRACEW(false, true, true); else PK_TRACEW(false, true, false); }

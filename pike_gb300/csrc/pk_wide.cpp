@@ -1,18 +1,24 @@
-// pk_wide.cpp -- collapse of the binary BVH into 8-wide nodes with 8-bit
-// child boxes (host side; the record layout is described in pk_wide.h).
+// pk_wide.cpp -- collapse of the binary BVH into compressed 8-wide nodes
+// (host side; the record layout is described in pk_wide.h).
 //
 // Collapse: a wide node starts from its binary node's two children and
-// repeatedly opens the inner child of largest surface area until it holds
-// eight children or only leaves (the greedy collapse of Wald et al.,
-// "Getting Rid of Packets", 2008; Ylitie et al., HPG 2017 use the same child
-// budget).  Wide nodes are numbered breadth first, so every child index is
-// larger than its parent's.
+// repeatedly opens the child of largest surface area until it holds eight
+// children or only leaves (the greedy collapse of Wald et al., "Getting Rid of
+// Packets", 2008, with the child budget of Ylitie et al., HPG 2017).  A leaf
+// child holds at most three triangles; a binary leaf with more is split into
+// halves of its triangle range as if it were an inner node.  Children are
+// assigned to slots greedily by the octant cost of Ylitie et al. (the
+// child whose centroid lies furthest against a direction octant takes that
+// octant's slot).  Nodes are built one breadth-first level at a time, each
+// level in parallel; a prefix sum over the level gives every node's internal
+// children consecutive indices after all earlier nodes.
 #include "pk_wide.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
-#include <deque>
+#include <thread>
 
 namespace pk {
 
@@ -34,11 +40,31 @@ struct DBox {
       hi[a] = std::max(hi[a], b.hi[a]);
     }
   }
+  bool empty() const { return !(lo[0] <= hi[0] && lo[1] <= hi[1] && lo[2] <= hi[2]); }
   double area() const {
+    if (empty()) return 0.0;
     const double x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
     return x * y + y * z + z * x;
   }
+  double centre(int a) const { return empty() ? 0.0 : 0.5 * (lo[a] + hi[a]); }
 };
+
+template <class F>
+void parallel_for(size_t n, F fn) {
+  const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+  const size_t nt = std::min(hw, std::max<size_t>(1, n / 4096));
+  if (nt <= 1) {
+    fn(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  const size_t chunk = (n + nt - 1) / nt;
+  for (size_t t = 0; t < nt; t++) {
+    const size_t b = t * chunk, e = std::min(n, b + chunk);
+    if (b < e) th.emplace_back([=]() { fn(b, e); });
+  }
+  for (std::thread& x : th) x.join();
+}
 
 // Largest float not above x / smallest float not below x.
 float f_down(double x) {
@@ -60,13 +86,51 @@ float decode(float p, float s, int q) {
 
 constexpr double MARGIN = 0x1p-18;
 
-// Bounds of every binary node over the triangle records the test reads
-// (v0, v0 + e1, v0 + e2), widened by MARGIN * max(1, |x|).
-int node_boxes(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, std::vector<DBox>& box,
-               std::string& why) {
-  // ---- conservative binary node boxes (children have larger BFS indices)
+void widen(DBox& b) {
+  for (int a = 0; a < 3; a++) {
+    if (!(b.lo[a] <= b.hi[a])) continue;  // empty: never hit
+    b.lo[a] -= MARGIN * std::max(1.0, std::fabs(b.lo[a]));
+    b.hi[a] += MARGIN * std::max(1.0, std::fabs(b.hi[a]));
+  }
+}
+
+// Triangle boxes over the three vertices and the 48-byte triangle records of
+// the binary leaf order (slot = leaf-order index).
+int triangle_data(const int32_t* tri4, uint32_t n_tris, const float* verts4, uint32_t n_verts,
+                  std::vector<DBox>& tbox, std::vector<float>& recs, std::string& why) {
+  tbox.assign(n_tris, DBox());
+  recs.assign((size_t)WIDE_TRI_FLOATS * n_tris, 0.0f);
+  std::atomic<bool> bad{false};
+  parallel_for(n_tris, [&](size_t b, size_t e) {
+    for (size_t t = b; t < e; t++) {
+      const int32_t* tr = tri4 + 4 * t;
+      float* r = &recs[(size_t)WIDE_TRI_FLOATS * t];
+      DBox box;
+      for (int k = 0; k < 3; k++) {
+        if (tr[k] < 0 || (uint32_t)tr[k] >= n_verts) { bad = true; continue; }
+        const float* v = verts4 + 4 * (size_t)tr[k];
+        r[3 * k] = v[0];
+        r[3 * k + 1] = v[1];
+        r[3 * k + 2] = v[2];
+        box.add(v[0], v[1], v[2]);
+      }
+      const uint32_t slot = (uint32_t)t;
+      std::memcpy(&r[9], &slot, 4);
+      tbox[t] = box;
+    }
+  });
+  if (bad) {
+    why = "triangle vertex index out of range";
+    return 1;
+  }
+  return 0;
+}
+
+// Bounds of every binary node over its triangles' vertices, widened by MARGIN.
+int node_boxes(const int32_t* nodes5, uint32_t n_nodes, uint32_t n_tris, const std::vector<DBox>& tbox,
+               std::vector<DBox>& box, std::string& why) {
   box.assign(n_nodes, DBox());
-  for (int64_t i = (int64_t)n_nodes - 1; i >= 0; i--) {
+  for (int64_t i = (int64_t)n_nodes - 1; i >= 0; i--) {  // children have larger BFS indices
     const int32_t* nd = nodes5 + 5 * (size_t)i;
     DBox b;
     if (nd[1] > -1) {
@@ -76,15 +140,7 @@ int node_boxes(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint3
         why = "leaf outside the triangle array";
         return 1;
       }
-      for (uint32_t k = 0; k < size; k++) {
-        const float* t = tris + 12 * (size_t)(base + k);
-        const double v0[3] = {t[0], t[1], t[2]};
-        const double e1[3] = {t[3], t[4], t[5]};
-        const double e2[3] = {t[6], t[7], t[8]};
-        b.add(v0[0], v0[1], v0[2]);
-        b.add(v0[0] + e1[0], v0[1] + e1[1], v0[2] + e1[2]);
-        b.add(v0[0] + e2[0], v0[1] + e2[1], v0[2] + e2[2]);
-      }
+      for (uint32_t k = 0; k < size; k++) b.add(tbox[base + k]);
     } else {
       const int32_t l = nd[0];
       if (l <= (int32_t)i || (uint32_t)l + 1 >= n_nodes) {
@@ -96,149 +152,279 @@ int node_boxes(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint3
     }
     box[i] = b;
   }
-  for (DBox& b : box)
-    for (int a = 0; a < 3; a++) {
-      if (!(b.lo[a] <= b.hi[a])) continue;  // empty leaf: never hit
-      b.lo[a] -= MARGIN * std::max(1.0, std::fabs(b.lo[a]));
-      b.hi[a] += MARGIN * std::max(1.0, std::fabs(b.hi[a]));
-    }
   return 0;
 }
 
+// A child candidate of a wide node: a binary inner node, or a range of
+// leaf-ordered triangles (a binary leaf, or part of one).
+struct Item {
+  uint32_t kind;  // 0 binary inner node, 1 triangle range
+  uint32_t a;     // node index, or first triangle
+  uint32_t n;     // triangle count (ranges)
+};
+
+constexpr uint32_t LEAF_MAX = 3;
+
+struct Builder {
+  const int32_t* nodes5;
+  const std::vector<DBox>& tbox;
+  const std::vector<DBox>& nbox;  // widened binary node boxes
+
+  Item item_of(uint32_t node) const {
+    const int32_t t = nodes5[5 * (size_t)node + 1];
+    if (t > -1) return Item{1u, (uint32_t)t & 0x00ffffffu, (uint32_t)t >> 24};
+    return Item{0u, node, 0u};
+  }
+  DBox box_of(const Item& it) const {
+    if (it.kind == 0) return nbox[it.a];
+    DBox b;
+    for (uint32_t k = 0; k < it.n; k++) b.add(tbox[it.a + k]);
+    widen(b);
+    return b;
+  }
+  bool openable(const Item& it) const { return it.kind == 0 || it.n > LEAF_MAX; }
+  void open(const Item& it, Item& l, Item& r) const {
+    if (it.kind == 0) {
+      const uint32_t c = (uint32_t)nodes5[5 * (size_t)it.a];
+      l = item_of(c);
+      r = item_of(c + 1);
+    } else {
+      const uint32_t h = it.n / 2;
+      l = Item{1u, it.a, h};
+      r = Item{1u, it.a + h, it.n - h};
+    }
+  }
+
+  // Children of the wide node for `it` (at most 8), in slot order (empty slots
+  // have n = 0 and kind 1), and their boxes.
+  void children(const Item& it, Item (&slot)[8], DBox (&sbox)[8], bool (&used)[8]) const {
+    Item ch[8];
+    DBox cb[8];
+    int nc = 0;
+    if (openable(it)) {
+      open(it, ch[0], ch[1]);
+      nc = 2;
+    } else {
+      ch[0] = it;
+      nc = 1;
+    }
+    for (int k = 0; k < nc; k++) cb[k] = box_of(ch[k]);
+    while (nc < 8) {
+      int best = -1;
+      double best_a = -1.0;
+      for (int k = 0; k < nc; k++) {
+        if (!openable(ch[k])) continue;
+        const double a = cb[k].area();
+        if (a > best_a) {
+          best_a = a;
+          best = k;
+        }
+      }
+      if (best < 0) break;
+      Item l, r;
+      open(ch[best], l, r);
+      for (int k = nc; k > best + 1; k--) {
+        ch[k] = ch[k - 1];
+        cb[k] = cb[k - 1];
+      }
+      ch[best] = l;
+      cb[best] = box_of(l);
+      ch[best + 1] = r;
+      cb[best + 1] = box_of(r);
+      nc++;
+    }
+    // octant slots: cost(child, s) = dot(centre offset, sign vector of s);
+    // repeatedly take the cheapest free (child, slot) pair
+    DBox all;
+    for (int k = 0; k < nc; k++) all.add(cb[k]);
+    double cost[8][8];
+    for (int k = 0; k < nc; k++) {
+      const double dx = cb[k].centre(0) - all.centre(0), dy = cb[k].centre(1) - all.centre(1),
+                   dz = cb[k].centre(2) - all.centre(2);
+      for (int s = 0; s < 8; s++)
+        cost[k][s] = ((s & 1) ? -dx : dx) + ((s & 2) ? -dy : dy) + ((s & 4) ? -dz : dz);
+    }
+    bool cdone[8] = {false, false, false, false, false, false, false, false};
+    for (int s = 0; s < 8; s++) used[s] = false;
+    for (int round = 0; round < nc; round++) {
+      int bk = -1, bs = -1;
+      double bc = INFINITY;
+      for (int k = 0; k < nc; k++) {
+        if (cdone[k]) continue;
+        for (int s = 0; s < 8; s++)
+          if (!used[s] && (bk < 0 || cost[k][s] < bc)) {
+            bc = cost[k][s];
+            bk = k;
+            bs = s;
+          }
+      }
+      cdone[bk] = true;
+      used[bs] = true;
+      slot[bs] = ch[bk];
+      sbox[bs] = cb[bk];
+    }
+    for (int s = 0; s < 8; s++)
+      if (!used[s]) slot[s] = Item{1u, 0u, 0u};
+  }
+};
+
 }  // namespace
 
-int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, WideHost& out,
-                   std::string& why) {
+int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                   const float* verts4, uint32_t n_verts, WideHost& out, std::string& why) {
   out = WideHost();
   if (n_nodes == 0) {
     why = "empty BVH";
     return 1;
   }
-  std::vector<DBox> box;
-  if (node_boxes(nodes5, n_nodes, tris, n_tris, box, why)) return 1;
-  auto is_leaf = [&](uint32_t i) { return nodes5[5 * (size_t)i + 1] > -1; };
+  std::vector<DBox> tbox, nbox;
+  std::vector<float> brecs;
+  if (triangle_data(tri4, n_tris, verts4, n_verts, tbox, brecs, why)) return 1;
+  if (node_boxes(nodes5, n_nodes, n_tris, tbox, nbox, why)) return 1;
+  for (DBox& b : nbox) widen(b);
+  const Builder B{nodes5, tbox, nbox};
 
-  // ---- collapse, breadth first
-  struct Item {
-    uint32_t bin;
-    uint32_t depth;
+  struct Plan {
+    Item slot[8];
+    DBox sbox[8];
+    bool used[8];
+    uint32_t n_inner = 0, n_tri = 0;
   };
-  std::deque<Item> queue;
-  queue.push_back({0u, 1u});
+  std::vector<Item> level{B.item_of(0)};
+  uint32_t node_base = 0;  // index of the level's first node
+  uint32_t depth = 0;
   std::vector<float>& W = out.nodes;
-  uint32_t next = 1;
-  while (!queue.empty()) {
-    const Item it = queue.front();
-    queue.pop_front();
-    out.max_depth = std::max(out.max_depth, it.depth);
-    std::vector<uint32_t> ch;
-    if (is_leaf(it.bin)) {
-      ch.push_back(it.bin);
-    } else {
-      const uint32_t l = (uint32_t)nodes5[5 * (size_t)it.bin];
-      ch.push_back(l);
-      ch.push_back(l + 1);
-      while (ch.size() < 8) {
-        int best = -1;
-        double best_a = -1.0;
-        for (size_t k = 0; k < ch.size(); k++) {
-          if (is_leaf(ch[k])) continue;
-          const double a = box[ch[k]].area();
-          if (a > best_a) {
-            best_a = a;
-            best = (int)k;
+  std::vector<float>& T = out.tris;
+  while (!level.empty()) {
+    depth++;
+    const size_t n = level.size();
+    std::vector<Plan> plan(n);
+    parallel_for(n, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; i++) {
+        Plan& p = plan[i];
+        B.children(level[i], p.slot, p.sbox, p.used);
+        for (int s = 0; s < 8; s++) {
+          if (!p.used[s]) continue;
+          if (B.openable(p.slot[s])) p.n_inner++;
+          else p.n_tri += p.slot[s].n;
+        }
+      }
+    });
+    // prefix sums: internal children follow the level in order; triangle
+    // records follow those of all earlier nodes
+    std::vector<uint32_t> child0(n), tri0(n);
+    uint32_t next_child = node_base + (uint32_t)n, next_tri = (uint32_t)(T.size() / WIDE_TRI_FLOATS);
+    for (size_t i = 0; i < n; i++) {
+      child0[i] = next_child;
+      tri0[i] = next_tri;
+      next_child += plan[i].n_inner;
+      next_tri += plan[i].n_tri;
+    }
+    W.resize((size_t)WIDE_NODE_FLOATS * (node_base + n));
+    T.resize((size_t)WIDE_TRI_FLOATS * next_tri);
+    std::vector<Item> nxt(next_child - node_base - (uint32_t)n);
+    std::atomic<bool> fit{true};
+    parallel_for(n, [&](size_t b, size_t e) {
+      for (size_t i = b; i < e; i++) {
+        const Plan& p = plan[i];
+        float rec[WIDE_NODE_FLOATS];
+        std::memset(rec, 0, sizeof(rec));
+        uint8_t q[6][8], meta[8];
+        std::memset(q, 0, sizeof(q));
+        std::memset(meta, 0, sizeof(meta));
+        DBox all;
+        for (int s = 0; s < 8; s++)
+          if (p.used[s]) all.add(p.sbox[s]);
+        float org[3];
+        int ex[3];
+        for (int a = 0; a < 3; a++) {
+          double lo = all.lo[a], hi = all.hi[a];
+          if (!(lo <= hi)) { lo = 0.0; hi = 0.0; }
+          org[a] = f_down(lo);
+          const double ext = hi - (double)org[a];
+          int e2 = ext > 0.0 ? (int)std::ceil(std::log2(ext / 255.0)) : -100;
+          e2 = std::max(-100, std::min(e2, 127));
+          while (e2 < 127 && (double)decode(org[a], std::ldexp(1.0f, e2), 255) < hi) e2++;
+          ex[a] = e2;
+        }
+        uint32_t imask = 0, inner_rank = 0, tri_off = 0;
+        for (int s = 0; s < 8; s++) {
+          if (!p.used[s]) continue;
+          const Item& c = p.slot[s];
+          if (B.openable(c)) {
+            imask |= 1u << s;
+            meta[s] = (uint8_t)(0x20u | (uint32_t)s);
+            nxt[child0[i] - node_base - n + inner_rank] = c;
+            inner_rank++;
+          } else {
+            if (c.n == 0) continue;
+            meta[s] = (uint8_t)((((1u << c.n) - 1u) << 5) | tri_off);
+            for (uint32_t k = 0; k < c.n; k++)
+              std::memcpy(&T[(size_t)WIDE_TRI_FLOATS * (tri0[i] + tri_off + k)],
+                          &brecs[(size_t)WIDE_TRI_FLOATS * (c.a + k)], WIDE_TRI_FLOATS * sizeof(float));
+            tri_off += c.n;
+          }
+          const DBox& cb = p.sbox[s];
+          if (cb.empty()) continue;  // all-zero planes at the frame origin: hit tests may pass, no triangles
+          for (int a = 0; a < 3; a++) {
+            const float sc = std::ldexp(1.0f, ex[a]);
+            int lo = (int)std::floor((cb.lo[a] - (double)org[a]) / (double)sc);
+            lo = std::max(0, std::min(lo, 255));
+            while (lo > 0 && (double)decode(org[a], sc, lo) > cb.lo[a]) lo--;
+            int hi = (int)std::ceil((cb.hi[a] - (double)org[a]) / (double)sc);
+            hi = std::max(0, std::min(hi, 255));
+            while (hi < 255 && (double)decode(org[a], sc, hi) < cb.hi[a]) hi++;
+            if ((double)decode(org[a], sc, lo) > cb.lo[a] || (double)decode(org[a], sc, hi) < cb.hi[a]) fit = false;
+            q[a][s] = (uint8_t)lo;
+            q[3 + a][s] = (uint8_t)hi;
           }
         }
-        if (best < 0) break;
-        const uint32_t l2 = (uint32_t)nodes5[5 * (size_t)ch[best]];
-        ch[best] = l2;
-        ch.insert(ch.begin() + best + 1, l2 + 1);
+        rec[0] = org[0];
+        rec[1] = org[1];
+        rec[2] = org[2];
+        const uint32_t packed = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) |
+                                ((uint32_t)(ex[2] + 127) << 16) | (imask << 24);
+        std::memcpy(&rec[3], &packed, 4);
+        const uint32_t bases[2] = {p.n_inner ? child0[i] : 0u, tri0[i]};
+        std::memcpy(&rec[4], bases, 8);
+        std::memcpy(&rec[6], meta, 8);
+        // qlo.x qlo.y | qlo.z qhi.x | qhi.y qhi.z
+        std::memcpy(&rec[8], q[0], 8);
+        std::memcpy(&rec[10], q[1], 8);
+        std::memcpy(&rec[12], q[2], 8);
+        std::memcpy(&rec[14], q[3], 8);
+        std::memcpy(&rec[16], q[4], 8);
+        std::memcpy(&rec[18], q[5], 8);
+        std::memcpy(&W[(size_t)WIDE_NODE_FLOATS * (node_base + i)], rec, sizeof(rec));
       }
+    });
+    if (!fit) {
+      why = "child box does not fit its 8-bit frame";
+      return 1;
     }
-    // frame: origin rounded down, power-of-two scale so that 255 steps reach
-    // the largest child bound
-    float rec[24];
-    std::memset(rec, 0, sizeof(rec));
-    uint8_t q[6][8];
-    std::memset(q, 0, sizeof(q));
-    int32_t code[8];
-    for (int k = 0; k < 8; k++) code[k] = (int32_t)0x80000000u;
-    DBox all;
-    for (uint32_t c : ch) all.add(box[c]);
-    uint32_t valid = 0;
-    float p[3];
-    int ex[3];
-    for (int a = 0; a < 3; a++) {
-      if (!(all.lo[a] <= all.hi[a])) { all.lo[a] = 0.0; all.hi[a] = 0.0; }
-      p[a] = f_down(all.lo[a]);
-      const double ext = all.hi[a] - (double)p[a];
-      int e = ext > 0.0 ? (int)std::ceil(std::log2(ext / 255.0)) : -100;
-      e = std::max(-100, std::min(e, 127));
-      while (e < 127 && (double)decode(p[a], std::ldexp(1.0f, e), 255) < all.hi[a]) e++;
-      ex[a] = e;
-    }
-    for (size_t k = 0; k < ch.size(); k++) {
-      const DBox& b = box[ch[k]];
-      bool empty = false;
-      for (int a = 0; a < 3; a++) empty |= !(b.lo[a] <= b.hi[a]);
-      if (is_leaf(ch[k])) {
-        const uint32_t word = (uint32_t)nodes5[5 * (size_t)ch[k] + 1];
-        if ((word >> 24) == 0u) empty = true;
-        code[k] = (int32_t)(0x80000000u | word);
-      } else {
-        code[k] = (int32_t)next++;
-        queue.push_back({ch[k], it.depth + 1});
-      }
-      if (empty) continue;
-      valid |= 1u << k;
-      for (int a = 0; a < 3; a++) {
-        const float s = std::ldexp(1.0f, ex[a]);
-        int lo = (int)std::floor((b.lo[a] - (double)p[a]) / (double)s);
-        lo = std::max(0, std::min(lo, 255));
-        while (lo > 0 && (double)decode(p[a], s, lo) > b.lo[a]) lo--;
-        int hi = (int)std::ceil((b.hi[a] - (double)p[a]) / (double)s);
-        hi = std::max(0, std::min(hi, 255));
-        while (hi < 255 && (double)decode(p[a], s, hi) < b.hi[a]) hi++;
-        if ((double)decode(p[a], s, lo) > b.lo[a] || (double)decode(p[a], s, hi) < b.hi[a]) {
-          why = "child box does not fit its 8-bit frame";
-          return 1;
-        }
-        q[a][k] = (uint8_t)lo;
-        q[3 + a][k] = (uint8_t)hi;
-      }
-    }
-    rec[0] = p[0];
-    rec[1] = p[1];
-    rec[2] = p[2];
-    const uint32_t packed = (uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) |
-                            ((uint32_t)(ex[2] + 127) << 16) | (valid << 24);
-    std::memcpy(&rec[3], &packed, 4);
-    std::memcpy(&rec[4], code, 32);
-    // qlo.x qlo.y | qlo.z qhi.x | qhi.y qhi.z
-    std::memcpy(&rec[12], q[0], 8);
-    std::memcpy(&rec[14], q[1], 8);
-    std::memcpy(&rec[16], q[2], 8);
-    std::memcpy(&rec[18], q[3], 8);
-    std::memcpy(&rec[20], q[4], 8);
-    std::memcpy(&rec[22], q[5], 8);
-    W.insert(W.end(), rec, rec + 24);
+    node_base += (uint32_t)n;
+    level.swap(nxt);
   }
-  out.n_nodes = (uint32_t)(W.size() / 24);
-  if (out.n_nodes != next) {
-    why = "internal: wide node count mismatch";
+  out.n_nodes = node_base;
+  out.max_depth = depth;
+  if (T.size() != (size_t)WIDE_TRI_FLOATS * n_tris) {
+    why = "internal: triangle count mismatch";
     return 1;
   }
   return 0;
 }
 
-int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris,
-                       std::vector<float>& records, int32_t& root_code, std::string& why) {
+int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                       const float* verts4, uint32_t n_verts, std::vector<float>& records,
+                       std::vector<float>& tris, int32_t& root_code, std::string& why) {
   if (n_nodes == 0) {
     why = "empty BVH";
     return 1;
   }
-  std::vector<DBox> box;
-  if (node_boxes(nodes5, n_nodes, tris, n_tris, box, why)) return 1;
+  std::vector<DBox> tbox, box;
+  if (triangle_data(tri4, n_tris, verts4, n_verts, tbox, tris, why)) return 1;
+  if (node_boxes(nodes5, n_nodes, n_tris, tbox, box, why)) return 1;
+  for (DBox& b : box) widen(b);
   std::vector<uint32_t> rank(n_nodes);
   uint32_t n_inner = 0;
   for (uint32_t i = 0; i < n_nodes; i++) {

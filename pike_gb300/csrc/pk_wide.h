@@ -1,20 +1,31 @@
-// pk_wide.h -- 8-wide compressed BVH collapsed from the binary SAH BVH.
+// pk_wide.h -- 8-wide compressed BVH (form (1)) collapsed from the binary SAH
+// BVH, in the node format of Ylitie, Karras & Laine, "Efficient Incoherent
+// Ray Traversal on GPUs Through Compressed Wide BVHs" (HPG 2017).
 //
-// Node record: 96 bytes = 6 x float4
-//   [0] p.x, p.y, p.z (FP32 frame origin), w = bytes {ex+127, ey+127, ez+127, valid mask}
-//   [1] code[0..3]   [2] code[4..7]
-//       code >= 0: index of an 8-wide child node
-//       code <  0: 0x80000000 | size << 24 | base, a binary leaf's triangles
-//                  (the same word the binary traversal uses)
-//   [3] qlo.x[8] qlo.y[8]   [4] qlo.z[8] qhi.x[8]   [5] qhi.y[8] qhi.z[8]
-// Child box k on axis a: [p.a + 2^e.a * qlo.a[k], p.a + 2^e.a * qhi.a[k]],
-// evaluated as one FP32 multiply (exact) and one FP32 add.  Quantisation is
-// rounded outward against that exact decode, around boxes that already
-// enclose every triangle (v0, v0 + e1, v0 + e2 as the triangle test sees
-// them) with a margin of 2^-18 (times max(1, |x|)), so no intersection the
-// triangle test accepts lies outside its ancestors' boxes, even after the
-// traversal folds the decode into its slab test (a few ulps of the frame's
-// coordinates).
+// Node record: 80 bytes = 5 x float4
+//   [0] p.x, p.y, p.z (FP32 frame origin),
+//       w = bytes {ex + 127, ey + 127, ez + 127, imask}
+//   [1] x = child_base (index of the first internal child node),
+//       y = tri_base (index of the first triangle record of the node's leaves),
+//       z, w = meta[0..7], one byte per child slot:
+//         internal child: 0b00100000 | slot  (imask bit set)
+//         leaf child:     unary triangle count (0b001, 0b011, 0b111) << 5 | offset
+//                         (its triangles are records tri_base + offset ...)
+//         empty slot:     0
+//   [2] qlo.x[8] qlo.y[8]   [3] qlo.z[8] qhi.x[8]   [4] qhi.y[8] qhi.z[8]
+// Child box k on axis a: [p.a + 2^e.a * qlo.a[k], p.a + 2^e.a * qhi.a[k]].
+// Internal children are stored contiguously from child_base in slot order, so
+// the child in slot s is node child_base + popc(imask & ((1 << s) - 1)).
+// Children sit in octant order: slot s holds the child that comes first for
+// rays whose direction signs are the bits of s (bit 0: x < 0, 1: y, 2: z), so
+// a ray of octant o visits its hit children in the order of (slot ^ o).
+// Quantisation is rounded outward around boxes that enclose every triangle
+// (its three vertices) with a margin of 2^-18 (times max(1, |x|)).
+//
+// Triangle records (both the wide BVH's own leaf order and the binary
+// tree's), 48 bytes = 3 x float4: {v0.xyz, v1.x}, {v1.yz, v2.xy},
+// {v2.z, slot bits, 0, 0}, where `slot` is the triangle's index in the binary
+// BVH's leaf order (the index every hit record reports and ties break on).
 #pragma once
 #include <cstdint>
 #include <string>
@@ -22,24 +33,30 @@
 
 namespace pk {
 
+constexpr int WIDE_NODE_FLOATS = 20;
+constexpr int WIDE_TRI_FLOATS = 12;
+
 struct WideHost {
-  std::vector<float> nodes;  // 24 floats per node
+  std::vector<float> nodes;  // WIDE_NODE_FLOATS per node
+  std::vector<float> tris;   // WIDE_TRI_FLOATS per triangle, in the wide BVH's order
   uint32_t n_nodes = 0;
   uint32_t max_depth = 0;
 };
 
-// nodes5: binary BFS nodes (5 words each); tris: 12 floats per leaf triangle
-// ({v0, e1, e2} as the traversal-format triangle records).  Returns 0 on
+// nodes5: binary BFS nodes (5 words each); tri4: leaf-ordered {i0, i1, i2,
+// matId}; verts4: normalised vertex positions (4 floats each).  Returns 0 on
 // success, non-zero with a reason otherwise.
-int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris, WideHost& out,
-                   std::string& why);
+int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                   const float* verts4, uint32_t n_verts, WideHost& out, std::string& why);
 
 // The binary BVH's inner records (64-byte layout of the drop-in traversal:
 // both children's boxes, then their child codes) with FP32 boxes rounded
-// outward from the same triangle-record bounds and margin as the wide nodes,
-// instead of the reference's inward-truncated snorm16 boxes.  Traversed with
-// (t, slot) ties and slack in the box tests, closest hits equal brute force.
-int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const float* tris, uint32_t n_tris,
-                       std::vector<float>& records, int32_t& root_code, std::string& why);
+// outward from the same vertex bounds and margin as the wide nodes, instead of
+// the reference's inward-truncated snorm16 boxes, and the binary leaf order's
+// triangle records in the format above.  Traversed with (t, slot) ties and
+// slack in the box tests, closest hits equal brute force.
+int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                       const float* verts4, uint32_t n_verts, std::vector<float>& records,
+                       std::vector<float>& tris, int32_t& root_code, std::string& why);
 
 }  // namespace pk

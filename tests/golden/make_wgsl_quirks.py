@@ -1,0 +1,76 @@
+"""Generates tests/golden/wgsl_quirks.json: reference-derived known answers
+for three behaviours of the reference path, worked out from the reference's
+own source text and the WGSL / JavaScript language rules, not from the
+oracle (the oracle is what the fixtures check).
+
+1. rand() == 1.0 (render/shader/camera.wgsl:46-56): rand() is
+   f32(hash()) / 4294967296.0.  A u32 above 2^32 - 128 is not representable in
+   binary32 and converts to 2^32 (round to nearest), so rand() returns exactly
+   1.0.  The search below runs the hash of camera.wgsl:46-52 (as numpy u32
+   arithmetic) over camera seeds (px*1973 + py*9277 + samples*26699) | 1
+   (camera.wgsl:86-87) and records the first pixel whose jitter-x draw is 1.0.
+2. The missing-tangent fallback for a +y normal (render/util/gltf_loader.js:
+   268-276): normalize(cross(n, (0,1,0))) with n = (0,1,0) is 0/0 = NaN per
+   component; scene.js _quantizeVec3ToInt (scene.js:104-111) stores each
+   component into an Int8Array, and ToInt8(NaN) = 0, so the tangent and the
+   bitangent words are 0; the normal (0,1,0) stores bytes {0, 127, 0, 0}.
+3. The environment rotation theta in sampleEnv and envPdf
+   (render/shader/shade_hit.wgsl:202-227): sampleEnv puts texel (cx, cy) at
+   azimuth u = -theta + (cx + 0.5)/W, and envPdf reads u' = (1 + theta +
+   atan2(z, x)/2pi) % 1 = (cx + 0.5)/W again, so the pdf of a sampled
+   direction is its own texel's (the signs undo each other).  Worked example
+   W x H = 8 x 4, theta = 0.25, texel (3, 1): u = 0.1875, v = 0.375, both
+   angles 3pi/8; direction (cos(3pi/8) sin(3pi/8), cos(3pi/8), sin^2(3pi/8)).
+
+Run: python tests/golden/make_wgsl_quirks.py
+"""
+import json
+import math
+import os
+
+import numpy as np
+
+
+def _hash(state):
+    s = state.astype(np.uint32)
+    nxt = (s * np.uint32(747796405) + np.uint32(2891336453)).astype(np.uint32)
+    word = (((s >> ((s >> np.uint32(28)) + np.uint32(4))) ^ s) * np.uint32(277803737)).astype(np.uint32)
+    return ((word >> np.uint32(22)) ^ word).astype(np.uint32), nxt
+
+
+def rand_one():
+    W = 4096
+    py, px = np.meshgrid(np.arange(W, dtype=np.uint32), np.arange(W, dtype=np.uint32), indexing="ij")
+    for samples in range(8):
+        seed = ((px * np.uint32(1973) + py * np.uint32(9277) + np.uint32(samples * 26699)) | np.uint32(1))
+        first, _ = _hash(seed)           # seed = hash(): the state becomes this output
+        jitter, _ = _hash(first)         # rand() #1, the jitter x of createPrimaryRay
+        hit = np.argwhere(jitter >= np.uint32(0xFFFFFF80))
+        if len(hit):
+            y, x = (int(v) for v in hit[0])
+            return {"px": x, "py": y, "samples": samples, "state": int(first[y, x]),
+                    "hash": int(jitter[y, x]), "rand_f32_bits": "0x3f800000",
+                    "why": "u32 >= 2^32 - 128 rounds to 2^32 in binary32; / 2^32 = 1.0"}
+    raise RuntimeError("no seed found")
+
+
+def main():
+    c, s = math.cos(3 * math.pi / 8), math.sin(3 * math.pi / 8)
+    out = {
+        "rand_one": rand_one(),
+        "nan_tangent": {"normal": [0.0, 1.0, 0.0], "tangent_word": 0, "bitangent_word": 0,
+                        "normal_word": 0x00007F00,
+                        "why": "normalize(cross(+y, +y)) = NaN; Int8Array stores NaN as 0"},
+        "env_theta_roundtrip": {"w": 8, "h": 4, "theta": 0.25, "texel": [3, 1], "u": 0.1875, "v": 0.375,
+                                "direction": [c * s, c, s * s], "pdf_texel": [3, 1],
+                                "why": "sampleEnv subtracts theta, envPdf adds it back"},
+    }
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "wgsl_quirks.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+        f.write("\n")
+    print(path)
+
+
+if __name__ == "__main__":
+    main()

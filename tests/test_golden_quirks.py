@@ -1,0 +1,74 @@
+"""Reference-derived known answers (tests/golden/wgsl_quirks.json, made by
+tests/golden/make_wgsl_quirks.py from the reference's source text and the
+WGSL / JavaScript rules, not from the oracle) checked against the oracle:
+rand() returning exactly 1.0 (camera.wgsl:54-56), the NaN fallback tangent
+of a +y normal stored as 0 (gltf_loader.js:275, scene.js:104-111), and the
+environment rotation undone between sampleEnv and envPdf (shade_hit.wgsl:
+202-227)."""
+import json
+import os
+
+import numpy as np
+
+from gltf_fixtures import GltfBuilder
+from pike_gb300.scene_loader import build_scene_arrays
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+with open(os.path.join(HERE, "golden", "wgsl_quirks.json")) as f:
+    Q = json.load(f)
+
+
+def test_rand_returns_one(oracle):
+    q = Q["rand_one"]
+    seed = (q["px"] * 1973 + q["py"] * 9277 + q["samples"] * 26699) & 0xFFFFFFFF | 1
+    first = int(oracle.hash_stream(seed, 1)[0])       # seed = hash(): the output becomes the state
+    jitter, jy = (int(v) for v in oracle.hash_stream(first, 2))
+    assert first == q["state"] and jitter == q["hash"]
+    assert np.float32(np.float32(jitter) / np.float32(4294967296.0)).view(np.uint32) == int(q["rand_f32_bits"], 16)
+    # the oracle's camera ray of that pixel: jitter x = 1.0 puts it on the
+    # pixel's right edge.  Pinhole camera at the origin looking down +z,
+    # fov pi/3, no lens: dir = normalize(-t ux, t uy, 1), t = tan(pi/6).
+    W, H = q["px"] + 1, q["py"] + 1
+    r = oracle.Renderer(W, H, batch=128, threads=1)
+    state = {"pos": [0.0, 0.0, 0.0], "dir": [0.0, 0.0, 1.0], "fov": float(np.pi / 3), "focalDepth": 0.5,
+             "apertureSize": 0.0, "distortion": 0.0, "bokeh": 0.5, "invocationOffset": q["py"] * W + q["px"]}
+    r.set_camera(state)
+    r.set_render_state(q["samples"])
+    r.clear_rays()
+    r.camera()
+    ray = r.rays(0, 1)[0]
+    jyf = float(np.float32(np.float32(jy) / np.float32(4294967296.0)))
+    ux = (2.0 * ((q["px"] + 1.0) / W) - 1.0) * (W / H)
+    uy = -(2.0 * ((q["py"] + jyf) / H) - 1.0)
+    t = np.tan(np.pi / 6)
+    want = np.array([-t * ux, t * uy, 1.0])
+    want /= np.linalg.norm(want)
+    assert np.allclose(ray[4:7], want, atol=2e-6), (ray[4:7], want)
+    assert ray[11].view(np.uint32) == q["py"] * W + q["px"]  # the pixel index rides in tp.w
+
+
+def test_nan_fallback_tangent_words(tmp_path, oracle):
+    q = Q["nan_tangent"]
+    g = GltfBuilder()
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], np.float32)
+    nrm = np.tile(np.array(q["normal"], np.float32), (3, 1))
+    m = g.material(name="m")
+    g.m["scenes"][0]["nodes"] = [g.node(mesh=g.mesh("t", [g.primitive(pos, [0, 2, 1], m, nrm)]))]
+    g.write_gltf(str(tmp_path / "t.gltf"))
+    a = build_scene_arrays({"props": [{"uri": "t.gltf"}]}, str(tmp_path))
+    _, attrs = oracle.flatten_tbn(a["pos"], a["normal"], a["tangent"], a["bnormal"], a["btangent"], a["uv"])
+    assert (attrs[:, 0] == q["tangent_word"]).all()
+    assert (attrs[:, 1] == q["bitangent_word"]).all()
+    assert (attrs[:, 2] == q["normal_word"]).all()
+
+
+def test_env_theta_roundtrip(oracle):
+    q = Q["env_theta_roundtrip"]
+    w, h = q["w"], q["h"]
+    r = oracle.Renderer(4, 4, threads=1)
+    rgbe = np.full((h, w, 4), 128, np.uint8)
+    r.set_env(oracle.Env(rgbe))
+    r.set_render_state(0, q["theta"])
+    d, texel = r.env_roundtrip(*q["texel"])
+    assert np.allclose(d, q["direction"], atol=1e-6), (d, q["direction"])
+    assert list(texel) == q["pdf_texel"]

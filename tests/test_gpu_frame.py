@@ -79,6 +79,20 @@ def test_fused_equals_pass_path(oracle, pk_built):
     assert_bits_equal(a.image("accum"), fused, "pass path vs fused frame")
 
 
+@pytest.mark.slow
+def test_full_size_frame_matches_oracle(oracle, pk_built):
+    """The benchmark's workload itself: 1920x1080 on the 1.3M-triangle scene
+    with the 2048x1024 environment and 8 bounces, one fused frame (in pixel
+    batches of 1920x270, as tick() renders them) bit-exact against the
+    oracle."""
+    src = synth.displaced_sphere_scene()
+    pair = Pair(src, oracle, threads=16, batch=src.width * 270)
+    fused_frames(pair, 1, 8)
+    oracle_frames(pair, 1, 8)
+    assert_bits_equal(pair.image("color"), pair.P.r.color(), "1080p frame colour")
+    assert_bits_equal(pair.image("accum"), pair.P.r.accum(), "1080p accumulated radiance")
+
+
 def test_full_size_determinism_and_counts(oracle, pk_built):
     """1920x1080 on the 1.3M-triangle scene: two renders are bit-identical, no
     device error flags, and the ray counts obey the queue invariants."""

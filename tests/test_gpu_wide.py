@@ -24,12 +24,13 @@ def wide_pair(oracle, src, mode=WIDE, **kw) -> Pair:
     return pair
 
 
-def wide_nodes(ctx):
+def wide_nodes(ctx, n_tris):
     n, depth = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
     ctx.call("pk_wide_info", ptr(n), ptr(depth))
-    nodes = np.zeros((int(n[0]), 24), np.float32)
-    ctx.call("pk_wide_download", ptr(nodes))
-    return nodes, int(depth[0])
+    nodes = np.zeros((int(n[0]), 20), np.float32)
+    tris = np.zeros((n_tris, 12), np.float32)
+    ctx.call("pk_wide_download", ptr(nodes), ptr(tris))
+    return nodes, tris, int(depth[0])
 
 
 def test_trace_mode_rules(pk_built, oracle):
@@ -41,33 +42,63 @@ def test_trace_mode_rules(pk_built, oracle):
         assert e.value.code == _lib.PK_ERR_ARG
 
 
-def test_wide_structure(oracle, pk_built):
-    """Every leaf-ordered triangle is reachable from exactly one valid slot;
-    child nodes come after their parent; decoded child boxes lie inside the
-    parent's own slot box."""
-    src = synth.displaced_sphere_scene(subdivisions=5, width=16, height=16, env_size=(64, 32))
+@pytest.mark.parametrize("make", [
+    lambda: synth.displaced_sphere_scene(subdivisions=5, width=16, height=16, env_size=(64, 32)),
+    lambda: synth.triangle_soup_scene(n_tris=20_000, width=16, height=16, env_size=(64, 32)),
+], ids=["sphere5", "soup20k"])
+def test_wide_structure(oracle, pk_built, make):
+    """Compressed wide nodes (pk_wide.h): internal children come after their
+    parent, contiguous from child_base in slot order, and every node but the
+    root is referenced once; leaf children hold 1-3 triangle records at
+    tri_base + offset, every record is referenced once and the records carry
+    every binary slot once, with that slot's vertices; every decoded leaf
+    child box contains its triangles' vertices (outward rounding)."""
+    src = make()
     pair = wide_pair(oracle, src)
-    nodes, depth = wide_nodes(pair.ctx)
-    words = nodes.view(np.uint32)
     n_tris = src.tris.shape[0]
+    nodes, tris, depth = wide_nodes(pair.ctx, n_tris)
+    words = nodes.view(np.uint32)
+    meta = np.ascontiguousarray(nodes[:, 6:8]).view(np.uint8)
+    q = np.ascontiguousarray(nodes[:, 8:20]).view(np.uint8).reshape(-1, 6, 8)  # qlo xyz, qhi xyz
     seen = np.zeros(n_tris, np.int64)
     referenced = np.zeros(nodes.shape[0], np.int64)
+    verts = tris[:, :9].reshape(-1, 3, 3)
     for i in range(nodes.shape[0]):
-        valid = words[i, 3] >> 24
-        codes = words[i, 4:12].view(np.int32)
+        imask = words[i, 3] >> 24
+        child_base, tri_base = int(words[i, 4]), int(words[i, 5])
+        p = nodes[i, :3].astype(np.float64)
+        e = np.array([(words[i, 3] >> (8 * a)) & 0xFF for a in range(3)], np.int64) - 127
+        s = np.ldexp(1.0, e)
+        rank = 0
         for k in range(8):
-            if not (valid >> k) & 1:
-                continue
-            c = int(codes[k])
-            if c >= 0:
+            m = int(meta[i, k])
+            if (imask >> k) & 1:
+                assert m == 0x20 | k
+                c = child_base + rank
+                rank += 1
                 assert c > i
                 referenced[c] += 1
-            else:
-                w = c & 0x7FFFFFFF
-                size, base = w >> 24, w & 0xFFFFFF
-                seen[base:base + size] += 1
+                continue
+            if m == 0:
+                continue
+            count = {1: 1, 3: 2, 7: 3}[m >> 5]
+            off = m & 31
+            assert off + count <= 24
+            r0 = tri_base + off
+            seen[r0:r0 + count] += 1
+            lo = (p + s * q[i, 0:3, k]).astype(np.float32)
+            hi = (p + s * q[i, 3:6, k]).astype(np.float32)
+            v = verts[r0:r0 + count].reshape(-1, 3)
+            assert (v >= lo).all() and (v <= hi).all(), f"node {i} slot {k}: box does not contain its triangles"
     assert (seen == 1).all()
     assert referenced[0] == 0 and (referenced[1:] == 1).all()
+    slots = tris[:, 9].view(np.uint32)
+    assert np.array_equal(np.sort(slots), np.arange(n_tris, dtype=np.uint32))
+    # each record holds its binary slot's vertices
+    tri4 = pair.P.bvh.tris.reshape(-1, 4)
+    bverts = pair.P.bvh.verts.reshape(-1, 4)[:, :3]
+    want = bverts[tri4[slots, :3]].reshape(-1, 9)
+    assert np.array_equal(tris[:, :9].view(np.uint32), want.astype(np.float32).view(np.uint32))
     assert 2 <= depth <= 16
 
 
@@ -116,6 +147,14 @@ def test_wide_pass_hits_match_bruteforce(oracle, pk_built, mode):
             c.call("pk_" + name)
 
 
+def brute_rows(pair, rays: np.ndarray) -> np.ndarray:
+    """The oracle's brute-force answers in per_ray's layout (a miss as {0,
+    0xffffffff, 0}; the oracle reports a miss with t = MAX_T)."""
+    want = pair.P.r.brute_rays(np.ascontiguousarray(rays[:, :8]))[:, :3].copy()
+    want[want[:, 1] == 0xFFFFFFFF] = [0, 0xFFFFFFFF, 0]
+    return want
+
+
 def per_ray(hits: np.ndarray, rays: np.ndarray) -> np.ndarray:
     """Hit records -> (n, 3) {t, slot, bary} per queue ray (slot 0xffffffff: miss).
     Records carry their ray, whose 12 words identify it in the queue."""
@@ -128,10 +167,13 @@ def per_ray(hits: np.ndarray, rays: np.ndarray) -> np.ndarray:
 
 
 def test_wide_vs_dropin_agreement(oracle, pk_built):
-    """Closest hits of the drop-in traversal agree with the wide one except on
-    rays where the drop-in's inward-truncated boxes lose a hit or a tie on t
-    resolves differently; on every differing ray the wide answer equals brute
-    force, and such rays are rare."""
+    """Closest-hit triangle ids of the drop-in traversal (Moller-Trumbore on
+    the reference's snorm16 boxes) agree with the wide one (watertight test)
+    except on rays where the drop-in's inward-truncated boxes lose a hit, a
+    tie on t resolves differently or the two triangle tests disagree at an
+    edge; on every differing ray the wide answer (slot, t, barycentrics)
+    equals brute force, and such rays are rare.  t and barycentrics come from
+    different triangle tests, so only the triangle id is compared."""
     src = synth.displaced_sphere_scene(subdivisions=7, width=320, height=180, env_size=(256, 128))
     pair = Pair(src, oracle)
     c = pair.ctx
@@ -149,12 +191,14 @@ def test_wide_vs_dropin_agreement(oracle, pk_built):
             c.call("pk_trace")
             res.append(per_ray(pair.hits(pair.counters()["num_hits"]), rays))
         plain, wide = res
-        bad = np.flatnonzero((plain != wide).any(axis=1))
+        bad = np.flatnonzero(plain[:, 1] != wide[:, 1])
         total += n
         differ += bad.size
         if bad.size:
-            want = pair.P.r.brute_rays(np.ascontiguousarray(rays[bad, :8]))
-            assert np.array_equal(wide[bad], want[:, :3]), f"bounce {bounce}: wide differs from brute force"
+            assert np.array_equal(wide[bad], brute_rows(pair, rays[bad])), f"bounce {bounce}: wide differs from brute force"
+        # a sample of all rays, not only the differing ones: the wide answer is brute force
+        pick = np.random.default_rng(bounce).choice(n, size=min(n, 3000), replace=False)
+        assert np.array_equal(wide[pick], brute_rows(pair, rays[pick])), f"bounce {bounce}: wide differs from brute force"
         for name in ("shade_hit", "trace_shadow", "shade_miss"):
             c.call("pk_" + name)
     assert total > 100_000
