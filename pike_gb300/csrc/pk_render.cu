@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
 constexpr int CW_STACK_SMEM = 16;   // group entries per thread in shared memory
 constexpr int CW_STACK_LOCAL = 16;  // overflow entries in local memory
 #ifndef PK_CW_POSTPONE
-#define PK_CW_POSTPONE 8
+#define PK_CW_POSTPONE 4
 #endif
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
 

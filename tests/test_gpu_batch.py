@@ -104,3 +104,38 @@ def test_bad_requests_are_rejected(scenes):
     with pytest.raises(PikeError) as e:
         batch.render(1)  # no requests yet
     assert e.value.code == _lib.PK_ERR_STATE
+
+
+def test_batch_pixel_exact_where_seeds_coincide(scenes):
+    """One sample of depth 1: the batch and the drop-in trace the same camera
+    rays (seeded by pixel and sample) to the same closest hits.  Shading seeds
+    differ by construction (the batch uses the bounce index, the drop-in the
+    hit-queue slot), except for the first hit of the queue (slot 0 = bounce
+    0).  So every pixel whose camera ray misses, and the pixel of hit slot 0,
+    must be bit-exact between the two."""
+    srcs, ctxs = scenes
+    src, ctx = srcs[1], ctxs[1]
+    W, H = 64, 48
+    cam = src.camera_state()
+    batch = Batch(ctxs)
+    batch.set_requests([Request(scene=1, width=W, height=H, spp=1, depth=1, camera=cam)])
+    batch.render(1)
+    got = batch.image(0)
+    want = plain_mean(ctx, cam, W, H, 1, 1)
+    # which camera rays hit: the pass path's first trace, in queue order
+    ctx.call("pk_set_render_state", 0, 0.0)
+    for name in ("clear_color", "clear_hits_misses", "clear_rays", "camera", "trace"):
+        ctx.call("pk_" + name)
+    cnt = np.zeros(8, np.uint32)
+    ctx.call("pk_read_counters", ptr(cnt))
+    n_hits = int(cnt[1])  # {samples, num_hits, ...}
+    hits = np.zeros((n_hits, 16), np.uint32)
+    ctx.call("pk_read_hits", 0, n_hits, ptr(hits))
+    hit_pix = hits[:, 15] & 0x0FFFFFFF  # the pixel index in the ray's tp.w
+    assert 0 < n_hits < W * H
+    miss = np.ones(W * H, bool)
+    miss[hit_pix] = False
+    g, w = got.reshape(-1, 4)[:, :3], want.reshape(-1, 4)[:, :3]
+    assert np.array_equal(g[miss].view(np.uint32), w[miss].view(np.uint32)), "pixels whose camera ray misses"
+    first = int(hit_pix[0])
+    assert np.array_equal(g[first].view(np.uint32), w[first].view(np.uint32)), "the pixel of hit slot 0"

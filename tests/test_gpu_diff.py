@@ -87,7 +87,9 @@ def test_adjoint_matches_central_differences(small):
             vals.append(float(l2_loss(out.double(), target.double())))
         fd = (vals[0] - vals[1]) / (2 * h)
         g = float(grads[name][idx])
-        assert abs(g - fd) <= 0.01 * abs(fd) + 2e-3 * scale[name], (name, idx, g, fd, scale[name])
+        # within 1% of the central difference; below 1e-3 of the largest
+        # gradient of the parameter kind, within 1e-5 of it (the benchmark's criterion)
+        assert abs(g - fd) <= 0.01 * max(abs(fd), 1e-3 * scale[name]), (name, idx, g, fd, scale[name])
 
 
 def test_inverse_rendering_reduces_loss(small):

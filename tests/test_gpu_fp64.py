@@ -62,3 +62,38 @@ def test_converged_image_against_independent_fp64_render(oracle, pk_built):
     z = m.mean() / (np.sqrt((se ** 2).sum()) / m.size)
     print("independent FP64 render: inside", float(inside.mean()), "z", float(z))
     assert inside.all() and abs(z) < 4.0
+
+
+def test_precision_soup_against_fp64(oracle, pk_built):
+    """The precision workload's scene family at reduced size: a seeded
+    triangle soup (200,000 triangles, the 8.4M soup's centroid and edge
+    distributions) with the 2048x1024 environment, 96x54, 8 frames of 4
+    bounces.  The GPU's converged image equals the FP32 oracle's bit for bit;
+    against the FP64 evaluation of the same light paths the per-pixel relative
+    error has median < 1e-6 and p99 < 1e-5, and once the FP64 evaluation takes
+    the FP32 texel choices (the measured cause of the outliers: nearest-texel
+    flips) no more than 0.1% of the values exceed 1e-4."""
+    src = synth.triangle_soup_scene(n_tris=200_000, width=96, height=54)
+    frames, bounces = 8, 4
+    pair = Pair(src, oracle, threads=16)
+    pair.ctx.call("pk_set_render_state", 0, 0.0)
+    pair.ctx.call("pk_render_frames", frames, bounces)
+    gpu = pair.image("accum")
+    rel = {}
+    for share in (False, True):
+        R = oracle.Prepared(src, threads=16).r if share else pair.P.r
+        R.set_track64(True, share_texels=share)
+        R.set_render_state(0)
+        for _ in range(frames):
+            R.tick(bounces)
+        if not share:
+            assert_bits_equal(gpu, R.accum(), "GPU vs FP32 oracle (soup)")
+        a64 = R.accum64()[..., :3]
+        d = np.abs(gpu[..., :3].astype(np.float64) - a64)
+        lit = a64 > 1e-6
+        rel[share] = d[lit] / a64[lit]
+    r = rel[False]
+    print("soup FP64: median", float(np.median(r)), "p99", float(np.percentile(r, 99)), "max", float(r.max()),
+          "above 1e-4", int((r > 1e-4).sum()), "shared texels above 1e-4", int((rel[True] > 1e-4).sum()))
+    assert np.median(r) < 1e-6 and np.percentile(r, 99) < 1e-5
+    assert (rel[True] > 1e-4).mean() <= 1e-3
