@@ -420,8 +420,11 @@ __device__ __forceinline__ uint2 cw_pop(uint2 (*sstack)[TRACE_THREADS], const ui
   return sp < CW_STACK_SMEM ? sstack[sp][tid] : lstack[sp - CW_STACK_SMEM];
 }
 
+#ifndef PK_CW_MINBLOCKS
+#define PK_CW_MINBLOCKS 10
+#endif
 template <bool ANY, bool FUSED, bool COUNT>
-__global__ void __launch_bounds__(TRACE_THREADS) k_trace_cw(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+__global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                              const uint32_t* __restrict__ countp, RayQ R,
                                                              uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
                                                              float4* __restrict__ color, uint32_t npix,

@@ -155,43 +155,162 @@ int node_boxes(const int32_t* nodes5, uint32_t n_nodes, uint32_t n_tris, const s
   return 0;
 }
 
-// A child candidate of a wide node: a binary inner node, or a range of
-// leaf-ordered triangles (a binary leaf, or part of one).
+// A child candidate of a wide node: a binary inner node (a wide node of its
+// own), a range of leaf-ordered triangles (part of a binary leaf), or a binary
+// subtree of at most LEAF_MAX triangles taken as one leaf child.
 struct Item {
-  uint32_t kind;  // 0 binary inner node, 1 triangle range
+  uint32_t kind;  // 0 binary inner node, 1 triangle range, 2 subtree as one leaf
   uint32_t a;     // node index, or first triangle
-  uint32_t n;     // triangle count (ranges)
+  uint32_t n;     // triangle count
 };
 
 constexpr uint32_t LEAF_MAX = 3;
+// SAH weights of the collapse: one wide-node visit (eight child tests) and
+// one triangle test, per unit of surface area of the box tested.
+constexpr float COST_NODE = 1.0f, COST_TRI = 0.3f;
+constexpr uint8_t OPT_LEAF = 0xf0, OPT_INNER = 0xf1;  // else: split, j slots to the left child
+
+// The SAH-optimal collapse of Ylitie et al. (HPG 2017, section 3.1): for
+// every binary node n and slot budget i (1..8), cost[n][i] is the cheapest
+// way to represent n's subtree with at most i children of a wide node: one
+// leaf child (subtree of at most LEAF_MAX triangles: area * COST_TRI *
+// triangles), one internal child (a wide node: area * COST_NODE + the best
+// distribution of n's two children over 8 slots), or (i >= 2) its two
+// children sharing the i slots.  Computed bottom-up, one binary level at a
+// time, each level in parallel.
+struct Collapse {
+  std::vector<float> cost;     // 8 per node (budgets 1..8)
+  std::vector<uint8_t> opt;    // 8 per node
+  std::vector<uint8_t> split;  // left child's slots in the node's own 8-slot distribution
+  std::vector<uint32_t> tris;  // triangles in the subtree
+
+  void run(const int32_t* nodes5, uint32_t n_nodes, const std::vector<DBox>& nbox) {
+    cost.assign(8 * (size_t)n_nodes, 0.0f);
+    opt.assign(8 * (size_t)n_nodes, OPT_LEAF);
+    split.assign(n_nodes, 1);
+    tris.assign(n_nodes, 0);
+    std::vector<uint32_t> depth(n_nodes, 0);
+    uint32_t maxd = 0;
+    for (uint32_t n = 0; n < n_nodes; n++) {
+      const int32_t* nd = nodes5 + 5 * (size_t)n;
+      if (nd[1] <= -1) depth[nd[0]] = depth[nd[0] + 1] = depth[n] + 1;
+      maxd = std::max(maxd, depth[n]);
+    }
+    std::vector<uint32_t> start(maxd + 2, 0), order(n_nodes);
+    for (uint32_t n = 0; n < n_nodes; n++) start[depth[n] + 1]++;
+    for (uint32_t d = 0; d <= maxd; d++) start[d + 1] += start[d];
+    {
+      std::vector<uint32_t> at(start.begin(), start.end() - 1);
+      for (uint32_t n = 0; n < n_nodes; n++) order[at[depth[n]]++] = n;
+    }
+    const float INF = INFINITY;
+    for (int64_t d = maxd; d >= 0; d--) {
+      const uint32_t b = start[d], e = start[d + 1];
+      parallel_for(e - b, [&](size_t lo, size_t hi) {
+        for (size_t k = lo; k < hi; k++) {
+          const uint32_t n = order[b + k];
+          const int32_t* nd = nodes5 + 5 * (size_t)n;
+          float* C = &cost[8 * (size_t)n];
+          uint8_t* O = &opt[8 * (size_t)n];
+          const double area = nbox[n].area();
+          if (nd[1] > -1) {
+            const uint32_t t = (uint32_t)nd[1] >> 24;
+            tris[n] = t;
+            const float leaf = t <= LEAF_MAX ? (float)(area * COST_TRI * t) : INF;
+            const float inner = t > LEAF_MAX ? (float)(area * (COST_NODE + COST_TRI * t)) : INF;
+            for (int i = 0; i < 8; i++) {
+              C[i] = std::min(leaf, inner);
+              O[i] = leaf <= inner ? OPT_LEAF : OPT_INNER;
+            }
+            continue;
+          }
+          const uint32_t l = (uint32_t)nd[0], r = l + 1;
+          tris[n] = tris[l] + tris[r];
+          const float* Cl = &cost[8 * (size_t)l];
+          const float* Cr = &cost[8 * (size_t)r];
+          float D[8];
+          uint8_t J[8];
+          D[0] = INF;
+          J[0] = 1;
+          for (int i = 2; i <= 8; i++) {  // i slots, j of them to the left
+            float best = INF;
+            uint8_t bj = 1;
+            for (int j = 1; j < i; j++) {
+              const float c = Cl[j - 1] + Cr[i - j - 1];
+              if (c < best) { best = c; bj = (uint8_t)j; }
+            }
+            D[i - 1] = best;
+            J[i - 1] = bj;
+          }
+          split[n] = J[7];
+          const float leaf = tris[n] <= LEAF_MAX ? (float)(area * COST_TRI * tris[n]) : INF;
+          const float inner = (float)(area * COST_NODE) + D[7];
+          C[0] = std::min(leaf, inner);
+          O[0] = leaf <= inner ? OPT_LEAF : OPT_INNER;
+          for (int i = 1; i < 8; i++) {
+            C[i] = C[i - 1];
+            O[i] = O[i - 1];
+            if (D[i] < C[i]) { C[i] = D[i]; O[i] = J[i]; }
+          }
+        }
+      });
+    }
+  }
+};
 
 struct Builder {
   const int32_t* nodes5;
   const std::vector<DBox>& tbox;
   const std::vector<DBox>& nbox;  // widened binary node boxes
+  const Collapse& dp;
 
+  bool is_leaf(uint32_t n) const { return nodes5[5 * (size_t)n + 1] > -1; }
   Item item_of(uint32_t node) const {
     const int32_t t = nodes5[5 * (size_t)node + 1];
     if (t > -1) return Item{1u, (uint32_t)t & 0x00ffffffu, (uint32_t)t >> 24};
     return Item{0u, node, 0u};
   }
   DBox box_of(const Item& it) const {
-    if (it.kind == 0) return nbox[it.a];
+    if (it.kind != 1) return nbox[it.a];
     DBox b;
     for (uint32_t k = 0; k < it.n; k++) b.add(tbox[it.a + k]);
     widen(b);
     return b;
   }
-  bool openable(const Item& it) const { return it.kind == 0 || it.n > LEAF_MAX; }
-  void open(const Item& it, Item& l, Item& r) const {
-    if (it.kind == 0) {
-      const uint32_t c = (uint32_t)nodes5[5 * (size_t)it.a];
-      l = item_of(c);
-      r = item_of(c + 1);
+  bool openable(const Item& it) const { return it.kind == 0 || (it.kind == 1 && it.n > LEAF_MAX); }
+  // The leaf-ordered triangles of a leaf child, in order.
+  void leaf_tris(const Item& it, uint32_t (&out)[LEAF_MAX], uint32_t& count) const {
+    count = 0;
+    if (it.kind == 1) {
+      for (uint32_t k = 0; k < it.n && count < LEAF_MAX; k++) out[count++] = it.a + k;
+      return;
+    }
+    uint32_t stack[64];
+    int sp = 0;
+    stack[sp++] = it.a;
+    while (sp) {
+      const uint32_t n = stack[--sp];
+      const int32_t* nd = nodes5 + 5 * (size_t)n;
+      if (nd[1] > -1) {
+        const uint32_t w = (uint32_t)nd[1];
+        for (uint32_t k = 0; k < (w >> 24) && count < LEAF_MAX; k++) out[count++] = (w & 0x00ffffffu) + k;
+      } else if (sp + 2 <= 64) {
+        stack[sp++] = (uint32_t)nd[0] + 1;
+        stack[sp++] = (uint32_t)nd[0];
+      }
+    }
+  }
+  // The children that binary node n's subtree contributes with a budget of i slots.
+  void collect(uint32_t n, int i, Item* ch, int& nc) const {
+    const uint8_t o = dp.opt[8 * (size_t)n + (i - 1)];
+    if (o == OPT_LEAF) {
+      ch[nc++] = is_leaf(n) ? item_of(n) : Item{2u, n, dp.tris[n]};
+    } else if (o == OPT_INNER) {
+      ch[nc++] = item_of(n);  // an inner node, or a binary leaf of more than LEAF_MAX triangles (a range)
     } else {
-      const uint32_t h = it.n / 2;
-      l = Item{1u, it.a, h};
-      r = Item{1u, it.a + h, it.n - h};
+      const uint32_t l = (uint32_t)nodes5[5 * (size_t)n];
+      collect(l, o, ch, nc);
+      collect(l + 1, i - o, ch, nc);
     }
   }
 
@@ -201,38 +320,36 @@ struct Builder {
     Item ch[8];
     DBox cb[8];
     int nc = 0;
-    if (openable(it)) {
-      open(it, ch[0], ch[1]);
+    if (it.kind == 0) {
+      const uint32_t l = (uint32_t)nodes5[5 * (size_t)it.a];
+      const int j = dp.split[it.a];
+      collect(l, j, ch, nc);
+      collect(l + 1, 8 - j, ch, nc);
+    } else if (openable(it)) {  // a long range: halves, opened largest first
+      const uint32_t h = it.n / 2;
+      ch[0] = Item{1u, it.a, h};
+      ch[1] = Item{1u, it.a + h, it.n - h};
       nc = 2;
+      while (nc < 8) {
+        int best = -1;
+        double best_a = -1.0;
+        for (int k = 0; k < nc; k++) {
+          if (!openable(ch[k])) continue;
+          const double a = box_of(ch[k]).area();
+          if (a > best_a) { best_a = a; best = k; }
+        }
+        if (best < 0) break;
+        const Item o = ch[best];
+        for (int k = nc; k > best + 1; k--) ch[k] = ch[k - 1];
+        ch[best] = Item{1u, o.a, o.n / 2};
+        ch[best + 1] = Item{1u, o.a + o.n / 2, o.n - o.n / 2};
+        nc++;
+      }
     } else {
       ch[0] = it;
       nc = 1;
     }
     for (int k = 0; k < nc; k++) cb[k] = box_of(ch[k]);
-    while (nc < 8) {
-      int best = -1;
-      double best_a = -1.0;
-      for (int k = 0; k < nc; k++) {
-        if (!openable(ch[k])) continue;
-        const double a = cb[k].area();
-        if (a > best_a) {
-          best_a = a;
-          best = k;
-        }
-      }
-      if (best < 0) break;
-      Item l, r;
-      open(ch[best], l, r);
-      for (int k = nc; k > best + 1; k--) {
-        ch[k] = ch[k - 1];
-        cb[k] = cb[k - 1];
-      }
-      ch[best] = l;
-      cb[best] = box_of(l);
-      ch[best + 1] = r;
-      cb[best + 1] = box_of(r);
-      nc++;
-    }
     // octant slots: cost(child, s) = dot(centre offset, sign vector of s);
     // repeatedly take the cheapest free (child, slot) pair
     DBox all;
@@ -282,7 +399,9 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4,
   if (triangle_data(tri4, n_tris, verts4, n_verts, tbox, brecs, why)) return 1;
   if (node_boxes(nodes5, n_nodes, n_tris, tbox, nbox, why)) return 1;
   for (DBox& b : nbox) widen(b);
-  const Builder B{nodes5, tbox, nbox};
+  Collapse dp;
+  dp.run(nodes5, n_nodes, nbox);
+  const Builder B{nodes5, tbox, nbox, dp};
 
   struct Plan {
     Item slot[8];
@@ -358,11 +477,13 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4,
             inner_rank++;
           } else {
             if (c.n == 0) continue;
-            meta[s] = (uint8_t)((((1u << c.n) - 1u) << 5) | tri_off);
-            for (uint32_t k = 0; k < c.n; k++)
+            uint32_t ids[LEAF_MAX], cnt = 0;
+            B.leaf_tris(c, ids, cnt);
+            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | tri_off);
+            for (uint32_t k = 0; k < cnt; k++)
               std::memcpy(&T[(size_t)WIDE_TRI_FLOATS * (tri0[i] + tri_off + k)],
-                          &brecs[(size_t)WIDE_TRI_FLOATS * (c.a + k)], WIDE_TRI_FLOATS * sizeof(float));
-            tri_off += c.n;
+                          &brecs[(size_t)WIDE_TRI_FLOATS * ids[k]], WIDE_TRI_FLOATS * sizeof(float));
+            tri_off += cnt;
           }
           const DBox& cb = p.sbox[s];
           if (cb.empty()) continue;  // all-zero planes at the frame origin: hit tests may pass, no triangles
