@@ -163,6 +163,11 @@ struct pk_ctx {
   float kind_n[pk::N_KINDS] = {0};
   unsigned long long frames = 0;
   unsigned long long diff_rays = 0;  // rays of the last differentiable render / adjoint
+  // the differentiable renderer's environment sampling tables (pk_diff_set_env_sampling)
+  uint32_t diff_env_w = 0, diff_env_h = 0, diff_env_nb = 0;
+  DevBuf<int2> diff_bins, diff_coords;
+  DevBuf<float> diff_pdf;
+  bool diff_env_ready = false;
   void* cast_scratch = nullptr;  // pk_cast_rays_noalloc's static scratch on this device (set by pk_create)
 
   RayQ R(int i) { return slot[0].R(i); }

@@ -32,6 +32,20 @@ __global__ void k_env_radiance(const uchar4* __restrict__ rgbe, uint32_t n, doub
   vals[i] = i;
 }
 
+// The same radiance for an FP32 RGB map (the differentiable renderer's
+// environment): luma of the stored values, in double.
+__global__ void k_env_radiance_f32(const float* __restrict__ rgb, uint32_t n, double* __restrict__ rad,
+                                   unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double r = 0.2126 * (double)rgb[3 * (size_t)i] + 0.7152 * (double)rgb[3 * (size_t)i + 1] +
+                   0.0722 * (double)rgb[3 * (size_t)i + 2];
+  const double v = r > 0.0 ? r : 0.0;  // negative or NaN radiance is never sampled
+  rad[i] = v;
+  keys[i] = ~(unsigned long long)__double_as_longlong(v);
+  vals[i] = i;
+}
+
 // totalRadiance += rad (row-major) and brightestTexel = max(rad, brightest).
 __global__ void k_env_total(const double* __restrict__ rad, uint32_t n, double* __restrict__ out2) {
   const int lane = threadIdx.x;
@@ -100,15 +114,17 @@ double js_max(double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a
 
 }  // namespace
 
-// Builds bins (<= 257 entries), sorted coordinates and the pdf for a w x h
-// RGBE image already on the device.  Returns non-zero with a reason on failure.
-int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
-                         uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why) {
+namespace {
+
+// The tables from per-texel radiance `rad` with sort keys and values already
+// set (the radiance kernels above).
+int build_from_radiance(cudaStream_t s, uint32_t w, uint32_t h, DevBuf<double>& rad,
+                        DevBuf<unsigned long long>& keys, DevBuf<uint32_t>& vals, DevBuf<int2>& bins_out,
+                        uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why) {
   const uint32_t n = w * h;
-  DevBuf<double> rad(n), tot(2);
-  DevBuf<unsigned long long> keys(n), keys_tmp(n);
-  DevBuf<uint32_t> vals(n), vals_tmp(n), nb(1);
-  k_env_radiance<<<(n + 255) / 256, 256, 0, s>>>(rgbe, n, rad.p, keys.p, vals.p);
+  DevBuf<double> tot(2);
+  DevBuf<unsigned long long> keys_tmp(n);
+  DevBuf<uint32_t> vals_tmp(n), nb(1);
   k_env_total<<<1, 32, 0, s>>>(rad.p, n, tot.p);
   check(cudaGetLastError(), "env radiance");
   radix_sort_pairs_u64(s, reinterpret_cast<uint64_t*>(keys.p), vals.p, reinterpret_cast<uint64_t*>(keys_tmp.p),
@@ -137,6 +153,31 @@ int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_
   check(cudaStreamSynchronize(s), "sync");
   nb_out = nbh;
   return 0;
+}
+
+}  // namespace
+
+// Builds bins (<= 257 entries), sorted coordinates and the pdf for a w x h
+// RGBE image already on the device.  Returns non-zero with a reason on failure.
+int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
+                         uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why) {
+  const uint32_t n = w * h;
+  DevBuf<double> rad(n);
+  DevBuf<unsigned long long> keys(n);
+  DevBuf<uint32_t> vals(n);
+  k_env_radiance<<<(n + 255) / 256, 256, 0, s>>>(rgbe, n, rad.p, keys.p, vals.p);
+  return build_from_radiance(s, w, h, rad, keys, vals, bins_out, nb_out, coords_out, pdf_out, why);
+}
+
+// The same tables for an FP32 RGB map (w x h x 3 on the device).
+int build_env_tables_gpu_f32(cudaStream_t s, const float* rgb, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
+                             uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why) {
+  const uint32_t n = w * h;
+  DevBuf<double> rad(n);
+  DevBuf<unsigned long long> keys(n);
+  DevBuf<uint32_t> vals(n);
+  k_env_radiance_f32<<<(n + 255) / 256, 256, 0, s>>>(rgb, n, rad.p, keys.p, vals.p);
+  return build_from_radiance(s, w, h, rad, keys, vals, bins_out, nb_out, coords_out, pdf_out, why);
 }
 
 }  // namespace pk

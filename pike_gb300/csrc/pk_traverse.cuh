@@ -44,6 +44,30 @@ __device__ __forceinline__ float snorm_hi(int m) { return snorm16_decode((int)(i
 __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, float ox, float oy, float oz, float ix,
                                                float iy, float iz, float& lh, float& rh, int& cl, int& cr);
 
+// trace.wgsl:97-114: Moller-Trumbore on one leaf-ordered triangle record
+// {v0.xyz, e1.x}{e1.yz, e2.xy}{e2.z}.  Returns false where the reference
+// `continue`s (parallel ray, u or v outside the triangle); otherwise res = the
+// distance when it exceeds eps, else MAX_T.
+__device__ __forceinline__ bool mt_test(const SceneDev& sc, int idx, float ox, float oy, float oz, float dx,
+                                        float dy, float dz, float eps, float& res, float& u, float& v) {
+  const float4* tp = sc.tris + 3 * (size_t)idx;
+  const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
+  const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
+  const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+  const float det = e1x * px + e1y * py + e1z * pz;
+  if (fabsf(det) < eps) return false;
+  const float inv_det = 1.0f / det;
+  const float tx = ox - A.x, ty = oy - A.y, tz = oz - A.z;
+  u = (tx * px + ty * py + tz * pz) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+  v = (dx * qx + dy * qy + dz * qz) * inv_det;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
+  res = dist > eps ? dist : MAX_T;
+  return true;
+}
+
 constexpr int TRACE_THREADS = 128;
 constexpr int STACK_SMEM = 32;   // per-thread entries kept in shared memory
 constexpr int STACK_LOCAL = 32;  // overflow entries in local memory (total depth 64)
@@ -114,21 +138,8 @@ __device__ __forceinline__ void traverse_rt(const bool ANY, const SceneDev& sc, 
       const int base = (int)(word & 0x00ffffffu);
       for (int i = 0; i < size; i++) {
         if (COUNT) ntest += 1;
-        const float4* tp = sc.tris + 3 * (size_t)(base + i);
-        const float4 A = __ldg(tp), B = __ldg(tp + 1), Cc = __ldg(tp + 2);
-        const float e1x = A.w, e1y = B.x, e1z = B.y, e2x = B.z, e2y = B.w, e2z = Cc.x;
-        const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
-        const float det = e1x * px + e1y * py + e1z * pz;
-        if (fabsf(det) < eps) continue;
-        const float inv_det = 1.0f / det;
-        const float tx = ox - A.x, ty = oy - A.y, tz = oz - A.z;
-        const float u = (tx * px + ty * py + tz * pz) * inv_det;
-        if (u < 0.0f || u > 1.0f) continue;
-        const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
-        const float v = (dx * qx + dy * qy + dz * qz) * inv_det;
-        if (v < 0.0f || u + v > 1.0f) continue;
-        const float dist = (e2x * qx + e2y * qy + e2z * qz) * inv_det;
-        const float res = dist > eps ? dist : MAX_T;
+        float res, u, v;
+        if (!mt_test(sc, base + i, ox, oy, oz, dx, dy, dz, eps, res, u, v)) continue;
         if (res < best_t) {
           best_t = res;
           best_i = base + i;

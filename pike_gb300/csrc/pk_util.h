@@ -56,5 +56,9 @@ void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64
 // EnvironmentGenerator tables on the GPU (pk_env.cu).
 int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
                          uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why);
+// The same tables for an FP32 RGB map (w x h x 3): radiance = luma of the
+// stored values in double (the differentiable renderer's sampling tables).
+int build_env_tables_gpu_f32(cudaStream_t s, const float* rgb, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
+                             uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why);
 
 }  // namespace pk
