@@ -345,37 +345,50 @@ int pk_set_trace_mode(pk_ctx* ctx, int mode);
 int pk_math_eval(pk_ctx* ctx, int fn, const float* x, const float* y, float* out, uint32_t n);
 
 /* ---- form (3): differentiable rendering (no reference counterpart) -------
- * A path tracer over the loaded scene and BVH with continuous parameters and
- * its path-replay adjoint.  Paths are cosine-sampled, so they depend on the
- * seed only; the image is a smooth function of the parameters and
- * pk_diff_backward returns its exact derivative for those paths (what central
- * differences with common random numbers measure).  All array pointers are
- * DEVICE pointers owned by the caller (e.g. torch tensors); the calls block
- * until the work on the library's stream is done, so the caller must finish
- * its own writes to the inputs first.  Resolution comes from pk_configure. */
-typedef struct pk_diff_camera {
-  float origin[3];
-  float forward[3];  /* unit view direction */
-  float right[3];    /* scaled by tan(fov/2) * width/height */
-  float up[3];       /* scaled by tan(fov/2) */
-} pk_diff_camera;
+ * The drop-in's estimator rendered path by path over the loaded scene and BVH
+ * (camera.wgsl rays from pk_set_camera, trace.wgsl / trace_shadow.wgsl
+ * traversal, shade_hit.wgsl shading with GGX VNDF sampling, the Fresnel lobe
+ * choice, environment next-event estimation and power-heuristic MIS,
+ * shade_miss.wgsl), with base colour, roughness and metallic taken from
+ * per-material FP32 parameters and the environment radiance from an FP32 RGB
+ * equirect map (environment rotation: pk_set_render_state's env_theta), and
+ * its path-replay adjoint.  Shading random numbers are seeded with the bounce
+ * index (as in pk_batch) instead of the wavefront's hit-queue slot.
+ * Sampling is detached: normals are sampled with roughness_sampling and
+ * environment directions from the tables of pk_diff_set_env_sampling; each
+ * path is weighted by the ratio of the VNDF densities at roughness and at
+ * roughness_sampling, so with roughness == roughness_sampling the estimator is
+ * the drop-in's and, with the paths held fixed, a smooth function of the
+ * parameters whose exact derivative pk_diff_backward returns (what central
+ * differences with common random numbers measure, moving roughness only).
+ * All array pointers are DEVICE pointers owned by the caller (e.g. torch
+ * tensors); the calls block until the work on the library's stream is done,
+ * so the caller must finish its own writes to the inputs first.  Resolution
+ * comes from pk_configure. */
 typedef struct pk_diff_params {
-  const float* albedo3;    /* n_mats x 3 */
-  const float* roughness;  /* n_mats, alpha = roughness^2 */
-  const float* metallic;   /* n_mats */
-  uint32_t n_mats;         /* >= the scene's material count, <= 4096 */
-  const float* env_rgb;    /* env_h x env_w x 3 equirect radiance */
-  uint32_t env_w, env_h;
-  uint32_t spp, depth;     /* depth = rays per path, 1..8 */
-  uint32_t seed;
+  const float* albedo3;             /* n_mats x 3: base colour */
+  const float* roughness;           /* n_mats, alpha = roughness^2 */
+  const float* metallic;            /* n_mats (not differentiated) */
+  const float* roughness_sampling;  /* n_mats, or NULL (= roughness): the roughness normals are sampled with */
+  uint32_t n_mats;                  /* >= the scene's material count, <= 4096 */
+  const float* env_rgb;             /* env_h x env_w x 3 equirect radiance */
+  uint32_t env_w, env_h;            /* the size given to pk_diff_set_env_sampling */
+  uint32_t spp, depth;              /* depth = closest-hit rays per path, 1..8 */
+  uint32_t sample_base;             /* sample s uses camera.wgsl's `samples` = sample_base + s */
 } pk_diff_params;
-/* image4: width x height x 4 floats (rgb, 0). */
-int pk_diff_render(pk_ctx* ctx, const pk_diff_camera* cam, const pk_diff_params* params, float* image4);
+/* Environment sampling tables (env_sampler.js's histogram and pdf, from the
+ * luma of an FP32 RGB map, w x h x 3 on the device), held until the next call. */
+int pk_diff_set_env_sampling(pk_ctx* ctx, const float* env_rgb, uint32_t w, uint32_t h);
+int pk_diff_env_info(pk_ctx* ctx, uint32_t* w, uint32_t* h, uint32_t* nb);
+/* Host copies: bins2 (nb x 2), coords2 (w*h x 2), pdf (w*h). */
+int pk_diff_env_download(pk_ctx* ctx, int32_t* bins2, int32_t* coords2, float* pdf);
+/* image4: width x height x 4 floats (rgb, 0), the mean over spp. */
+int pk_diff_render(pk_ctx* ctx, const pk_diff_params* params, float* image4);
 /* d_image4: dLoss/dimage (width x height x 4); the gradients are ADDED to
  * g_albedo3 (n_mats x 3), g_roughness (n_mats) and g_env_rgb (env_h x env_w x 3). */
-int pk_diff_backward(pk_ctx* ctx, const pk_diff_camera* cam, const pk_diff_params* params, const float* d_image4,
-                     double* g_albedo3, double* g_roughness, double* g_env_rgb);
-/* Rays traced by the last pk_diff_render / pk_diff_backward call. */
+int pk_diff_backward(pk_ctx* ctx, const pk_diff_params* params, const float* d_image4, double* g_albedo3,
+                     double* g_roughness, double* g_env_rgb);
+/* Rays traced (closest hit and shadow) by the last pk_diff_render / pk_diff_backward call. */
 int pk_diff_rays(pk_ctx* ctx, unsigned long long* rays);
 
 /* ---- form (2): batched rendering (no reference counterpart) -------------

@@ -422,23 +422,15 @@ struct EnvTables {
   std::vector<float> pdf;          // r32f, texel (x + w*y)
   double total = 0, brightest = 0;
 };
-static inline EnvTables build_env(const uint8_t* rgbe, uint32_t w, uint32_t h) {
-  EnvTables e;
-  e.w = w; e.h = h;
-  const size_t N = (size_t)w * h;
-  e.rgbe.assign(rgbe, rgbe + 4 * N);
-  std::vector<double> rad(N);
-  // _sortPixels: y outer, x inner; _getRadiance = 2^(a-128) * luma / 255.
-  for (uint32_t y = 0; y < h; y++) {
-    for (uint32_t x = 0; x < w; x++) {
-      const uint8_t* c = rgbe + 4 * ((size_t)y * w + x);
-      double power = std::ldexp(1.0, (int)c[3] - 128);
-      double luma = 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2];
-      double r = power * luma / 255.0;
-      e.brightest = js_max(r, e.brightest);
-      e.total += r;
-      rad[(size_t)y * w + x] = r;
-    }
+// The tables from per-texel radiance in row-major order (_sortPixels: y
+// outer, x inner): totalRadiance and brightestTexel accumulated in that order,
+// stable descending sort, equal-mass bins, pdf.
+static inline void build_env_from_rad(EnvTables& e, const std::vector<double>& rad) {
+  const uint32_t w = e.w;
+  const size_t N = rad.size();
+  for (size_t i = 0; i < N; i++) {
+    e.brightest = js_max(rad[i], e.brightest);
+    e.total += rad[i];
   }
   std::vector<int32_t> order(N);
   for (size_t i = 0; i < N; i++) order[i] = (int32_t)i;
@@ -478,6 +470,36 @@ static inline EnvTables build_env(const uint8_t* rgbe, uint32_t w, uint32_t h) {
       e.pdf[order[i]] = (float)pdf;
     }
   }
+}
+static inline EnvTables build_env(const uint8_t* rgbe, uint32_t w, uint32_t h) {
+  EnvTables e;
+  e.w = w; e.h = h;
+  const size_t N = (size_t)w * h;
+  e.rgbe.assign(rgbe, rgbe + 4 * N);
+  std::vector<double> rad(N);
+  // _getRadiance = 2^(a-128) * luma / 255.
+  for (size_t i = 0; i < N; i++) {
+    const uint8_t* c = rgbe + 4 * i;
+    double power = std::ldexp(1.0, (int)c[3] - 128);
+    double luma = 0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2];
+    rad[i] = power * luma / 255.0;
+  }
+  build_env_from_rad(e, rad);
+  return e;
+}
+// The same tables for an FP32 RGB map (the differentiable renderer's
+// sampling environment, pk_diff_set_env_sampling): radiance = luma of the
+// stored values in double, negative or NaN radiance taken as 0.
+static inline EnvTables build_env_f32(const float* rgb, uint32_t w, uint32_t h) {
+  EnvTables e;
+  e.w = w; e.h = h;
+  const size_t N = (size_t)w * h;
+  std::vector<double> rad(N);
+  for (size_t i = 0; i < N; i++) {
+    const double r = 0.2126 * (double)rgb[3 * i] + 0.7152 * (double)rgb[3 * i + 1] + 0.0722 * (double)rgb[3 * i + 2];
+    rad[i] = r > 0.0 ? r : 0.0;
+  }
+  build_env_from_rad(e, rad);
   return e;
 }
 

@@ -126,6 +126,14 @@ void* or_env_build(const uint8_t* rgbe, uint32_t w, uint32_t h) {
     return nullptr;
   }
 }
+void* or_env_build_f32(const float* rgb, uint32_t w, uint32_t h) {
+  try {
+    return new EnvTables(build_env_f32(rgb, w, h));
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
 void or_env_free(void* h) { delete (EnvTables*)h; }
 size_t or_env_num_bins(void* h) { return ((EnvTables*)h)->bins2.size() / 2; }
 void or_env_copy(void* h, int32_t* bins2, int32_t* coords2, float* pdf, double* total_brightest) {
@@ -343,35 +351,36 @@ int or_render64_read(void* p, int which, double* out) {
   return 0;
 }
 
-// Differentiable path tracer (pk_diff.cu) in binary64: image and gradient.
-static DiffScene diff_scene(void* p, const float* cam12, const double* albedo, const double* rough,
-                            const double* metal, uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h,
-                            uint32_t spp, uint32_t depth, uint32_t seed, uint32_t W, uint32_t H) {
+// Differentiable renderer (pk_diff.cu) in binary64: image and gradient.  The
+// renderer supplies scene, BVH, atlas, camera and env rotation; `tables` is an
+// or_env_build_f32 handle of the sampling environment.
+static DiffScene diff_scene(void* p, uint32_t W, uint32_t H, const double* albedo, const double* rough,
+                            const double* rough0, const double* metal, uint32_t n_mats, const double* env,
+                            uint32_t env_w, uint32_t env_h, void* tables, uint32_t spp, uint32_t depth,
+                            uint32_t sample_base) {
   DiffScene S;
   S.r = (Renderer*)p;
-  for (int k = 0; k < 3; k++) {
-    S.cam.o[k] = cam12[k];
-    S.cam.f[k] = cam12[3 + k];
-    S.cam.r[k] = cam12[6 + k];
-    S.cam.u[k] = cam12[9 + k];
-  }
   S.W = W; S.H = H;
-  S.albedo = albedo; S.rough = rough; S.metal = metal; S.n_mats = n_mats;
+  S.albedo = albedo; S.rough = rough; S.rough0 = rough0; S.metal = metal; S.n_mats = n_mats;
   S.env = env; S.env_w = (int)env_w; S.env_h = (int)env_h;
-  S.spp = (int)spp; S.depth = (int)depth; S.seed = seed;
+  S.tab = (const EnvTables*)tables;
+  S.spp = (int)spp; S.depth = (int)depth; S.sample_base = sample_base;
   return S;
 }
-uint64_t or_diff_render(void* p, const float* cam12, const double* albedo, const double* rough, const double* metal,
-                        uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h, uint32_t spp,
-                        uint32_t depth, uint32_t seed, uint32_t W, uint32_t H, double* image3) {
-  const DiffScene S = diff_scene(p, cam12, albedo, rough, metal, n_mats, env, env_w, env_h, spp, depth, seed, W, H);
+uint64_t or_diff_render(void* p, uint32_t W, uint32_t H, const double* albedo, const double* rough,
+                        const double* rough0, const double* metal, uint32_t n_mats, const double* env, uint32_t env_w,
+                        uint32_t env_h, void* tables, uint32_t spp, uint32_t depth, uint32_t sample_base,
+                        double* image3) {
+  const DiffScene S =
+      diff_scene(p, W, H, albedo, rough, rough0, metal, n_mats, env, env_w, env_h, tables, spp, depth, sample_base);
   return diff_render(S, image3, ((Renderer*)p)->nthreads);
 }
-void or_diff_grad(void* p, const float* cam12, const double* albedo, const double* rough, const double* metal,
-                  uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h, uint32_t spp, uint32_t depth,
-                  uint32_t seed, uint32_t W, uint32_t H, const double* dimage3, double* g_albedo, double* g_rough,
-                  double* g_env) {
-  const DiffScene S = diff_scene(p, cam12, albedo, rough, metal, n_mats, env, env_w, env_h, spp, depth, seed, W, H);
+void or_diff_grad(void* p, uint32_t W, uint32_t H, const double* albedo, const double* rough, const double* rough0,
+                  const double* metal, uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h,
+                  void* tables, uint32_t spp, uint32_t depth, uint32_t sample_base, const double* dimage3,
+                  double* g_albedo, double* g_rough, double* g_env) {
+  const DiffScene S =
+      diff_scene(p, W, H, albedo, rough, rough0, metal, n_mats, env, env_w, env_h, tables, spp, depth, sample_base);
   diff_gradient(S, dimage3, g_albedo, g_rough, g_env, ((Renderer*)p)->nthreads);
 }
 

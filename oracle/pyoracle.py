@@ -35,7 +35,7 @@ def lib():
         build()
         _lib = C.CDLL(_LIB)
         _lib.or_last_error.restype = C.c_char_p
-        for name in ("or_bvh_build", "or_env_build", "or_renderer_new"):
+        for name in ("or_bvh_build", "or_env_build", "or_env_build_f32", "or_renderer_new"):
             getattr(_lib, name).restype = C.c_void_p
         _lib.or_env_num_bins.restype = C.c_size_t
         _lib.or_shadow_offset.restype = C.c_size_t
@@ -165,6 +165,34 @@ class Env:
         self.total, self.brightest = float(tb[0]), float(tb[1])
 
 
+class EnvF32:
+    """The differentiable renderer's sampling tables of an FP32 RGB map (h, w, 3)
+    (pk_diff_set_env_sampling): bins (nb,2), coords (N,2), pdf (h,w); the C
+    handle stays alive for the oracle's diff_render / diff_grad."""
+
+    def __init__(self, rgb: np.ndarray):
+        L = lib()
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        h, w = rgb.shape[:2]
+        hd = L.or_env_build_f32(_p(rgb), C.c_uint32(w), C.c_uint32(h))
+        if not hd:
+            _err("or_env_build_f32")
+        self._h = hd
+        nb = int(L.or_env_num_bins(C.c_void_p(hd)))
+        self.w, self.h = w, h
+        self.bins = np.zeros((nb, 2), np.int32)
+        self.coords = np.zeros((w * h, 2), np.int32)
+        self.pdf = np.zeros((h, w), np.float32)
+        tb = np.zeros(2, np.float64)
+        L.or_env_copy(C.c_void_p(hd), _p(self.bins), _p(self.coords), _p(self.pdf), _p(tb))
+        self.total, self.brightest = float(tb[0]), float(tb[1])
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.or_env_free(C.c_void_p(self._h))
+            self._h = None
+
+
 def camera_bytes(state: dict, width: int, height: int) -> bytes:
     """CameraStateStuct (structs.js:235-249) with dimsMask = W<<16 | H (camera_pass.js:118-125)."""
     dims = ((width & 0xFFFF) << 16) | (height & 0xFFFF)
@@ -283,31 +311,35 @@ class Renderer:
         lib().or_trace_rays(self.p, _p(rays8), C.c_size_t(rays8.shape[0]), C.c_int(1 if any_hit else 0), _p(out))
         return out
 
-    def _diff_args(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H):
-        self._dkeep = [np.ascontiguousarray(cam12, np.float32), np.ascontiguousarray(albedo, np.float64),
-                       np.ascontiguousarray(rough, np.float64), np.ascontiguousarray(metal, np.float64),
-                       np.ascontiguousarray(env, np.float64)]
-        c, a, r, m, e = self._dkeep
-        return [self.p, _p(c), _p(a), _p(r), _p(m), C.c_uint32(r.shape[0]), _p(e), C.c_uint32(e.shape[1]),
-                C.c_uint32(e.shape[0]), C.c_uint32(spp), C.c_uint32(depth), C.c_uint32(seed), C.c_uint32(W),
-                C.c_uint32(H)]
+    def _diff_args(self, W, H, albedo, rough, metal, env, tables, spp, depth, sample_base, rough0):
+        rough0 = rough if rough0 is None else rough0
+        self._dkeep = [np.ascontiguousarray(albedo, np.float64), np.ascontiguousarray(rough, np.float64),
+                       np.ascontiguousarray(rough0, np.float64), np.ascontiguousarray(metal, np.float64),
+                       np.ascontiguousarray(env, np.float64), tables]
+        a, r, r0, m, e, _ = self._dkeep
+        assert (e.shape[1], e.shape[0]) == (tables.w, tables.h)
+        return [self.p, C.c_uint32(W), C.c_uint32(H), _p(a), _p(r), _p(r0), _p(m), C.c_uint32(r.shape[0]), _p(e),
+                C.c_uint32(e.shape[1]), C.c_uint32(e.shape[0]), C.c_void_p(tables._h), C.c_uint32(spp),
+                C.c_uint32(depth), C.c_uint32(sample_base)]
 
-    def diff_render(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H):
-        """FP64 oracle of pk_diff_render: (H, W, 3) image and the rays traced."""
+    def diff_render(self, W, H, albedo, rough, metal, env, tables, spp, depth, sample_base=0, rough0=None):
+        """FP64 oracle of pk_diff_render (camera and env rotation: set_camera,
+        set_render_state): (H, W, 3) image and the rays traced."""
         img = np.zeros((H, W, 3), np.float64)
         L = lib()
         L.or_diff_render.restype = C.c_uint64
-        rays = L.or_diff_render(*self._diff_args(cam12, albedo, rough, metal, env, spp, depth, seed, W, H), _p(img))
+        rays = L.or_diff_render(*self._diff_args(W, H, albedo, rough, metal, env, tables, spp, depth, sample_base,
+                                                 rough0), _p(img))
         return img, int(rays)
 
-    def diff_grad(self, cam12, albedo, rough, metal, env, spp, depth, seed, W, H, dimage):
+    def diff_grad(self, W, H, albedo, rough, metal, env, tables, spp, depth, dimage, sample_base=0, rough0=None):
         """FP64 oracle of pk_diff_backward for dLoss/dimage = dimage (H, W, 3)."""
         d = np.ascontiguousarray(dimage, np.float64)
         ga = np.zeros((np.asarray(albedo).shape[0], 3))
         gr = np.zeros(np.asarray(rough).shape[0])
         ge = np.zeros(np.asarray(env).shape)
-        lib().or_diff_grad(*self._diff_args(cam12, albedo, rough, metal, env, spp, depth, seed, W, H), _p(d), _p(ga),
-                           _p(gr), _p(ge))
+        lib().or_diff_grad(*self._diff_args(W, H, albedo, rough, metal, env, tables, spp, depth, sample_base, rough0),
+                           _p(d), _p(ga), _p(gr), _p(ge))
         return ga, gr, ge
 
     def set_track64(self, on: bool = True, share_texels: bool = False):

@@ -39,6 +39,21 @@ class CameraState(C.Structure):
                 ("invocation_offset", C.c_uint32)]
 
 
+def camera_struct(state: dict) -> CameraState:
+    """pk_camera_state of a CameraState dict (pos, dir, fov, focalDepth,
+    apertureSize, distortion, bokeh, invocationOffset)."""
+    cs = CameraState()
+    cs.pos[:] = [float(v) for v in state["pos"]]
+    cs.dir[:] = [float(v) for v in state["dir"]]
+    cs.fov = float(state["fov"])
+    cs.focal_depth = float(state.get("focalDepth", 0.5))
+    cs.aperture_size = float(state.get("apertureSize", 0.0))
+    cs.distortion = float(state.get("distortion", 0.0))
+    cs.bokeh = float(state.get("bokeh", 0.5))
+    cs.invocation_offset = int(state.get("invocationOffset", 0))
+    return cs
+
+
 _lib = None
 _P = C.c_void_p
 
@@ -68,8 +83,9 @@ def load(path: str = LIB_PATH):
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
         "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
         "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P, _P],
-        "pk_diff_render": [_P, _P, _P, _P], "pk_diff_backward": [_P, _P, _P, _P, _P, _P, _P],
-        "pk_diff_rays": [_P, _P],
+        "pk_diff_render": [_P, _P, _P], "pk_diff_backward": [_P, _P, _P, _P, _P, _P],
+        "pk_diff_rays": [_P, _P], "pk_diff_set_env_sampling": [_P, _P, u32, u32],
+        "pk_diff_env_info": [_P, _P, _P, _P], "pk_diff_env_download": [_P, _P, _P, _P],
         "pk_batch_create": [_P, _P, u32], "pk_batch_destroy": [_P], "pk_batch_set_requests": [_P, _P, u32],
         "pk_batch_set_config": [_P, C.c_int, C.c_int, C.c_int], "pk_batch_get_config": [_P, _P, _P, _P],
         "pk_batch_autotune": [_P, C.c_uint64, _P], "pk_batch_render": [_P, u32], "pk_batch_reset": [_P],

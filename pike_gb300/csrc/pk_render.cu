@@ -137,8 +137,13 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 // boxes are truncated inward, so a hit can lie outside its leaf's box, and
 // testing a leaf later changes which boxes are culled and so, on rare rays,
 // the hit.  The counting variant keeps the reference order for its counts.
+// Measured on the 1080p benchmark (paired runs, same call), postponing was
+// slower: 2971-2976 Mrays/s against 3000-3002 without (the any-hit share of
+// the frame rose from 0.288 to 0.304: with about 2 leaves per shadow ray the
+// extra inner steps cost more than the coherent leaf tests save), so it is
+// off by default (PK_ANY_SPEC=1 builds it).
 #ifndef PK_ANY_SPEC
-#define PK_ANY_SPEC 1
+#define PK_ANY_SPEC 0
 #endif
 constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
 
@@ -440,8 +445,10 @@ __device__ __forceinline__ uint2 cw_pop(uint2 (*sstack)[TRACE_THREADS], const ui
   return sp < CW_STACK_SMEM ? sstack[sp][tid] : lstack[sp - CW_STACK_SMEM];
 }
 
+// 8 resident blocks per SM (64 registers): 2982 Mrays/s on the 1080p
+// benchmark against 2945 at 10 blocks and 2744 at 12 (same call).
 #ifndef PK_CW_MINBLOCKS
-#define PK_CW_MINBLOCKS 10
+#define PK_CW_MINBLOCKS 8
 #endif
 template <bool ANY, bool FUSED, bool COUNT>
 __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
