@@ -17,6 +17,7 @@
 #pragma once
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <vector>
 
 #include "om_render.h"
@@ -99,8 +100,13 @@ struct DiffScene {
 
 static const float DIFF_TAU_F = 6.283185307179586f;
 
+// pk_diff.cu clamp_y: the y component of an environment lookup direction
+// clamped to [-1, 1] (where it rounds beyond, acos would be NaN).
+static inline V3 clamp_y(V3 d) { return v3(d.x, fmin_(fmax_(d.y, -1.0f), 1.0f), d.z); }
+
 // shade_miss.wgsl's texel choice on the parameter map (pk_diff.cu diff_env).
 static inline int diff_env_texel(const DiffScene& S, V3 dir) {
+  dir = clamp_y(dir);
   const float u = S.r->env_theta + atan2_(dir.z, dir.x) / DIFF_TAU_F;
   const float v = acos_(dir.y) * INV_PI_F;
   int x = f2i(std::floor(u * (float)S.env_w)), y = f2i(std::floor(v * (float)S.env_h));
@@ -115,6 +121,7 @@ static inline float diff_pdf_texel(const DiffScene& S, int32_t x, int32_t y) {
 // envPdf (shade_hit.wgsl:202-210) on the sampling tables: the texel chosen in
 // binary32, the division by sin(phi) in binary64.
 static inline double diff_env_pdf64(const DiffScene& S, V3 dir) {
+  dir = clamp_y(dir);
   const float a = 1.0f + S.r->env_theta + atan2_(dir.z, dir.x) / DIFF_TAU_F;
   const float u = a - std::trunc(a);
   const float v = acos_(dir.y) * INV_PI_F;
@@ -309,6 +316,178 @@ static inline void diff_path64(const DiffScene& S, uint32_t px, uint32_t py, int
     o = si.origin;
     d = ndir;
   }
+}
+
+// The device's forward pass in binary32, operation for operation (pk_diff.cu
+// shade_diff / diff_path without the derivative factors): every rounding of
+// the weights, throughputs and accumulation as the GPU performs them, so its
+// image equals pk_diff_render's bit for bit.  `trace` (a pixel index, or -1)
+// prints that pixel's events.
+static inline float diff_pdf_dir32(const DiffScene& S, V3 dir) {
+  dir = clamp_y(dir);
+  const float a = 1.0f + S.r->env_theta + atan2_(dir.z, dir.x) / DIFF_TAU_F;
+  const float u = a - std::trunc(a);
+  const float v = acos_(dir.y) * INV_PI_F;
+  const int32_t cx = f2i(u * (float)S.env_w), cy = f2i(v * (float)S.env_h);
+  return diff_pdf_texel(S, cx, cy) / sin_(v * PI_F);
+}
+static inline V3 diff_env32(const DiffScene& S, const std::vector<float>& env32, V3 dir) {
+  const int tex = diff_env_texel(S, dir);
+  return v3(env32[3 * (size_t)tex], env32[3 * (size_t)tex + 1], env32[3 * (size_t)tex + 2]);
+}
+static inline void diff_path32(const DiffScene& S, const std::vector<float>& env32, uint32_t px, uint32_t py,
+                               int32_t samples, float acc[3], std::vector<int32_t>& stack, uint64_t& nrays,
+                               bool trace) {
+  const Renderer& R = *S.r;
+  Hash hc;
+  hc.seed = (px * 1973u + py * 9277u + (uint32_t)samples * 26699u) | 1u;
+  hc.seed = hc.hash();
+  V3 o;
+  V3 d = R.create_primary_ray_dir(hc, (float)px, (float)py, (float)S.W, (float)S.H, &o);
+  float t4[3] = {1.0f, 1.0f, 1.0f};
+  const uint32_t pixel = py * S.W + px;
+  for (int bounce = 0; bounce < S.depth; bounce++) {
+    const Renderer::TravResult t = R.intersect<false>(o, d, stack);
+    nrays++;
+    if (t.index < 0) {
+      const V3 e = diff_env32(S, env32, d);
+      acc[0] = acc[0] + e.x * t4[0];
+      acc[1] = acc[1] + e.y * t4[1];
+      acc[2] = acc[2] + e.z * t4[2];
+      if (trace) std::printf("s%d b%d miss e=(%g %g %g) t4=(%g %g %g)\n", samples, bounce, e.x, e.y, e.z, t4[0], t4[1], t4[2]);
+      return;
+    }
+    DeferredRay ray;
+    ray.o[0] = o.x; ray.o[1] = o.y; ray.o[2] = o.z;
+    ray.d[0] = d.x; ray.d[1] = d.y; ray.d[2] = d.z;
+    ray.tp[0] = t4[0]; ray.tp[1] = t4[1]; ray.tp[2] = t4[2];
+    ray.tp[3] = u2f(pixel);
+    const Hit hit{t.t, t.index, t.bary, ray};
+    Hash h;
+    h.seed = ((uint32_t)bounce * 1973u + pixel * 9277u + (uint32_t)samples * 26699u) | 1u;
+    h.seed = h.hash();
+    Renderer::SI si = R.surface(hit);
+    int mat = R.tri4[4 * (size_t)t.index + 3];
+    const int nm_scene = (int)(R.mat4.size() / 4);
+    if (mat < 0 || mat >= nm_scene) mat = 0;
+    const float rho = (float)S.rough[mat], rho0 = (float)S.rough0[mat], mu = (float)S.metal[mat];
+    si.base = v3((float)S.albedo[3 * (size_t)mat], (float)S.albedo[3 * (size_t)mat + 1], (float)S.albedo[3 * (size_t)mat + 2]);
+    si.metallic = mu;
+    si.alpha = rho * rho;
+    si.spec = v3(mix1(1.0f, si.base.x, mu), mix1(1.0f, si.base.y, mu), mix1(1.0f, si.base.z, mu));
+    const bool next = bounce + 1 < S.depth;
+    if (h.rand() > si.opacity) {
+      if (!next) return;
+      o = add(o, scale(d, t.t + 1e-7f * 40.0f));
+      continue;
+    }
+    float cr = 0.0f, cg = 0.0f, cb = 0.0f;
+    if (dot(si.emission, v3(1.0f, 1.0f, 1.0f)) > 0.0f) {
+      const float att = fmax_(dot(si.normal, matvec(si.b1, si.b2, si.n, si.wo)), 0.0f);
+      cr = 50.0f * si.emission.x * t4[0] * att;
+      cg = 50.0f * si.emission.y * t4[1] * att;
+      cb = 50.0f * si.emission.z * t4[2] * att;
+      acc[0] = acc[0] + cr; acc[1] = acc[1] + cg; acc[2] = acc[2] + cb;
+      return;
+    }
+    Renderer::SI s0 = si;
+    s0.alpha = rho0 * rho0;
+    const V3 m = Renderer::sample_ggx(h, s0);
+    const float f = mix1(Renderer::schlick(fmax_(dot(si.wo, m), 0.0f), 1.5f), 1.0f, si.metallic);
+    const float a = si.alpha;
+    const bool vndf = dot(si.wo, m) * si.wo.z > 0.0f;
+    float ratio = 1.0f;
+    if (vndf && s0.alpha != a)
+      ratio = (Renderer::ggx_g1(si.wo, m, a, a) * Renderer::ggx_d(m, a, a)) /
+              (Renderer::ggx_g1(si.wo, m, s0.alpha, s0.alpha) * Renderer::ggx_d(m, s0.alpha, s0.alpha));
+    Renderer::Sample bs;
+    V3 bsdf;
+    if (h.rand() > f) {
+      bs = Renderer::sample_lambert(h);
+      bsdf = Renderer::eval_lambert(si, bs);
+    } else {
+      bs = Renderer::Sample{reflect(neg(si.wo), m), 0.0f};
+      bs.pdf = Renderer::specular_pdf(si, m);
+      bsdf = Renderer::eval_specular(si, bs);
+    }
+    bool eb = false;
+    V3 ndir = v3(0.0f, 0.0f, 0.0f);
+    float bt[3] = {0.0f, 0.0f, 0.0f};
+    if (bs.wi.z > 0.0f) {
+      ndir = matvec(si.b1, si.b2, si.n, bs.wi);
+      const float pe = diff_pdf_dir32(S, ndir);
+      const float weight = Renderer::power_heuristic(bs.pdf, pe);
+      eb = true;
+      bt[0] = bsdf.x * t4[0] * weight * ratio;
+      bt[1] = bsdf.y * t4[1] * weight * ratio;
+      bt[2] = bsdf.z * t4[2] * weight * ratio;
+      if (trace)
+        std::printf("s%d b%d hit mat %d m=(%g %g %g) wo=(%g %g %g) f=%g wi=(%g %g %g) pdf=%g pe=%g w=%g bsdf=(%g %g %g) bt=(%g %g %g)\n",
+                    samples, bounce, mat, m.x, m.y, m.z, si.wo.x, si.wo.y, si.wo.z, f, bs.wi.x, bs.wi.y, bs.wi.z, bs.pdf,
+                    pe, weight, bsdf.x, bsdf.y, bsdf.z, bt[0], bt[1], bt[2]);
+    }
+    {
+      const EnvTables& tb = *S.tab;
+      const uint32_t nb = (uint32_t)(tb.bins2.size() / 2);
+      const int32_t idx = (int32_t)(h.hash() % nb);
+      const int32_t h0 = tb.bins2[2 * idx], h1 = tb.bins2[2 * idx + 1];
+      const int32_t ci = (int32_t)(h.hash() % (uint32_t)(h1 - h0)) + h0;
+      const int32_t cx = tb.coords2[2 * (size_t)ci], cy = tb.coords2[2 * (size_t)ci + 1];
+      const float u = -R.env_theta + ((0.5f + (float)cx) / (float)S.env_w);
+      const float v = (0.5f + (float)cy) / (float)S.env_h;
+      const float th = u * TAU_F, phi = v * PI_F, sin_phi = sin_(phi);
+      const V3 dir = v3(cos_(th) * sin_phi, cos_(phi), sin_(th) * sin_phi);
+      const Renderer::Sample es{vecmat(dir, si.b1, si.b2, si.n), diff_pdf_texel(S, cx, cy) / sin_phi};
+      if (dot(es.wi, m) > 0.0f && es.wi.z > 0.0f) {
+        const DeferredRay sr = Renderer::material_sample_ray(si, es, f, t4);
+        const float st[3] = {sr.tp[0] * ratio, sr.tp[1] * ratio, sr.tp[2] * ratio};
+        const V3 sdir = v3(sr.d[0], sr.d[1], sr.d[2]);
+        const Renderer::TravResult ts = R.intersect<true>(si.origin, sdir, stack);
+        nrays++;
+        if (ts.index < 0) {
+          const V3 e = diff_env32(S, env32, sdir);
+          cr += e.x * st[0];
+          cg += e.y * st[1];
+          cb += e.z * st[2];
+        }
+        if (trace)
+          std::printf("s%d b%d nee wi=(%g %g %g) pdf=%g st=(%g %g %g) vis=%d\n", samples, bounce, es.wi.x, es.wi.y,
+                      es.wi.z, es.pdf, st[0], st[1], st[2], ts.index < 0 ? 1 : 0);
+      }
+    }
+    acc[0] = acc[0] + cr;
+    acc[1] = acc[1] + cg;
+    acc[2] = acc[2] + cb;
+    if (!(eb && next)) return;
+    o = si.origin;
+    d = ndir;
+    t4[0] = bt[0]; t4[1] = bt[1]; t4[2] = bt[2];
+  }
+}
+// Rows [y0, y1) of the binary32 image (W x (y1-y0) x 4, alpha 0).
+static inline uint64_t diff_render32(const DiffScene& S, uint32_t y0, uint32_t y1, float* image4, int nthreads,
+                                     int64_t trace_pixel) {
+  std::vector<float> env32(3 * (size_t)S.env_w * S.env_h);
+  for (size_t i = 0; i < env32.size(); i++) env32[i] = (float)S.env[i];
+  std::vector<uint64_t> rays(std::max(nthreads, 1), 0);
+  parallel_for((size_t)S.W * (y1 - y0), nthreads, [&](size_t b, size_t e, int tid) {
+    std::vector<int32_t> stack;
+    for (size_t k = b; k < e; k++) {
+      const uint32_t px = (uint32_t)(k % S.W), py = y0 + (uint32_t)(k / S.W);
+      float acc[3] = {0.0f, 0.0f, 0.0f};
+      const bool tr = (int64_t)(py * S.W + px) == trace_pixel;
+      for (int s = 0; s < S.spp; s++)
+        diff_path32(S, env32, px, py, (int32_t)(S.sample_base + (uint32_t)s), acc, stack, rays[tid], tr);
+      const float inv = 1.0f / (float)S.spp;
+      image4[4 * k] = acc[0] * inv;
+      image4[4 * k + 1] = acc[1] * inv;
+      image4[4 * k + 2] = acc[2] * inv;
+      image4[4 * k + 3] = 0.0f;
+    }
+  });
+  uint64_t n = 0;
+  for (uint64_t r : rays) n += r;
+  return n;
 }
 
 // image3 (W x H x 3): the mean over spp of each path's contributions.

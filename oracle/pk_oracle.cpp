@@ -375,6 +375,14 @@ uint64_t or_diff_render(void* p, uint32_t W, uint32_t H, const double* albedo, c
       diff_scene(p, W, H, albedo, rough, rough0, metal, n_mats, env, env_w, env_h, tables, spp, depth, sample_base);
   return diff_render(S, image3, ((Renderer*)p)->nthreads);
 }
+uint64_t or_diff_render32(void* p, uint32_t W, uint32_t H, const double* albedo, const double* rough,
+                          const double* rough0, const double* metal, uint32_t n_mats, const double* env,
+                          uint32_t env_w, uint32_t env_h, void* tables, uint32_t spp, uint32_t depth,
+                          uint32_t sample_base, uint32_t y0, uint32_t y1, float* image4, int64_t trace_pixel) {
+  const DiffScene S =
+      diff_scene(p, W, H, albedo, rough, rough0, metal, n_mats, env, env_w, env_h, tables, spp, depth, sample_base);
+  return diff_render32(S, y0, y1, image4, ((Renderer*)p)->nthreads, trace_pixel);
+}
 void or_diff_grad(void* p, uint32_t W, uint32_t H, const double* albedo, const double* rough, const double* rough0,
                   const double* metal, uint32_t n_mats, const double* env, uint32_t env_w, uint32_t env_h,
                   void* tables, uint32_t spp, uint32_t depth, uint32_t sample_base, const double* dimage3,

@@ -332,6 +332,19 @@ class Renderer:
                                                  rough0), _p(img))
         return img, int(rays)
 
+    def diff_render32(self, W, H, albedo, rough, metal, env, tables, spp, depth, sample_base=0, rough0=None,
+                      rows=None, trace_pixel: int = -1):
+        """pk_diff_render's binary32 arithmetic replayed on the CPU: rows
+        (y0, y1) of the (H, W, 4) float32 image, and the rays traced."""
+        y0, y1 = rows if rows is not None else (0, H)
+        img = np.zeros((y1 - y0, W, 4), np.float32)
+        L = lib()
+        L.or_diff_render32.restype = C.c_uint64
+        rays = L.or_diff_render32(*self._diff_args(W, H, albedo, rough, metal, env, tables, spp, depth, sample_base,
+                                                   rough0), C.c_uint32(y0), C.c_uint32(y1), _p(img),
+                                  C.c_int64(trace_pixel))
+        return img, int(rays)
+
     def diff_grad(self, W, H, albedo, rough, metal, env, tables, spp, depth, dimage, sample_base=0, rough0=None):
         """FP64 oracle of pk_diff_backward for dLoss/dimage = dimage (H, W, 3)."""
         d = np.ascontiguousarray(dimage, np.float64)

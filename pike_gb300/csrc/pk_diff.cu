@@ -74,8 +74,15 @@ struct DiffParams {
   uint32_t sample_base;
 };
 
+// A unit direction's y component can round to just above 1 in magnitude,
+// where acos (and with it envPdf in the drop-in) is NaN and the NaN poisons
+// the pixel; the differentiable renderer clamps y to [-1, 1] in its
+// environment lookups (the texel chosen is the one the drop-in reads).
+__device__ __forceinline__ V3 clamp_y(V3 d) { return v3(d.x, fmin_(fmax_(d.y, -1.0f), 1.0f), d.z); }
+
 // shade_miss.wgsl's texel choice (env_color) on the FP32 map; tex = its index.
 __device__ __forceinline__ V3 diff_env(const DiffParams& P, float theta, V3 dir, int& tex) {
+  dir = clamp_y(dir);
   const float u = theta + atan2_(dir.z, dir.x) / c::TAU;
   const float v = acos_(dir.y) * c::INV_PI;
   int x = f2i(floorf(u * (float)P.env_w)), y = f2i(floorf(v * (float)P.env_h));
@@ -197,7 +204,7 @@ __device__ __forceinline__ void shade_diff(const SceneDev& sc, const EnvDev& env
   }
   if (bs.wi.z > 0.0f) {
     const V3 dir = matvec(si.b1, si.b2, si.n, bs.wi);
-    const float pe = env.enabled ? env_pdf_dir(env, theta, dir) : 0.0f;
+    const float pe = env.enabled ? env_pdf_dir(env, theta, clamp_y(dir)) : 0.0f;
     const float weight = env.enabled ? power_heuristic(bs.pdf, pe) : 1.0f;
     out.eb = true;
     out.bo = make_float4(si.origin.x, si.origin.y, si.origin.z, 0.0f);

@@ -1,13 +1,12 @@
 // pk_wide.cpp -- collapse of the binary BVH into compressed 8-wide nodes
 // (host side; the record layout is described in pk_wide.h).
 //
-// Collapse: a wide node starts from its binary node's two children and
-// repeatedly opens the child of largest surface area until it holds eight
-// children or only leaves (the greedy collapse of Wald et al., "Getting Rid of
-// Packets", 2008, with the child budget of Ylitie et al., HPG 2017).  A leaf
-// child holds at most three triangles; a binary leaf with more is split into
-// halves of its triangle range as if it were an inner node.  Children are
-// assigned to slots greedily by the octant cost of Ylitie et al. (the
+// Collapse: the SAH-optimal collapse of Ylitie et al. (HPG 2017, section
+// 3.1; see Collapse below) picks, for every binary node, whether it becomes a
+// leaf child, a wide node, or shares its slots between its two children.  A
+// leaf child holds at most three triangles; a binary leaf with more is split
+// into halves of its triangle range as if it were an inner node.  Children
+// are assigned to slots greedily by the octant cost of Ylitie et al. (the
 // child whose centroid lies furthest against a direction octant takes that
 // octant's slot).  Nodes are built one breadth-first level at a time, each
 // level in parallel; a prefix sum over the level gives every node's internal
