@@ -141,6 +141,12 @@ int pk_bvh_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* n_leaf_tris, double no
  * wide BVH's order; PK_ERR_STATE before PK_TRACE_WIDE was set. */
 int pk_wide_info(pk_ctx* ctx, uint32_t* n_nodes, uint32_t* depth);
 int pk_wide_download(pk_ctx* ctx, float* nodes20, float* tris12);
+/* Records of the FP32 binary reference (PK_TRACE_EXACT; no reference
+ * counterpart): records16 = 16 floats per inner node of the binary BVH (both
+ * children's outward-rounded boxes {hi, lo} per axis, then the two child
+ * codes), tris12 = 12 floats per triangle in the binary leaf order, root_code
+ * = the root's code; PK_ERR_STATE before PK_TRACE_EXACT was set. */
+int pk_exact_download(pk_ctx* ctx, float* records16, float* tris12, int32_t* root_code);
 int pk_bvh_download(pk_ctx* ctx, int32_t* nodes5, int32_t* tri4_leaf, float* verts4);
 
 /* ---- environment (row E) --------------------------------------------------

@@ -1,5 +1,10 @@
-// pk_wide.cpp -- collapse of the binary BVH into compressed 8-wide nodes
-// (host side; the record layout is described in pk_wide.h).
+// om_wide.h -- host restatement of form (1)'s builders (the compressed 8-wide
+// BVH by the SAH-optimal collapse, and the FP32 binary reference's records);
+// the record layouts are those of pike_gb300/csrc/pk_wide.h.
+//
+// TEST INFRASTRUCTURE ONLY (see om_math.h): the library builds these
+// structures on the GPU (pike_gb300/csrc/pk_wide.cu), and the tests require
+// its records to equal this restatement's bit for bit.
 //
 // Collapse: the SAH-optimal collapse of Ylitie et al. (HPG 2017, section
 // 3.1; see Collapse below) picks, for every binary node, whether it becomes a
@@ -11,7 +16,25 @@
 // octant's slot).  Nodes are built one breadth-first level at a time, each
 // level in parallel; a prefix sum over the level gives every node's internal
 // children consecutive indices after all earlier nodes.
-#include "pk_wide.h"
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace om_wide {
+
+constexpr int WIDE_NODE_FLOATS = 20;
+constexpr int WIDE_TRI_FLOATS = 12;
+
+struct WideHost {
+  std::vector<float> nodes;  // WIDE_NODE_FLOATS per node
+  std::vector<float> tris;   // WIDE_TRI_FLOATS per triangle, in the wide BVH's order
+  uint32_t n_nodes = 0;
+  uint32_t max_depth = 0;
+};
+
+}  // namespace om_wide
+
 
 #include <algorithm>
 #include <atomic>
@@ -19,9 +42,9 @@
 #include <cstring>
 #include <thread>
 
-namespace pk {
+namespace om_wide {
 
-namespace {
+namespace detail {
 
 struct DBox {
   double lo[3] = {INFINITY, INFINITY, INFINITY};
@@ -384,9 +407,10 @@ struct Builder {
   }
 };
 
-}  // namespace
+}  // namespace detail
+using namespace detail;
 
-int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+inline int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
                    const float* verts4, uint32_t n_verts, WideHost& out, std::string& why) {
   out = WideHost();
   if (n_nodes == 0) {
@@ -460,7 +484,12 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4,
           if (!(lo <= hi)) { lo = 0.0; hi = 0.0; }
           org[a] = f_down(lo);
           const double ext = hi - (double)org[a];
-          int e2 = ext > 0.0 ? (int)std::ceil(std::log2(ext / 255.0)) : -100;
+          int e2 = -100;  // ceil(log2(ext / 255)), exactly: ext / 255 = m 2^k with m in [0.5, 1)
+          if (ext > 0.0) {
+            int k;
+            const double m = std::frexp(ext / 255.0, &k);
+            e2 = m == 0.5 ? k - 1 : k;
+          }
           e2 = std::max(-100, std::min(e2, 127));
           while (e2 < 127 && (double)decode(org[a], std::ldexp(1.0f, e2), 255) < hi) e2++;
           ex[a] = e2;
@@ -534,7 +563,7 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4,
   return 0;
 }
 
-int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+inline int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
                        const float* verts4, uint32_t n_verts, std::vector<float>& records,
                        std::vector<float>& tris, int32_t& root_code, std::string& why) {
   if (n_nodes == 0) {
@@ -580,4 +609,4 @@ int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* t
   return 0;
 }
 
-}  // namespace pk
+}  // namespace om_wide

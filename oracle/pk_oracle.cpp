@@ -17,6 +17,7 @@
 #include "om_render.h"
 #include "om_render_f64.h"
 #include "om_diff.h"
+#include "om_wide.h"
 
 using namespace om;
 
@@ -390,6 +391,40 @@ void or_diff_grad(void* p, uint32_t W, uint32_t H, const double* albedo, const d
   const DiffScene S =
       diff_scene(p, W, H, albedo, rough, rough0, metal, n_mats, env, env_w, env_h, tables, spp, depth, sample_base);
   diff_gradient(S, dimage3, g_albedo, g_rough, g_env, ((Renderer*)p)->nthreads);
+}
+
+// Form (1)'s builders restated on the host (om_wide.h).
+void* or_wide_build(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                    const float* verts4, uint32_t n_verts) {
+  om_wide::WideHost* w = new om_wide::WideHost();
+  std::string why;
+  if (om_wide::build_wide_bvh(nodes5, n_nodes, tri4, n_tris, verts4, n_verts, *w, why)) {
+    g_err = why;
+    delete w;
+    return nullptr;
+  }
+  return w;
+}
+uint32_t or_wide_nodes(void* h) { return ((om_wide::WideHost*)h)->n_nodes; }
+uint32_t or_wide_depth(void* h) { return ((om_wide::WideHost*)h)->max_depth; }
+void or_wide_copy(void* h, float* nodes20, float* tris12) {
+  const om_wide::WideHost* w = (const om_wide::WideHost*)h;
+  std::memcpy(nodes20, w->nodes.data(), w->nodes.size() * 4);
+  std::memcpy(tris12, w->tris.data(), w->tris.size() * 4);
+}
+void or_wide_free(void* h) { delete (om_wide::WideHost*)h; }
+// records16: 16 floats per inner node (the caller sizes it), tris12: 12 per triangle.
+int or_exact_build(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
+                   const float* verts4, uint32_t n_verts, float* records16, float* tris12, int32_t* root) {
+  std::vector<float> rec, tris;
+  std::string why;
+  if (om_wide::build_exact_binary(nodes5, n_nodes, tri4, n_tris, verts4, n_verts, rec, tris, *root, why)) {
+    g_err = why;
+    return 1;
+  }
+  std::memcpy(records16, rec.data(), rec.size() * 4);
+  std::memcpy(tris12, tris.data(), tris.size() * 4);
+  return 0;
 }
 
 // Elementwise math probes for parity of the built-in definitions:

@@ -23,7 +23,7 @@ _lib = None
 
 def build(force: bool = False) -> str:
     srcs = [os.path.join(_HERE, f) for f in ("pk_oracle.cpp", "om_math.h", "om_build.h", "om_render.h", "om_render64.h",
-                                             "om_render_f64.h", "om_diff.h", "Makefile")]
+                                             "om_render_f64.h", "om_diff.h", "om_wide.h", "Makefile")]
     if force or not os.path.exists(_LIB) or max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(_LIB):
         subprocess.run(["make", "-s", "-C", _HERE, "-B", "liboracle.so"], check=True)
     return _LIB
@@ -35,7 +35,7 @@ def lib():
         build()
         _lib = C.CDLL(_LIB)
         _lib.or_last_error.restype = C.c_char_p
-        for name in ("or_bvh_build", "or_env_build", "or_env_build_f32", "or_renderer_new"):
+        for name in ("or_bvh_build", "or_env_build", "or_env_build_f32", "or_renderer_new", "or_wide_build"):
             getattr(_lib, name).restype = C.c_void_p
         _lib.or_env_num_bins.restype = C.c_size_t
         _lib.or_shadow_offset.restype = C.c_size_t
@@ -163,6 +163,46 @@ class Env:
         L.or_env_copy(C.c_void_p(hd), _p(self.bins), _p(self.coords), _p(self.pdf), _p(tb))
         L.or_env_free(C.c_void_p(hd))
         self.total, self.brightest = float(tb[0]), float(tb[1])
+
+
+def wide_build(nodes5: np.ndarray, tri4: np.ndarray, verts4: np.ndarray):
+    """Form (1)'s compressed 8-wide BVH restated on the host (om_wide.h):
+    nodes (n, 20) float32, tris (n_tris, 12) float32, depth."""
+    L = lib()
+    nodes5 = np.ascontiguousarray(nodes5, np.int32)
+    tri4 = np.ascontiguousarray(tri4, np.int32)
+    verts4 = np.ascontiguousarray(verts4, np.float32)
+    h = L.or_wide_build(_p(nodes5), C.c_uint32(nodes5.size // 5), _p(tri4), C.c_uint32(tri4.size // 4), _p(verts4),
+                        C.c_uint32(verts4.size // 4))
+    if not h:
+        _err("or_wide_build")
+    h = C.c_void_p(h)
+    L.or_wide_nodes.restype = C.c_uint32
+    L.or_wide_depth.restype = C.c_uint32
+    n = int(L.or_wide_nodes(h))
+    nodes = np.zeros((n, 20), np.float32)
+    tris = np.zeros((tri4.size // 4, 12), np.float32)
+    L.or_wide_copy(h, _p(nodes), _p(tris))
+    depth = int(L.or_wide_depth(h))
+    L.or_wide_free(h)
+    return nodes, tris, depth
+
+
+def exact_build(nodes5: np.ndarray, tri4: np.ndarray, verts4: np.ndarray):
+    """The FP32 binary reference's records restated on the host: records
+    (n_inner, 16) float32, tris (n_tris, 12) float32, root code."""
+    L = lib()
+    nodes5 = np.ascontiguousarray(nodes5, np.int32)
+    tri4 = np.ascontiguousarray(tri4, np.int32)
+    verts4 = np.ascontiguousarray(verts4, np.float32)
+    n_inner = max(int((nodes5.reshape(-1, 5)[:, 1] <= -1).sum()), 1)
+    rec = np.zeros((n_inner, 16), np.float32)
+    tris = np.zeros((max(tri4.size // 4, 1), 12), np.float32)
+    root = C.c_int32(0)
+    if L.or_exact_build(_p(nodes5), C.c_uint32(nodes5.size // 5), _p(tri4), C.c_uint32(tri4.size // 4), _p(verts4),
+                        C.c_uint32(verts4.size // 4), _p(rec), _p(tris), C.byref(root)):
+        _err("or_exact_build")
+    return rec, tris, int(root.value)
 
 
 class EnvF32:

@@ -82,7 +82,7 @@ def load(path: str = LIB_PATH):
         "pk_scene_upload": [_P, _P, u32, _P, _P, u32], "pk_scene_download": [_P, _P, _P],
         "pk_materials_set": [_P, _P, u32], "pk_materials_upload": [_P, _P, u32, _P, u32],
         "pk_materials_download": [_P, _P, _P, _P, _P], "pk_atlas_upload": [_P, _P, u32, u32],
-        "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P, _P],
+        "pk_wide_info": [_P, _P, _P], "pk_wide_download": [_P, _P, _P], "pk_exact_download": [_P, _P, _P, _P],
         "pk_diff_render": [_P, _P, _P], "pk_diff_backward": [_P, _P, _P, _P, _P, _P],
         "pk_diff_rays": [_P, _P], "pk_diff_set_env_sampling": [_P, _P, u32, u32],
         "pk_diff_env_info": [_P, _P, _P, _P], "pk_diff_env_download": [_P, _P, _P, _P],

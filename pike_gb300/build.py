@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libpike.so")
 BUILD_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["pk_api.cu", "pk_render.cu", "pk_scene.cu", "pk_util.cu", "pk_bvh.cu", "pk_cast.cu", "pk_env.cu", "pk_diff.cu", "pk_batch.cu", "pk_probe.cu", "pk_host_tables.cpp", "pk_wide.cpp"]
+SOURCES = ["pk_api.cu", "pk_render.cu", "pk_scene.cu", "pk_util.cu", "pk_bvh.cu", "pk_cast.cu", "pk_env.cu", "pk_diff.cu", "pk_batch.cu", "pk_probe.cu", "pk_wide.cu", "pk_host_tables.cpp"]
 HEADERS = ["pk_internal.cuh", "pk_math.cuh", "pk_render.h", "pk_util.h", "pk_bvh.h", "pk_host_tables.h", "pk_ctx.h",
            "pk_traverse.cuh", "pk_traverse_wide.cuh", "pk_wide.h", "pk_shade.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -379,57 +379,28 @@ int pk_materials_download(pk_ctx* c, uint32_t* n_mats, uint32_t* n_layers, int32
 }
 
 // ---------------- BVH ----------------
-// Host copies of the binary nodes, leaf-ordered triangle indices and
-// normalised vertices (the inputs of form (1)'s structures).
-static void download_bvh_inputs(pk_ctx* c, std::vector<int32_t>& nodes, std::vector<int32_t>& tri4,
-                                std::vector<float>& verts) {
-  nodes.resize(5 * (size_t)c->n_nodes);
-  tri4.resize(4 * (size_t)c->n_leaf_tris);
-  verts.resize(4 * (size_t)c->bvh_verts);
-  check(cudaMemcpyAsync(nodes.data(), c->nodes5.p, nodes.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  if (c->n_leaf_tris)
-    check(cudaMemcpyAsync(tri4.data(), c->tri4_leaf.p, tri4.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  if (c->bvh_verts)
-    check(cudaMemcpyAsync(verts.data(), c->verts4.p, verts.size() * 4, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  check(cudaStreamSynchronize(c->stream), "sync");
-}
-
-// The compressed 8-wide BVH and its triangle records.
+// The compressed 8-wide BVH and its triangle records, built on the GPU.
 static int build_wide(pk_ctx* c) {
-  std::vector<int32_t> nodes, tri4;
-  std::vector<float> verts;
-  download_bvh_inputs(c, nodes, tri4, verts);
-  WideHost w;
   std::string why;
-  if (build_wide_bvh(nodes.data(), c->n_nodes, tri4.data(), c->n_leaf_tris, verts.data(), c->bvh_verts, w, why))
+  uint32_t n = 0, depth = 0;
+  if (build_wide_bvh_gpu(c->stream, c->nodes5.p, c->n_nodes, c->tri4_leaf.p, c->n_leaf_tris, c->verts4.p,
+                         c->bvh_verts, c->wide, c->wide_tris, n, depth, why))
     return fail(c, PK_ERR_ARG, "wide BVH: " + why);
-  upload(c->wide, reinterpret_cast<const float4*>(w.nodes.data()), 5 * (size_t)w.n_nodes, c->stream);
-  upload(c->wide_tris, reinterpret_cast<const float4*>(w.tris.data()), std::max<size_t>(w.tris.size() / 4, 1),
-         c->stream);
-  check(cudaStreamSynchronize(c->stream), "sync");
-  c->wide_nodes = w.n_nodes;
-  c->wide_depth = w.max_depth;
+  c->wide_nodes = n;
+  c->wide_depth = depth;
   c->wide_ready = true;
   c->invalidate_graph();
   return PK_OK;
 }
 
 // Binary records with outward-rounded FP32 boxes and the binary leaf order's
-// triangle records for PK_TRACE_EXACT.
+// triangle records for PK_TRACE_EXACT, built on the GPU.
 static int build_exact(pk_ctx* c) {
-  std::vector<int32_t> nodes, tri4;
-  std::vector<float> verts;
-  download_bvh_inputs(c, nodes, tri4, verts);
-  std::vector<float> rec, tris;
   int32_t root = 0;
   std::string why;
-  if (build_exact_binary(nodes.data(), c->n_nodes, tri4.data(), c->n_leaf_tris, verts.data(), c->bvh_verts, rec,
-                         tris, root, why))
+  if (build_exact_binary_gpu(c->stream, c->nodes5.p, c->n_nodes, c->tri4_leaf.p, c->n_leaf_tris, c->verts4.p,
+                             c->bvh_verts, c->exact, c->exact_tris, root, why))
     return fail(c, PK_ERR_ARG, "exact binary records: " + why);
-  upload(c->exact, reinterpret_cast<const float4*>(rec.data()), rec.size() / 4, c->stream);
-  upload(c->exact_tris, reinterpret_cast<const float4*>(tris.data()), std::max<size_t>(tris.size() / 4, 1),
-         c->stream);
-  check(cudaStreamSynchronize(c->stream), "sync");
   c->exact_root = root;
   c->exact_ready = true;
   c->invalidate_graph();
@@ -487,6 +458,18 @@ int pk_wide_download(pk_ctx* c, float* nodes20, float* tris12) {
     check(cudaMemcpy(nodes20, c->wide.p, 80 * (size_t)c->wide_nodes, cudaMemcpyDeviceToHost), "D2H");
     if (tris12 && c->n_leaf_tris)
       check(cudaMemcpy(tris12, c->wide_tris.p, 48 * (size_t)c->n_leaf_tris, cudaMemcpyDeviceToHost), "D2H");
+    return PK_OK;
+  });
+}
+
+int pk_exact_download(pk_ctx* c, float* records16, float* tris12, int32_t* root_code) {
+  return guarded(c, [&]() {
+    if (!c->exact_ready) return fail(c, PK_ERR_STATE, "no FP32 binary records: set PK_TRACE_EXACT after building a BVH");
+    if (!records16 || !root_code) return fail(c, PK_ERR_ARG, "null output");
+    check(cudaMemcpy(records16, c->exact.p, c->exact.bytes(), cudaMemcpyDeviceToHost), "D2H");
+    if (tris12 && c->n_leaf_tris)
+      check(cudaMemcpy(tris12, c->exact_tris.p, 48 * (size_t)c->n_leaf_tris, cudaMemcpyDeviceToHost), "D2H");
+    *root_code = c->exact_root;
     return PK_OK;
   });
 }

@@ -27,27 +27,28 @@
 // {v2.z, slot bits, 0, 0}, where `slot` is the triangle's index in the binary
 // BVH's leaf order (the index every hit record reports and ties break on).
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
-#include <vector>
+
+#include "pk_util.h"
 
 namespace pk {
 
 constexpr int WIDE_NODE_FLOATS = 20;
 constexpr int WIDE_TRI_FLOATS = 12;
 
-struct WideHost {
-  std::vector<float> nodes;  // WIDE_NODE_FLOATS per node
-  std::vector<float> tris;   // WIDE_TRI_FLOATS per triangle, in the wide BVH's order
-  uint32_t n_nodes = 0;
-  uint32_t max_depth = 0;
-};
-
-// nodes5: binary BFS nodes (5 words each); tri4: leaf-ordered {i0, i1, i2,
-// matId}; verts4: normalised vertex positions (4 floats each).  Returns 0 on
-// success, non-zero with a reason otherwise.
-int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
-                   const float* verts4, uint32_t n_verts, WideHost& out, std::string& why);
+// Built on the GPU (pk_wide.cu) from the breadth-first binary nodes (5 words
+// each), the leaf-ordered {i0, i1, i2, matId} and the normalised vertices on
+// the device.  Return 0 on success, non-zero with a reason otherwise.
+//
+// The compressed 8-wide BVH: nodes_out (5 float4 per node), tris_out (3
+// float4 per triangle, in the wide BVH's own leaf order), the node count and
+// the depth in wide levels.
+int build_wide_bvh_gpu(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4* tri4, uint32_t n_tris,
+                       const float4* verts4, uint32_t n_verts, DevBuf<float4>& nodes_out, DevBuf<float4>& tris_out,
+                       uint32_t& n_wide, uint32_t& depth, std::string& why);
 
 // The binary BVH's inner records (64-byte layout of the drop-in traversal:
 // both children's boxes, then their child codes) with FP32 boxes rounded
@@ -55,8 +56,8 @@ int build_wide_bvh(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4,
 // the reference's inward-truncated snorm16 boxes, and the binary leaf order's
 // triangle records in the format above.  Traversed with (t, slot) ties and
 // slack in the box tests, closest hits equal brute force.
-int build_exact_binary(const int32_t* nodes5, uint32_t n_nodes, const int32_t* tri4, uint32_t n_tris,
-                       const float* verts4, uint32_t n_verts, std::vector<float>& records,
-                       std::vector<float>& tris, int32_t& root_code, std::string& why);
+int build_exact_binary_gpu(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4* tri4,
+                           uint32_t n_tris, const float4* verts4, uint32_t n_verts, DevBuf<float4>& records,
+                           DevBuf<float4>& tris, int32_t& root_code, std::string& why);
 
 }  // namespace pk

@@ -33,6 +33,41 @@ def wide_nodes(ctx, n_tris):
     return nodes, tris, int(depth[0])
 
 
+@pytest.mark.parametrize("make", [
+    lambda: synth.displaced_sphere_scene(subdivisions=6, width=16, height=16, env_size=(64, 32)),
+    lambda: synth.triangle_soup_scene(n_tris=60_000, width=16, height=16, env_size=(64, 32)),
+    lambda: synth.small_scene(width=16, height=16),
+], ids=["sphere6", "soup60k", "small"])
+def test_gpu_builds_equal_host_restatement(oracle, pk_built, make):
+    """The GPU builders of the 8-wide BVH and of the FP32 binary reference
+    (pk_wide.cu) give the host restatement's records (oracle/om_wide.h) bit
+    for bit: nodes, triangle records, depth, root code."""
+    src = make()
+    pair = Pair(src, oracle)
+    ctx = pair.ctx
+    n_nodes, n_tris = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
+    ctx.call("pk_bvh_info", ptr(n_nodes), ptr(n_tris), ptr(np.zeros(4)))
+    nodes5 = np.zeros((int(n_nodes[0]), 5), np.int32)
+    tri4 = np.zeros((int(n_tris[0]), 4), np.int32)
+    verts = np.zeros_like(pair.P.bvh.verts)
+    ctx.call("pk_bvh_download", ptr(nodes5), ptr(tri4), ptr(verts))
+    ctx.call("pk_set_trace_mode", WIDE)
+    nodes, tris, depth = wide_nodes(ctx, int(n_tris[0]))
+    hn, ht, hd = oracle.wide_build(nodes5, tri4, verts)
+    assert (nodes.shape, depth) == (hn.shape, hd)
+    assert np.array_equal(nodes.view(np.uint32), hn.view(np.uint32))
+    assert np.array_equal(tris.view(np.uint32), ht.view(np.uint32))
+    ctx.call("pk_set_trace_mode", EXACT)
+    rec, et, root = oracle.exact_build(nodes5, tri4, verts)
+    grec = np.zeros_like(rec)
+    gtris = np.zeros_like(et)
+    groot = np.zeros(1, np.int32)
+    ctx.call("pk_exact_download", ptr(grec), ptr(gtris), ptr(groot))
+    assert int(groot[0]) == root
+    assert np.array_equal(grec.view(np.uint32), rec.view(np.uint32))
+    assert np.array_equal(gtris.view(np.uint32), et.view(np.uint32))
+
+
 def test_trace_mode_rules(pk_built, oracle):
     src = synth.small_scene(width=8, height=8)
     pair = Pair(src, oracle)
