@@ -617,9 +617,9 @@ def adjoint_form(args, local: int):
     torch.cuda.synchronize()
     opt_s = time.perf_counter() - t0
 
-    def eval_loss(A, R, E):
+    def eval_loss(A, R, E):  # L2 error of the expected image, estimated from 8 renders
         scene.set_env_sampling(E)
-        return float(l2_loss(scene.render(A, R, E, seed=99999), target_hq))
+        return float(l2_loss(sum(scene.render(A, R, E, seed=90000 + k) for k in range(8)) / 8, target_hq))
 
     # recovery error: parameters the image constrains (materials on hit
     # surfaces, env texels the camera or a bounce sees: non-zero gradient at
@@ -638,7 +638,8 @@ def adjoint_form(args, local: int):
                                    "selection": "random among parameters with |grad| >= 1% of the largest of its kind"},
             "inverse_rendering": {
                 "steps": steps, "seconds": opt_s,
-                "objective": "L2 to a 128-spp target, fresh 16-spp samples every step (Adam, lr 0.02)",
+                "objective": "L2 to a 128-spp target; fresh 16-spp samples every step, the gradient from an independent "
+                             "16-spp replay (Adam, lr 0.02); loss_eval = L2 of a 128-spp render",
                 "loss_first": hist[0], "loss_last": hist[-1],
                 "loss_eval_start": eval_loss(a0, r0, e0), "loss_eval_end": eval_loss(a, r, e),
                 "loss_eval_at_hidden_params": eval_loss(albedo, rough, env),

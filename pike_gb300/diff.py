@@ -135,8 +135,8 @@ def _function():
 
     class PikeRender(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, albedo, rough, env, scene, seed):
-            ctx.scene, ctx.seed = scene, seed
+        def forward(ctx, albedo, rough, env, scene, seed, grad_seed):
+            ctx.scene, ctx.seed = scene, seed if grad_seed is None else grad_seed
             ctx.save_for_backward(albedo, rough, env)
             scene.set_env_sampling(env)  # detached: the tables follow the current map
             return scene.render(albedo.detach().contiguous(), rough.detach().contiguous(), env.detach().contiguous(),
@@ -147,7 +147,7 @@ def _function():
             albedo, rough, env = ctx.saved_tensors
             ga, gr, ge = ctx.scene.backward(albedo.detach().contiguous(), rough.detach().contiguous(),
                                             env.detach().contiguous(), grad_image, ctx.seed)
-            return ga.to(albedo.dtype), gr.to(rough.dtype), ge.to(env.dtype), None, None
+            return ga.to(albedo.dtype), gr.to(rough.dtype), ge.to(env.dtype), None, None, None
 
     return PikeRender
 
@@ -155,12 +155,17 @@ def _function():
 _FN = None
 
 
-def render(scene: DiffScene, albedo, rough, env, seed: int = 0):
-    """Differentiable image (H, W, 4) of the scene for these parameters."""
+def render(scene: DiffScene, albedo, rough, env, seed: int = 0, grad_seed: int | None = None):
+    """Differentiable image (H, W, 4) of the scene for these parameters.  The
+    backward pass replays the paths of `grad_seed` (default: `seed`).  With an
+    independent grad_seed the gradient of a loss that is nonlinear in the
+    image, such as L2, is unbiased for the loss of the expected image: with the
+    same samples in both passes it also carries the gradient of the image's
+    Monte Carlo variance."""
     global _FN
     if _FN is None:
         _FN = _function()
-    return _FN.apply(albedo, rough, env, scene, seed)
+    return _FN.apply(albedo, rough, env, scene, seed, grad_seed)
 
 
 def l2_loss(image, target):
@@ -170,9 +175,12 @@ def l2_loss(image, target):
 def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 200, lr: float = 0.02,
                    n_free: int | None = None, seed_per_step: bool = True, seed: int = 0, env_floor: float = 1e-3):
     """Adam on (albedo, roughness, env) towards the target image; materials at
-    index >= n_free stay fixed.  Step k renders with seed + k (fresh samples)
-    or, with seed_per_step=False, always with `seed` (common random numbers).
-    Returns the parameters and the loss history."""
+    index >= n_free stay fixed.  With seed_per_step, step k renders with seed
+    2k and differentiates with the independent samples of seed 2k + 1
+    (decorrelated: unbiased gradients of the expected image's L2 error);
+    otherwise every step renders and differentiates `seed` (common random
+    numbers: a deterministic objective).  Returns the parameters and the loss
+    history."""
     import torch
     a = albedo.clone().requires_grad_(True)
     r = rough.clone().requires_grad_(True)
@@ -184,7 +192,11 @@ def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 20
     hist = []
     for k in range(steps):
         opt.zero_grad()
-        loss = l2_loss(render(scene, a, r, e, seed=seed + k if seed_per_step else seed), target)
+        if seed_per_step:
+            img = render(scene, a, r, e, seed=seed + 2 * k, grad_seed=seed + 2 * k + 1)
+        else:
+            img = render(scene, a, r, e, seed=seed)
+        loss = l2_loss(img, target)
         loss.backward()
         opt.step()
         with torch.no_grad():

@@ -172,10 +172,10 @@ def test_forward_matches_dropin_in_distribution(small):
 
 
 def test_inverse_rendering_reduces_loss(small):
-    """Adam through torch.autograd with fresh samples every step (the sampling
-    tables and roughness following the current parameters) towards a target
-    rendered with 16x the samples; the loss at a fixed evaluation seed must
-    fall by more than half."""
+    """Adam through torch.autograd with fresh, decorrelated samples every step
+    (the sampling tables and roughness following the current parameters)
+    towards a target rendered with 16x the samples; the L2 error of the
+    expected image (estimated from 16 renders) must fall by more than half."""
     from pike_gb300.diff import inverse_render, l2_loss
     src, scene, P, _, _, _, _ = small
     albedo, rough, env = scene.source_params(env_size=(64, 32), sun=5.0)
@@ -185,14 +185,14 @@ def test_inverse_rendering_reduces_loss(small):
     r0 = torch.full_like(rough, 0.5)
     e0 = torch.full_like(env, float(env.mean()))
 
-    def eval_loss(a, r, e):
+    def bias_loss(a, r, e):
         scene.set_env_sampling(e)
-        return float(l2_loss(scene.render(a, r, e, seed=999), target))
+        return float(l2_loss(sum(scene.render(a, r, e, seed=5000 + k) for k in range(16)) / 16, target))
 
-    first = eval_loss(a0, r0, e0)
+    first = bias_loss(a0, r0, e0)
     a, r, e, hist = inverse_render(scene, target, a0, r0, e0, steps=60, lr=0.05,
                                    n_free=src.materials.shape[0] - 1, seed_per_step=True)
     assert all(np.isfinite(hist))
-    last = eval_loss(a, r, e)
+    last = bias_loss(a, r, e)
     assert last < 0.5 * first, (first, last, hist[-5:])
     assert float(a[-1].sub(0.5).abs().max()) == 0.0  # the fixed box material did not move
