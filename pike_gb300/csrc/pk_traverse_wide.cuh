@@ -92,6 +92,18 @@ __device__ __forceinline__ bool wt_test(const float4* __restrict__ tris, uint32_
   return true;
 }
 
+// Byte k of `word` as a float: the word {byte, 0, 0, 0x4B} is the float
+// 2^23 + byte exactly, so one byte permute and one exact subtraction replace
+// a shift, a mask and an integer-to-float conversion (a quarter-rate
+// instruction; a node needs 48 of them).  Bit-identical to (float)byte.
+#ifndef PK_CW_I2F
+__device__ __forceinline__ float byte_float(uint32_t word, int k) {
+  return __fsub_rn(__uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | (uint32_t)k)), 8388608.0f);
+}
+#else
+__device__ __forceinline__ float byte_float(uint32_t word, int k) { return (float)((word >> (8 * k)) & 0xffu); }
+#endif
+
 // Child test of one compressed wide node (pk_wide.h).  Returns the node's
 // internal-child hit mask, with the child of slot s at bit (s ^ oct) (the
 // visiting order of the ray's octant), and the triangle-record hit mask
@@ -130,14 +142,14 @@ __device__ __forceinline__ void cw_node(const float4* __restrict__ nodes, uint32
   tri_hits = 0u;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    const int sh = 8 * (k & 3);
+    const int sh = 8 * (k & 3), kb = k & 3;
     const uint32_t meta = ((k < 4 ? b.z : b.w) >> sh) & 0xffu;
-    const float tnx = __fmaf_rn((float)(((k < 4 ? nx0 : nx1) >> sh) & 0xffu), bx, ax);
-    const float tny = __fmaf_rn((float)(((k < 4 ? ny0 : ny1) >> sh) & 0xffu), by, ay);
-    const float tnz = __fmaf_rn((float)(((k < 4 ? nz0 : nz1) >> sh) & 0xffu), bz, az);
-    const float tfx = __fmaf_rn((float)(((k < 4 ? fx0 : fx1) >> sh) & 0xffu), bx, ax);
-    const float tfy = __fmaf_rn((float)(((k < 4 ? fy0 : fy1) >> sh) & 0xffu), by, ay);
-    const float tfz = __fmaf_rn((float)(((k < 4 ? fz0 : fz1) >> sh) & 0xffu), bz, az);
+    const float tnx = __fmaf_rn(byte_float(k < 4 ? nx0 : nx1, kb), bx, ax);
+    const float tny = __fmaf_rn(byte_float(k < 4 ? ny0 : ny1, kb), by, ay);
+    const float tnz = __fmaf_rn(byte_float(k < 4 ? nz0 : nz1, kb), bz, az);
+    const float tfx = __fmaf_rn(byte_float(k < 4 ? fx0 : fx1, kb), bx, ax);
+    const float tfy = __fmaf_rn(byte_float(k < 4 ? fy0 : fy1, kb), by, ay);
+    const float tfz = __fmaf_rn(byte_float(k < 4 ? fz0 : fz1, kb), bz, az);
     const float tmin = fmaxf(fmaxf(tnx, tny), tnz);
     const float tmax = fminf(fminf(tfx, tfy), tfz);
     const float tmax_s = tmax + fabsf(tmax) * WIDE_SLACK;

@@ -2,10 +2,11 @@
 // (record layouts in pk_wide.h): the compressed 8-wide BVH and the FP32
 // binary reference's outward-rounded records.
 //
-// Inputs are the drop-in's device arrays (breadth-first binary nodes, the
-// leaf-ordered triangle indices, normalised vertices).  Every step works one
-// breadth-first level at a time with one thread per node, in double precision
-// where boxes are formed:
+// Inputs are the drop-in's device arrays (binary nodes with children after
+// their parents, the leaf-ordered triangle indices, normalised vertices).
+// Every step works one tree level at a time (the level's node list built top
+// down by a prefix sum) with one thread per node, in double precision where
+// boxes are formed:
 //   1. triangle boxes over the three vertices and the 48-byte triangle
 //      records of the binary leaf order (slot = leaf-order index);
 //   2. node boxes bottom up (leaf: union of its triangles, inner: union of
@@ -139,28 +140,37 @@ __global__ void k_tri_data(const int4* __restrict__ tri4, uint32_t n_tris, const
   tbox[t] = b;
 }
 
-// breadth-first levels: inner nodes of [b, e) (their children must form the next level)
-__global__ void k_count_inner(const int32_t* __restrict__ nodes5, uint32_t b, uint32_t e, uint32_t* count) {
-  const uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x;
-  const bool inner = i < e && nodes5[5 * (size_t)i + 1] <= -1;
-  const uint32_t m = __ballot_sync(0xffffffffu, inner);
-  if ((threadIdx.x & 31u) == 0 && m) atomicAdd(count, (uint32_t)__popc(m));
+// levels: order[b, e) lists the nodes of one level (any order within it);
+// the children of its inner nodes, in that order, form the next level
+__global__ void k_level_flags(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
+                              uint32_t e, uint32_t* __restrict__ flag) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b + k >= e) return;
+  flag[k] = nodes5[5 * (size_t)order[b + k] + 1] <= -1 ? 1u : 0u;
 }
-__global__ void k_check_children(const int32_t* __restrict__ nodes5, uint32_t b, uint32_t e, uint32_t next_end,
-                                 uint32_t* err) {
-  const uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= e) return;
-  const int32_t* nd = nodes5 + 5 * (size_t)i;
+__global__ void k_level_children(const int32_t* __restrict__ nodes5, uint32_t* __restrict__ order, uint32_t b,
+                                 uint32_t e, const uint32_t* __restrict__ rank, uint32_t n_nodes, uint32_t* err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b + k >= e) return;
+  const uint32_t node = order[b + k];
+  const int32_t* nd = nodes5 + 5 * (size_t)node;
   if (nd[1] > -1) return;
   const int32_t l = nd[0];
-  if (l < (int32_t)e || (uint32_t)l + 1 >= next_end) atomicOr(err, E_ORDER);
+  if (l <= (int32_t)node || (uint32_t)l + 1 >= n_nodes) {  // children must come after their parent
+    atomicOr(err, E_ORDER);
+    return;
+  }
+  order[e + 2 * rank[k]] = (uint32_t)l;
+  order[e + 2 * rank[k] + 1] = (uint32_t)l + 1;
 }
 
 // 2. node boxes of one level (children already done)
-__global__ void k_node_boxes(const int32_t* __restrict__ nodes5, uint32_t b, uint32_t e, uint32_t n_tris,
-                             const BoxD* __restrict__ tbox, BoxD* __restrict__ nbox, uint32_t* err) {
-  const uint32_t i = b + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= e) return;
+__global__ void k_node_boxes(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
+                             uint32_t e, uint32_t n_tris, const BoxD* __restrict__ tbox, BoxD* __restrict__ nbox,
+                             uint32_t* err) {
+  const uint32_t k = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e) return;
+  const uint32_t i = order[k];
   const int32_t* nd = nodes5 + 5 * (size_t)i;
   BoxD bx = box_empty();
   if (nd[1] > -1) {
@@ -184,11 +194,12 @@ __global__ void k_widen(BoxD* __restrict__ box, uint32_t n) {
 }
 
 // 3. the collapse's dynamic programme for one level
-__global__ void k_collapse(const int32_t* __restrict__ nodes5, uint32_t b, uint32_t e, const BoxD* __restrict__ nbox,
-                           float* __restrict__ cost, uint8_t* __restrict__ opt, uint8_t* __restrict__ split,
-                           uint32_t* __restrict__ tris) {
-  const uint32_t n = b + blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= e) return;
+__global__ void k_collapse(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
+                           uint32_t e, const BoxD* __restrict__ nbox, float* __restrict__ cost,
+                           uint8_t* __restrict__ opt, uint8_t* __restrict__ split, uint32_t* __restrict__ tris) {
+  const uint32_t k = b + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= e) return;
+  const uint32_t n = order[k];
   const int32_t* nd = nodes5 + 5 * (size_t)n;
   float* C = cost + 8 * (size_t)n;
   uint8_t* O = opt + 8 * (size_t)n;
@@ -544,15 +555,16 @@ uint32_t read_u32(cudaStream_t s, const uint32_t* p) {
 const char* error_text(uint32_t e) {
   if (e & E_VERTEX) return "triangle vertex index out of range";
   if (e & E_LEAF) return "leaf outside the triangle array";
-  if (e & E_ORDER) return "binary nodes not in breadth-first order";
+  if (e & E_ORDER) return "malformed binary tree (a child not after its parent, or a node not reached once)";
   if (e & E_FIT) return "child box does not fit its 8-bit frame";
   return "internal error";
 }
 
-// Steps 1 and 2, shared by both builds: breadth-first level bounds, triangle
+// Steps 1 and 2, shared by both builds: the levels (node lists), triangle
 // boxes and records, widened node boxes.
 struct Prepared {
-  std::vector<uint32_t> level;  // level d = [level[d], level[d + 1])
+  std::vector<uint32_t> level;  // level d = order[level[d], level[d + 1])
+  DevBuf<uint32_t> order;
   DevBuf<BoxD> tbox, nbox;
   DevBuf<float> brecs;
 };
@@ -562,25 +574,27 @@ int prepare(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4*
   P.brecs.alloc((size_t)WIDE_TRI_FLOATS * std::max<uint32_t>(n_tris, 1u));
   P.nbox.alloc(n_nodes);
   if (n_tris) k_tri_data<<<blocks(n_tris), 128, 0, s>>>(tri4, n_tris, verts4, n_verts, P.tbox.p, P.brecs.p, err.p);
-  DevBuf<uint32_t> cnt(1);
+  P.order.alloc(n_nodes);
+  check(cudaMemsetAsync(P.order.p, 0, 4, s), "memset");  // the root
+  DevBuf<uint32_t> flag(n_nodes), tot(1);
   P.level.assign(1, 0u);
   uint32_t b = 0, e = 1;
   while (b < e) {
     P.level.push_back(e);
-    check(cudaMemsetAsync(cnt.p, 0, 4, s), "memset");
-    k_count_inner<<<blocks(e - b), 128, 0, s>>>(nodes5, b, e, cnt.p);
-    const uint32_t c = read_u32(s, cnt.p);
+    k_level_flags<<<blocks(e - b), 128, 0, s>>>(nodes5, P.order.p, b, e, flag.p);
+    scan_exclusive_u32(s, flag.p, flag.p, e - b, tot.p);
+    const uint32_t c = read_u32(s, tot.p);
     const uint64_t next_end = (uint64_t)e + 2ull * c;
     if (next_end > n_nodes) { why = error_text(E_ORDER); return 1; }
-    k_check_children<<<blocks(e - b), 128, 0, s>>>(nodes5, b, e, (uint32_t)next_end, err.p);
+    k_level_children<<<blocks(e - b), 128, 0, s>>>(nodes5, P.order.p, b, e, flag.p, n_nodes, err.p);
     b = e;
     e = (uint32_t)next_end;
   }
   if (e != n_nodes) { why = error_text(E_ORDER); return 1; }
   if (uint32_t ev = read_u32(s, err.p)) { why = error_text(ev); return 1; }
   for (size_t d = P.level.size() - 1; d-- > 0;)
-    k_node_boxes<<<blocks(P.level[d + 1] - P.level[d]), 128, 0, s>>>(nodes5, P.level[d], P.level[d + 1], n_tris,
-                                                                      P.tbox.p, P.nbox.p, err.p);
+    k_node_boxes<<<blocks(P.level[d + 1] - P.level[d]), 128, 0, s>>>(nodes5, P.order.p, P.level[d], P.level[d + 1],
+                                                                      n_tris, P.tbox.p, P.nbox.p, err.p);
   k_widen<<<blocks(n_nodes), 128, 0, s>>>(P.nbox.p, n_nodes);
   check(cudaGetLastError(), "form (1) boxes");
   if (uint32_t ev = read_u32(s, err.p)) { why = error_text(ev); return 1; }
@@ -601,8 +615,8 @@ int build_wide_bvh_gpu(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, 
   DevBuf<uint8_t> opt(8 * (size_t)n_nodes), split(n_nodes);
   DevBuf<uint32_t> ntri(n_nodes);
   for (size_t d = P.level.size() - 1; d-- > 0;)
-    k_collapse<<<blocks(P.level[d + 1] - P.level[d]), 128, 0, s>>>(nodes5, P.level[d], P.level[d + 1], P.nbox.p,
-                                                                    cost.p, opt.p, split.p, ntri.p);
+    k_collapse<<<blocks(P.level[d + 1] - P.level[d]), 128, 0, s>>>(nodes5, P.order.p, P.level[d], P.level[d + 1],
+                                                                    P.nbox.p, cost.p, opt.p, split.p, ntri.p);
   check(cudaGetLastError(), "k_collapse");
   const BuildView V{nodes5, P.tbox.p, P.nbox.p, opt.p, split.p, ntri.p};
   // top down; node capacity grows geometrically
