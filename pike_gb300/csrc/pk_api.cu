@@ -414,9 +414,7 @@ static int finish_bvh(pk_ctx* c) {
   c->exact_ready = false;
   c->exact.release();
   c->exact_tris.release();
-  // at least 128 records, so that a traversal may stage the first records of
-  // any tree in shared memory without reading past the allocation
-  c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 128u));
+  c->inner.alloc(4 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->inner32.alloc(2 * (size_t)std::max<uint32_t>(c->n_nodes, 1u));
   c->tris.alloc(3 * (size_t)std::max<uint32_t>(c->n_leaf_tris, 1u));
   DevBuf<int> root(1);

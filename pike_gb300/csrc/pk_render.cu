@@ -174,12 +174,6 @@ __device__ __forceinline__ void inner_children_exact(const SceneDev& sc, int cur
 // 10 resident blocks per SM (<= 48 registers): with several frames in
 // flight this beats the unconstrained 55 registers (2607-2611 vs 2579-2581
 // Mrays/s at 1080p, paired runs) and 12 blocks (2494).
-// PK_TREELET > 0 stages the first PK_TREELET inner records (the top levels:
-// records are numbered breadth first) in shared memory per block; the inner
-// record array is allocated with at least TREELET_ALLOC records.
-#ifndef PK_TREELET
-#define PK_TREELET 0
-#endif
 template <bool ANY, bool FUSED, bool COUNT, bool EXACT>
 __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                               const uint32_t* __restrict__ countp, RayQ R,
@@ -187,13 +181,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
                                                               float4* __restrict__ color, uint32_t npix,
                                                               uint32_t* __restrict__ ticket, int defer) {
   __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
-#if PK_TREELET > 0
-  __shared__ float4 s_tree[EXACT ? 1 : 4 * PK_TREELET];
-  const bool treelet = !EXACT && sc.inner32 == nullptr;
-  if (treelet)
-    for (int i = threadIdx.x; i < 4 * PK_TREELET; i += TRACE_THREADS) s_tree[i] = __ldg(sc.inner + i);
-  __syncthreads();
-#endif
   int lstack[STACK_LOCAL];
   const uint32_t n = *countp;
   const int lane = threadIdx.x & 31;
@@ -321,16 +308,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
         lok = lh < MAX_T && lh <= lim;
         rok = rh < MAX_T && rh <= lim;
       } else {
-#if PK_TREELET > 0
-        if (treelet && cur < PK_TREELET) {
-          const float4 a = s_tree[4 * cur], b = s_tree[4 * cur + 1], c4 = s_tree[4 * cur + 2];
-          const float4 chf = s_tree[4 * cur + 3];
-          lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
-          rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
-          cl = __float_as_int(chf.x);
-          cr = __float_as_int(chf.y);
-        } else
-#endif
         inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
         lok = lh < best_t;
         rok = rh < best_t;

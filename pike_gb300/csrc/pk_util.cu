@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <string>
 #include <utility>
+#include <vector>
 
 #include "pk_internal.cuh"
 #include "pk_util.h"
@@ -164,6 +166,59 @@ void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64
     check(cudaMemcpyAsync(keys, kin, (size_t)n * 8, cudaMemcpyDeviceToDevice, s), "memcpy");
     check(cudaMemcpyAsync(vals, vin, (size_t)n * 4, cudaMemcpyDeviceToDevice, s), "memcpy");
   }
+}
+
+// ---- levels of a binary tree ------------------------------------------------
+// order[b, e) lists the nodes of one level (any order within it); the
+// children of its inner nodes, in that order, form the next level.
+__global__ void k_level_flags(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
+                              uint32_t e, uint32_t* __restrict__ flag) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b + k >= e) return;
+  flag[k] = nodes5[5 * (size_t)order[b + k] + 1] <= -1 ? 1u : 0u;
+}
+__global__ void k_level_children(const int32_t* __restrict__ nodes5, uint32_t* __restrict__ order, uint32_t b,
+                                 uint32_t e, const uint32_t* __restrict__ rank, uint32_t n_nodes, uint32_t* err) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b + k >= e) return;
+  const uint32_t node = order[b + k];
+  const int32_t* nd = nodes5 + 5 * (size_t)node;
+  if (nd[1] > -1) return;
+  const int32_t l = nd[0];
+  if (l <= (int32_t)node || (uint32_t)l + 1 >= n_nodes) {  // children must come after their parent
+    atomicOr(err, 1u);
+    return;
+  }
+  order[e + 2 * rank[k]] = (uint32_t)l;
+  order[e + 2 * rank[k] + 1] = (uint32_t)l + 1;
+}
+
+int tree_levels(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, DevBuf<uint32_t>& order,
+                std::vector<uint32_t>& level) {
+  order.alloc(std::max<uint32_t>(n_nodes, 1u));
+  check(cudaMemsetAsync(order.p, 0, 4, s), "memset");  // the root
+  DevBuf<uint32_t> flag(std::max<uint32_t>(n_nodes, 1u)), tot(1), err(1);
+  check(cudaMemsetAsync(err.p, 0, 4, s), "memset");
+  level.assign(1, 0u);
+  uint32_t b = 0, e = n_nodes ? 1u : 0u;
+  uint32_t c = 0;
+  while (b < e) {
+    level.push_back(e);
+    const unsigned blocks = (e - b + 127) / 128;
+    k_level_flags<<<blocks, 128, 0, s>>>(nodes5, order.p, b, e, flag.p);
+    scan_exclusive_u32(s, flag.p, flag.p, e - b, tot.p);
+    check(cudaMemcpyAsync(&c, tot.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+    check(cudaStreamSynchronize(s), "sync");
+    const uint64_t next_end = (uint64_t)e + 2ull * c;
+    if (next_end > n_nodes) return 1;
+    k_level_children<<<blocks, 128, 0, s>>>(nodes5, order.p, b, e, flag.p, n_nodes, err.p);
+    b = e;
+    e = (uint32_t)next_end;
+  }
+  uint32_t herr = 0;
+  check(cudaMemcpyAsync(&herr, err.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaStreamSynchronize(s), "sync");
+  return (e != n_nodes || herr) ? 1 : 0;
 }
 
 }  // namespace pk

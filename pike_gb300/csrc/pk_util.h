@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 namespace pk {
 
@@ -52,6 +53,14 @@ void scan_exclusive_u32(cudaStream_t s, const uint32_t* in, uint32_t* out, uint3
 // 64-bit keys, ascending.  Sorts in place using the given scratch buffers.
 void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64_t* keys_tmp, uint32_t* vals_tmp,
                           uint32_t n, int bits);
+
+// The levels of a binary tree (nodes5: 5 words per node, word 0 the left
+// child (the right child follows it), word 1 > -1 for a leaf; children after
+// their parents): the nodes of depth d are order[level[d], level[d + 1]).
+// Returns non-zero when the tree is malformed (a child not after its parent,
+// or a node not reached exactly once).
+int tree_levels(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, DevBuf<uint32_t>& order,
+                std::vector<uint32_t>& level);
 
 // EnvironmentGenerator tables on the GPU (pk_env.cu).
 int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,

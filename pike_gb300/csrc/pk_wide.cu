@@ -140,30 +140,6 @@ __global__ void k_tri_data(const int4* __restrict__ tri4, uint32_t n_tris, const
   tbox[t] = b;
 }
 
-// levels: order[b, e) lists the nodes of one level (any order within it);
-// the children of its inner nodes, in that order, form the next level
-__global__ void k_level_flags(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
-                              uint32_t e, uint32_t* __restrict__ flag) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b + k >= e) return;
-  flag[k] = nodes5[5 * (size_t)order[b + k] + 1] <= -1 ? 1u : 0u;
-}
-__global__ void k_level_children(const int32_t* __restrict__ nodes5, uint32_t* __restrict__ order, uint32_t b,
-                                 uint32_t e, const uint32_t* __restrict__ rank, uint32_t n_nodes, uint32_t* err) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b + k >= e) return;
-  const uint32_t node = order[b + k];
-  const int32_t* nd = nodes5 + 5 * (size_t)node;
-  if (nd[1] > -1) return;
-  const int32_t l = nd[0];
-  if (l <= (int32_t)node || (uint32_t)l + 1 >= n_nodes) {  // children must come after their parent
-    atomicOr(err, E_ORDER);
-    return;
-  }
-  order[e + 2 * rank[k]] = (uint32_t)l;
-  order[e + 2 * rank[k] + 1] = (uint32_t)l + 1;
-}
-
 // 2. node boxes of one level (children already done)
 __global__ void k_node_boxes(const int32_t* __restrict__ nodes5, const uint32_t* __restrict__ order, uint32_t b,
                              uint32_t e, uint32_t n_tris, const BoxD* __restrict__ tbox, BoxD* __restrict__ nbox,
@@ -574,23 +550,7 @@ int prepare(cudaStream_t s, const int32_t* nodes5, uint32_t n_nodes, const int4*
   P.brecs.alloc((size_t)WIDE_TRI_FLOATS * std::max<uint32_t>(n_tris, 1u));
   P.nbox.alloc(n_nodes);
   if (n_tris) k_tri_data<<<blocks(n_tris), 128, 0, s>>>(tri4, n_tris, verts4, n_verts, P.tbox.p, P.brecs.p, err.p);
-  P.order.alloc(n_nodes);
-  check(cudaMemsetAsync(P.order.p, 0, 4, s), "memset");  // the root
-  DevBuf<uint32_t> flag(n_nodes), tot(1);
-  P.level.assign(1, 0u);
-  uint32_t b = 0, e = 1;
-  while (b < e) {
-    P.level.push_back(e);
-    k_level_flags<<<blocks(e - b), 128, 0, s>>>(nodes5, P.order.p, b, e, flag.p);
-    scan_exclusive_u32(s, flag.p, flag.p, e - b, tot.p);
-    const uint32_t c = read_u32(s, tot.p);
-    const uint64_t next_end = (uint64_t)e + 2ull * c;
-    if (next_end > n_nodes) { why = error_text(E_ORDER); return 1; }
-    k_level_children<<<blocks(e - b), 128, 0, s>>>(nodes5, P.order.p, b, e, flag.p, n_nodes, err.p);
-    b = e;
-    e = (uint32_t)next_end;
-  }
-  if (e != n_nodes) { why = error_text(E_ORDER); return 1; }
+  if (tree_levels(s, nodes5, n_nodes, P.order, P.level)) { why = error_text(E_ORDER); return 1; }
   if (uint32_t ev = read_u32(s, err.p)) { why = error_text(ev); return 1; }
   for (size_t d = P.level.size() - 1; d-- > 0;)
     k_node_boxes<<<blocks(P.level[d + 1] - P.level[d]), 128, 0, s>>>(nodes5, P.order.p, P.level[d], P.level[d + 1],
