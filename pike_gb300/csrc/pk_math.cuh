@@ -186,18 +186,10 @@ __device__ __forceinline__ float qdiv(float v, float d, float r) {
   const float q0 = __fmul_rn(v, r);
   return __fmaf_rn(__fmaf_rn(-q0, d, v), r, q0);
 }
-// Integer to float for |v| < 2^22, exactly and without the (quarter-rate)
-// conversion unit: the float 1.5 * 2^23 has ulp 1, so adding v to its bit
-// pattern gives the float 1.5 * 2^23 + v, and one exact subtraction leaves v.
-#ifndef PK_CVT_I2F
-__device__ __forceinline__ float small_i2f(int v) { return __fsub_rn(__int_as_float(0x4B400000 + v), 12582912.0f); }
-#else
-__device__ __forceinline__ float small_i2f(int v) { return (float)v; }
-#endif
-__device__ __forceinline__ float unorm16(uint32_t v) { return qdiv(small_i2f((int)v), 65535.0f, 0x1.0001p-16f); }
-__device__ __forceinline__ float snorm16(int v) { return fmax_(qdiv(small_i2f(v), 32767.0f, 0x1.0002p-15f), -1.0f); }
-__device__ __forceinline__ float snorm8(int v) { return fmax_(qdiv(small_i2f(v), 127.0f, 0x1.020408p-7f), -1.0f); }
-__device__ __forceinline__ float unorm8(uint32_t v) { return qdiv(small_i2f((int)v), 255.0f, 0x1.010102p-8f); }
+__device__ __forceinline__ float unorm16(uint32_t v) { return qdiv((float)v, 65535.0f, 0x1.0001p-16f); }
+__device__ __forceinline__ float snorm16(int v) { return fmax_(qdiv((float)v, 32767.0f, 0x1.0002p-15f), -1.0f); }
+__device__ __forceinline__ float snorm8(int v) { return fmax_(qdiv((float)v, 127.0f, 0x1.020408p-7f), -1.0f); }
+__device__ __forceinline__ float unorm8(uint32_t v) { return qdiv((float)v, 255.0f, 0x1.010102p-8f); }
 __device__ __forceinline__ uint32_t pack_unorm16(float e) {
   return (uint32_t)floorf(0.5f + 65535.0f * fmin_(1.0f, fmax_(0.0f, e)));
 }
