@@ -146,6 +146,10 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 #define PK_ANY_SPEC 0
 #endif
 constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
+#ifndef PK_INNER_BUDGET
+#define PK_INNER_BUDGET 0
+#endif
+constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 
 // Box test of the exact binary records: like box_hit, with the far distance
 // widened by WIDE_SLACK (relative) so that rounding never drops a box.
@@ -296,8 +300,10 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       }
       if (!fin && pl == 0 && cur == SPEC_DONE) fin = true;
     }
-    // inner nodes
-    while (!SPEC && cur >= 0) {
+    // inner nodes (at most INNER_BUDGET steps before the warp meets again at
+    // the top of the loop, when the budget is not 0)
+    int budget = INNER_BUDGET;
+    while (!SPEC && cur >= 0 && (INNER_BUDGET == 0 || budget-- > 0)) {
       if (COUNT) nfetch += 3;
       float lh, rh;
       int cl, cr;
