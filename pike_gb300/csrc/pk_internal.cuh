@@ -139,6 +139,55 @@ __device__ __forceinline__ unsigned long long lookback2(unsigned long long* tile
   return excl;
 }
 
+// The same prefix computed by one whole warp (every lane calls it; all get
+// the result): each round reads a window of 32 earlier tiles at once, waits
+// (bounded) until each has published, and sums the aggregates from the tile
+// before this one back to the nearest tile holding an inclusive prefix, which
+// ends the walk.  A walk over n unfinished predecessors takes n / 32 rounds
+// of memory latency instead of n.
+__device__ __forceinline__ unsigned long long lookback2_warp(unsigned long long* tiles, uint32_t tile,
+                                                             unsigned long long agg, uint32_t* err) {
+  const int lane = (int)(threadIdx.x & 31u);
+  if (tile == 0) {
+    if (lane == 0) st_release(&tiles[0], TILE_PRE | agg);
+    return 0ull;
+  }
+  if (lane == 0) st_release(&tiles[tile], TILE_AGG | agg);
+  unsigned long long excl = 0;
+  int base = (int)tile - 1;  // the window is tiles base, base - 1, ..., base - 31
+  for (;;) {
+    const int i = base - lane;
+    unsigned long long v = i >= 0 ? ld_acquire(&tiles[i]) : TILE_PRE;  // before tile 0: an empty prefix
+    int spins = 0;
+    uint32_t pre;
+    for (;;) {  // until every tile from this one's predecessor to the nearest prefix has published
+      const uint32_t ready = __ballot_sync(0xffffffffu, (v & ~TILE_VAL) != 0);
+      pre = __ballot_sync(0xffffffffu, (v & ~TILE_VAL) == TILE_PRE);
+      const int last = pre ? __ffs(pre) - 1 : 31;
+      const uint32_t need = last == 31 ? 0xffffffffu : ((1u << (last + 1)) - 1u);
+      if ((ready & need) == need) break;
+      if ((v & ~TILE_VAL) == 0) {
+        if (++spins > LOOKBACK_SPIN_LIMIT) {
+          atomicOr(err, ERR_LOOKBACK);
+          v = TILE_PRE;
+        } else {
+          __nanosleep(64);
+          v = ld_acquire(&tiles[i]);
+        }
+      }
+    }
+    const int first = pre ? __ffs(pre) - 1 : 32;  // the nearest inclusive prefix in the window
+    unsigned long long c = lane <= first ? (v & TILE_VAL) : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    excl += c;
+    if (pre) break;
+    base -= 32;
+  }
+  if (lane == 0) st_release(&tiles[tile], TILE_PRE | (excl + agg));
+  return excl;
+}
+
 // Block-wide exclusive scan of two per-thread counts (blockDim.x <= 1024,
 // multiple of 32).  Returns this thread's exclusive offsets and the block totals.
 template <int NWARPS>

@@ -564,6 +564,12 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
 //   MODE 1: any-hit flags     -> unoccluded shadow rays appended to the miss queue
 // =====================================================================
 constexpr int COMPACT_THREADS = 256;
+// The compaction and shade kernels take their tile's prefix with a whole warp
+// (lookback2_warp) rather than one thread (lookback2).
+#ifndef PK_LOOKBACK_WARP
+#define PK_LOOKBACK_WARP 1
+#endif
+constexpr bool LOOKBACK_WARP = PK_LOOKBACK_WARP;
 
 template <int MODE, bool MISSQ>
 __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restrict__ ctr,
@@ -603,7 +609,14 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
     const uint32_t cb = (MODE == 1 || MISSQ) ? (uint32_t)__popc(mm) : 0u;
     uint32_t ea, eb, ta, tb;
     block_scan2<COMPACT_THREADS / 32>(ca, cb, ea, eb, ta, tb, s_warp);
-    if (threadIdx.x == 0) s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    if (LOOKBACK_WARP) {
+      if (threadIdx.x < 32) {
+        const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
+        if (threadIdx.x == 0) s_excl = e;
+      }
+    } else if (threadIdx.x == 0) {
+      s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    }
     __syncthreads();
     const uint32_t pa = unpack_a(s_excl) + ea;
     uint32_t pb = unpack_b(s_excl) + eb;
@@ -783,7 +796,14 @@ __global__ void __launch_bounds__(SHADE_THREADS, 12) k_shade(SceneDev sc, EnvDev
     }
     uint32_t ea, es2, ta, tb;
     block_scan2<SHADE_THREADS / 32>(eb ? 1u : 0u, es ? 1u : 0u, ea, es2, ta, tb, s_warp);
-    if (threadIdx.x == 0) s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    if (LOOKBACK_WARP) {
+      if (threadIdx.x < 32) {
+        const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
+        if (threadIdx.x == 0) s_excl = e;
+      }
+    } else if (threadIdx.x == 0) {
+      s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    }
     __syncthreads();
     const uint32_t pb = unpack_a(s_excl) + ea, ps = unpack_b(s_excl) + es2;
     if (eb) {
