@@ -61,6 +61,12 @@ namespace pk {
 
 constexpr int DIFF_THREADS = 128;  // = TRACE_THREADS (traversal stack layout)
 constexpr int DIFF_MAX_DEPTH = 8;
+#ifndef PK_DIFF_FWD_BLOCKS
+#define PK_DIFF_FWD_BLOCKS 1
+#endif
+#ifndef PK_DIFF_ADJ_BLOCKS
+#define PK_DIFF_ADJ_BLOCKS 1
+#endif
 
 struct DiffParams {
   const float* albedo;  // n_mats x 3 (base colour)
@@ -374,7 +380,7 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
   }
 }
 
-__global__ void __launch_bounds__(DIFF_THREADS) k_diff_forward(SceneDev sc, EnvDev env, CamState cam, DiffParams P,
+__global__ void __launch_bounds__(DIFF_THREADS, PK_DIFF_FWD_BLOCKS) k_diff_forward(SceneDev sc, EnvDev env, CamState cam, DiffParams P,
                                                                float theta, uint32_t W, uint32_t H,
                                                                float4* __restrict__ image, uint32_t* err,
                                                                unsigned long long* rays) {
@@ -404,7 +410,7 @@ __device__ __forceinline__ float group_sum(unsigned mask, int key, float v, bool
   return sum;
 }
 
-__global__ void __launch_bounds__(DIFF_THREADS) k_diff_adjoint(SceneDev sc, EnvDev env, CamState cam, DiffParams P,
+__global__ void __launch_bounds__(DIFF_THREADS, PK_DIFF_ADJ_BLOCKS) k_diff_adjoint(SceneDev sc, EnvDev env, CamState cam, DiffParams P,
                                                                float theta, uint32_t W, uint32_t H,
                                                                const float4* __restrict__ dimage,
                                                                double* __restrict__ g_albedo,
