@@ -146,8 +146,13 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 #define PK_ANY_SPEC 0
 #endif
 constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
+// Inner-node steps a lane takes before the warp meets again at the top of the
+// loop (0: until it reaches a leaf).  Lanes whose rays need many steps no
+// longer hold the warp while the others wait in the leaf loop or idle for a
+// refill; measured at 1080p (same call): 4 steps 3340 Mrays/s, unbounded
+// 3137-3140, 1 step 2749-2754.
 #ifndef PK_INNER_BUDGET
-#define PK_INNER_BUDGET 0
+#define PK_INNER_BUDGET 4
 #endif
 constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 
