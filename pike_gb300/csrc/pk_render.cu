@@ -521,7 +521,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
         G = make_uint2(0u, 0u);
       }
       const bool tested = T.y != 0u;
-    while (!fin && T.y != 0u) {
+      while (!fin && T.y != 0u) {
         if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
           if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
           T.y = 0u;
