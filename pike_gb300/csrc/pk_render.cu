@@ -149,12 +149,22 @@ constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
 // Inner-node steps a lane takes before the warp meets again at the top of the
 // loop (0: until it reaches a leaf).  Lanes whose rays need many steps no
 // longer hold the warp while the others wait in the leaf loop or idle for a
-// refill; measured at 1080p (same call): 4 steps 3340 Mrays/s, unbounded
-// 3137-3140, 1 step 2749-2754.
+// refill.  Measured at 1080p, Mrays/s: unbounded 3137-3140; 1 step
+// 2749-2754, 2: 3082, 3: 3171-3190, 4: 3288-3342, 6: 3281-3294, 8:
+// 3365-3418, 12: 3345-3349, 16: 3248-3267, 24: 3165-3167.  PK_ANY_BUDGET
+// is the any-hit kernel's (default: the same).
 #ifndef PK_INNER_BUDGET
-#define PK_INNER_BUDGET 4
+#define PK_INNER_BUDGET 8
+#endif
+#ifndef PK_ANY_BUDGET
+#define PK_ANY_BUDGET PK_INNER_BUDGET
 #endif
 constexpr int INNER_BUDGET = PK_INNER_BUDGET;
+#ifndef PK_LEAF_BUDGET
+#define PK_LEAF_BUDGET 0
+#endif
+constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
+constexpr int ANY_BUDGET = PK_ANY_BUDGET;
 
 // Box test of the exact binary records: like box_hit, with the far distance
 // widened by WIDE_SLACK (relative) so that rounding never drops a box.
@@ -307,8 +317,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
     }
     // inner nodes (at most INNER_BUDGET steps before the warp meets again at
     // the top of the loop, when the budget is not 0)
-    int budget = INNER_BUDGET;
-    while (!SPEC && cur >= 0 && (INNER_BUDGET == 0 || budget-- > 0)) {
+    constexpr int BUDGET = ANY ? ANY_BUDGET : INNER_BUDGET;
+    int budget = BUDGET;
+    while (!SPEC && cur >= 0 && (BUDGET == 0 || budget-- > 0)) {
       if (COUNT) nfetch += 3;
       float lh, rh;
       int cl, cr;
@@ -339,8 +350,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       --sp;
       cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
     }
-    // leaves
-    while (!SPEC && !fin && cur < 0) {
+    // leaves (at most LEAF_BUDGET before the warp meets, when not 0)
+    int lbudget = LEAF_BUDGET;
+    while (!SPEC && !fin && cur < 0 && (LEAF_BUDGET == 0 || lbudget-- > 0)) {
       if (COUNT) nfetch += 1;
       const uint32_t word = (uint32_t)cur & 0x7fffffffu;
       const int size = (int)(word >> 24);
