@@ -422,7 +422,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
 // instead and tested later (Ylitie et al.'s triangle postponing); measured on
 // the 1080p benchmark it costs more than it saves (p = 4: 2669 Mrays/s,
 // p = 8: 2569, p = 0: 2939), so it is off by default.  Lanes take new rays as
-// in k_trace_dyn.
+// in k_trace_dyn.  Unlike the binary traversal, letting a lane visit several
+// nodes in a row before the warp meets again did not pay (1080p: one visit
+// 3102-3108 Mrays/s, up to two 2893-2900, up to four 1753-1767).
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
@@ -432,10 +434,6 @@ constexpr int CW_STACK_LOCAL = 16;  // overflow entries in local memory
 #define PK_CW_POSTPONE 0
 #endif
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
-#ifndef PK_CW_BUDGET
-#define PK_CW_BUDGET 1
-#endif
-constexpr int CW_BUDGET = PK_CW_BUDGET;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -512,54 +510,49 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
     if (!__any_sync(0xffffffffu, have)) break;
     if (!have) continue;
     bool fin = false;
-    // up to CW_BUDGET node visits while no triangle is tested, then the warp meets
-    for (int step = 1;; ++step) {
-      if (G.y > 0x00ffffffu) {  // visit the nearest remaining child of the node group
-        const uint32_t bit = (uint32_t)__ffs(G.y >> 24) - 1u;
-        const uint32_t slot = bit ^ oct;
-        const uint32_t node = G.x + (uint32_t)__popc(G.y & ((1u << slot) - 1u) & 0xffu);
-        G.y &= ~(1u << (24u + bit));
-        if (G.y > 0x00ffffffu && !cw_push(sstack, lstack, tid, sp, G)) {
-          atomicOr(&ctr->err, ERR_STACK);
-          fin = true;
-        }
-        if (COUNT) nfetch += 1;
-        uint32_t cb, tb, im, ih, th;
-        cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
-        G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
-        T = make_uint2(tb, th);
-      } else {  // a triangle group taken from the stack
-        T = G;
-        G = make_uint2(0u, 0u);
+    if (G.y > 0x00ffffffu) {  // visit the nearest remaining child of the node group
+      const uint32_t bit = (uint32_t)__ffs(G.y >> 24) - 1u;
+      const uint32_t slot = bit ^ oct;
+      const uint32_t node = G.x + (uint32_t)__popc(G.y & ((1u << slot) - 1u) & 0xffu);
+      G.y &= ~(1u << (24u + bit));
+      if (G.y > 0x00ffffffu && !cw_push(sstack, lstack, tid, sp, G)) {
+        atomicOr(&ctr->err, ERR_STACK);
+        fin = true;
       }
-      const bool tested = T.y != 0u;
-      while (!fin && T.y != 0u) {
-        if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
-          if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
-          T.y = 0u;
-          break;
-        }
-        const uint32_t i = (uint32_t)__ffs(T.y) - 1u;
-        T.y &= T.y - 1u;
-        if (COUNT) ntest += 1;
-        float t, u, v;
-        uint32_t slot;
-        if (wt_test(sc.wtris, T.x + i, wr, eps, t, u, v, slot) &&
-            (t < best_t || (t == best_t && (int)slot < best_i))) {
-          best_t = t;
-          best_i = (int)slot;
-          best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
-          if (ANY && !COUNT) fin = true;  // any hit: the first is enough
-        }
+      if (COUNT) nfetch += 1;
+      uint32_t cb, tb, im, ih, th;
+      cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
+      G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
+      T = make_uint2(tb, th);
+    } else {  // a triangle group taken from the stack
+      T = G;
+      G = make_uint2(0u, 0u);
+    }
+    while (!fin && T.y != 0u) {
+      if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
+        if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
+        T.y = 0u;
+        break;
       }
-      if (!fin) {
-        if (ANY && best_i != -1) fin = true;
-        else if (G.y <= 0x00ffffffu) {
-          if (sp == 0) fin = true;
-          else G = cw_pop(sstack, lstack, tid, sp);
-        }
+      const uint32_t i = (uint32_t)__ffs(T.y) - 1u;
+      T.y &= T.y - 1u;
+      if (COUNT) ntest += 1;
+      float t, u, v;
+      uint32_t slot;
+      if (wt_test(sc.wtris, T.x + i, wr, eps, t, u, v, slot) &&
+          (t < best_t || (t == best_t && (int)slot < best_i))) {
+        best_t = t;
+        best_i = (int)slot;
+        best_b = pack_unorm16(u) | (pack_unorm16(v) << 16);
+        if (ANY && !COUNT) fin = true;  // any hit: the first is enough
       }
-      if (fin || tested || step >= CW_BUDGET || G.y <= 0x00ffffffu) break;
+    }
+    if (!fin) {
+      if (ANY && best_i != -1) fin = true;
+      else if (G.y <= 0x00ffffffu) {
+        if (sp == 0) fin = true;
+        else G = cw_pop(sstack, lstack, tid, sp);
+      }
     }
     if (fin) {
       const bool hit = best_i != -1;
