@@ -621,6 +621,10 @@ def adjoint_form(args, local: int):
         scene.set_env_sampling(E)
         return float(l2_loss(sum(scene.render(A, R, E, seed=90000 + k) for k in range(8)) / 8, target_hq))
 
+    # the same with the environment known (materials only): how well the
+    # gradients recover what the image constrains without the map's ambiguity
+    a_k, r_k, _, hist_k = inverse_render(scene, target_hq, a0, r0, env, steps=steps, lr=0.02, n_free=n_free,
+                                         seed_per_step=True, seed=0, optimise_env=False)
     # recovery error: parameters the image constrains (materials on hit
     # surfaces, env texels the camera or a bounce sees: non-zero gradient at
     # the start)
@@ -648,7 +652,10 @@ def adjoint_form(args, local: int):
                 "albedo_mae_end": float((a[:n_free] - albedo[:n_free]).abs()[seen_m].mean()),
                 "roughness_mae_start": float((r0[:n_free] - rough[:n_free]).abs()[seen_m].mean()),
                 "roughness_mae_end": float((r[:n_free] - rough[:n_free]).abs()[seen_m].mean()),
-                "env_rel_l1_start": rel_env(e0), "env_rel_l1_end": rel_env(e)}}
+                "env_rel_l1_start": rel_env(e0), "env_rel_l1_end": rel_env(e),
+                "env_known": {"loss_eval_end": eval_loss(a_k, r_k, env),
+                              "albedo_mae_end": float((a_k[:n_free] - albedo[:n_free]).abs()[seen_m].mean()),
+                              "roughness_mae_end": float((r_k[:n_free] - rough[:n_free]).abs()[seen_m].mean())}}}
 
 
 def batch_form(args, local: int):

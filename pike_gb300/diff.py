@@ -173,19 +173,21 @@ def l2_loss(image, target):
 
 
 def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 200, lr: float = 0.02,
-                   n_free: int | None = None, seed_per_step: bool = True, seed: int = 0, env_floor: float = 1e-3):
+                   n_free: int | None = None, seed_per_step: bool = True, seed: int = 0, env_floor: float = 1e-3,
+                   optimise_env: bool = True):
     """Adam on (albedo, roughness, env) towards the target image; materials at
     index >= n_free stay fixed.  With seed_per_step, step k renders with seed
     2k and differentiates with the independent samples of seed 2k + 1
     (decorrelated: unbiased gradients of the expected image's L2 error);
     otherwise every step renders and differentiates `seed` (common random
-    numbers: a deterministic objective).  Returns the parameters and the loss
-    history."""
+    numbers: a deterministic objective).  With optimise_env=False the map
+    stays as given and only the materials move.  Returns the parameters and
+    the loss history."""
     import torch
     a = albedo.clone().requires_grad_(True)
     r = rough.clone().requires_grad_(True)
-    e = env.clone().requires_grad_(True)
-    opt = torch.optim.Adam([a, r, e], lr=lr)
+    e = env.clone().requires_grad_(optimise_env)
+    opt = torch.optim.Adam([a, r, e] if optimise_env else [a, r], lr=lr)
     keep = None
     if n_free is not None and n_free < a.shape[0]:
         keep = (a.detach()[n_free:].clone(), r.detach()[n_free:].clone())
