@@ -164,6 +164,10 @@ constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 #define PK_LEAF_BUDGET 0
 #endif
 constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
+#ifndef PK_ANY_LEAF_FIRST
+#define PK_ANY_LEAF_FIRST 0
+#endif
+constexpr bool ANY_LEAF_FIRST = PK_ANY_LEAF_FIRST;
 constexpr int ANY_BUDGET = PK_ANY_BUDGET;
 
 // Box test of the exact binary records: like box_hit, with the far distance
@@ -337,6 +341,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (lok && rok) {
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
+        // any hit only needs some hit: with PK_ANY_LEAF_FIRST a leaf child is
+        // visited before an inner one (the counting variant keeps the order)
+        if (ANY_LEAF_FIRST && ANY && !COUNT && !EXACT && farc < 0 && nearc >= 0) {
+          const int t = nearc; nearc = farc; farc = t;
+        }
         if (sp < STACK_SMEM) sstack[sp][tid] = farc;
         else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
         else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
@@ -774,7 +783,10 @@ __device__ __forceinline__ bool shade_one(const SceneDev& sc, const EnvDev& env,
   return emitted;
 }
 
-__global__ void __launch_bounds__(SHADE_THREADS, 12) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+#ifndef PK_SHADE_BLOCKS
+#define PK_SHADE_BLOCKS 12
+#endif
+__global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                           const uint32_t* __restrict__ hit_list,
                                                           const uint4* __restrict__ hrec, RayQ Rin, RayQ Rout,
                                                           RayQ S, uint32_t capacity, float4* __restrict__ color,
