@@ -136,8 +136,21 @@ struct DiffShade {
   int mat;
 };
 
+// Out of line by default (PK_DIFF_INLINE=0): the path loop of the forward
+// and adjoint kernels with the shading and both traversals inlined overflows
+// the instruction cache (ncu: instruction-fetch stalls were the largest
+// stall reason), as in the batch kernel.
+#ifndef PK_DIFF_INLINE
+#define PK_DIFF_INLINE 0
+#endif
+#if PK_DIFF_INLINE
+#define PK_DIFF_CALL __forceinline__
+#else
+#define PK_DIFF_CALL __noinline__
+#endif
+
 template <bool DERIV>
-__device__ __forceinline__ void shade_diff(const SceneDev& sc, const EnvDev& env, const DiffParams& P, float theta,
+__device__ PK_DIFF_CALL void shade_diff(const SceneDev& sc, const EnvDev& env, const DiffParams& P, float theta,
                                            int32_t samples, uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr,
                                            DiffShade& out) {
   const V3 zero = v3(0.0f, 0.0f, 0.0f);
@@ -292,6 +305,14 @@ struct DVert {
 __device__ __forceinline__ void set3(float* d, V3 v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; }
 __device__ __forceinline__ void set3(float* d, float x, float y, float z) { d[0] = x; d[1] = y; d[2] = z; }
 
+// trace.wgsl (any = false) or trace_shadow.wgsl (any = true) on the drop-in's records.
+__device__ PK_DIFF_CALL void diff_trace(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
+                                        uint32_t& bary, int (*sstack)[TRACE_THREADS], uint32_t* err) {
+  uint32_t nf = 0, nt = 0;
+  traverse_rt<false, TRACE_THREADS, STACK_SMEM>(any, sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf,
+                                                nt);
+}
+
 // One path of pixel (px, py) with camera.wgsl's sample index `samples`: the
 // loop of k_batch (closest hit, shading, the shadow ray, the next bounce while
 // fewer than depth closest-hit rays were traced).  acc += its contributions in
@@ -309,8 +330,8 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
   for (int bounce = 0; bounce < P.depth; bounce++) {
     float t;
     int idx;
-    uint32_t bary, nf = 0, nt = 0;
-    traverse<false, false>(sc, o4.x, o4.y, o4.z, d4.x, d4.y, d4.z, t, idx, bary, sstack, err, nf, nt);
+    uint32_t bary;
+    diff_trace(false, sc, o4, d4, t, idx, bary, sstack, err);
     nrays++;
     if (idx < 0) {
       int tex;
@@ -340,8 +361,8 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
     if (s.es) {
       float ts;
       int is;
-      uint32_t sb, nf2 = 0, nt2 = 0;
-      traverse<true, false>(sc, s.so.x, s.so.y, s.so.z, s.sd.x, s.sd.y, s.sd.z, ts, is, sb, sstack, err, nf2, nt2);
+      uint32_t sb;
+      diff_trace(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
       nrays++;
       if (is < 0) {
         se = diff_env(P, theta, v3(s.sd.x, s.sd.y, s.sd.z), stex);
