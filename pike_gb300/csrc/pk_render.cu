@@ -164,10 +164,7 @@ constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 #define PK_LEAF_BUDGET 0
 #endif
 constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
-#ifndef PK_ANY_LEAF_FIRST
-#define PK_ANY_LEAF_FIRST 0
-#endif
-constexpr bool ANY_LEAF_FIRST = PK_ANY_LEAF_FIRST;
+
 constexpr int ANY_BUDGET = PK_ANY_BUDGET;
 
 // Box test of the exact binary records: like box_hit, with the far distance
@@ -341,11 +338,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (lok && rok) {
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
-        // any hit only needs some hit: with PK_ANY_LEAF_FIRST a leaf child is
-        // visited before an inner one (the counting variant keeps the order)
-        if (ANY_LEAF_FIRST && ANY && !COUNT && !EXACT && farc < 0 && nearc >= 0) {
-          const int t = nearc; nearc = farc; farc = t;
-        }
         if (sp < STACK_SMEM) sstack[sp][tid] = farc;
         else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
         else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
@@ -783,6 +775,8 @@ __device__ __forceinline__ bool shade_one(const SceneDev& sc, const EnvDev& env,
   return emitted;
 }
 
+// (measured again with the warp-wide look-back, 1080p: 10 blocks 3342-3359
+// Mrays/s, 12: 3394-3396, 14: 3392-3407, 16: 3384-3392)
 #ifndef PK_SHADE_BLOCKS
 #define PK_SHADE_BLOCKS 12
 #endif
