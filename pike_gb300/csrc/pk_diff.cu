@@ -136,21 +136,8 @@ struct DiffShade {
   int mat;
 };
 
-// Out of line by default (PK_DIFF_INLINE=0): the path loop of the forward
-// and adjoint kernels with the shading and both traversals inlined overflows
-// the instruction cache (ncu: instruction-fetch stalls were the largest
-// stall reason), as in the batch kernel.
-#ifndef PK_DIFF_INLINE
-#define PK_DIFF_INLINE 0
-#endif
-#if PK_DIFF_INLINE
-#define PK_DIFF_CALL __forceinline__
-#else
-#define PK_DIFF_CALL __noinline__
-#endif
-
 template <bool DERIV>
-__device__ PK_DIFF_CALL void shade_diff(const SceneDev& sc, const EnvDev& env, const DiffParams& P, float theta,
+__device__ __forceinline__ void shade_diff(const SceneDev& sc, const EnvDev& env, const DiffParams& P, float theta,
                                            int32_t samples, uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr,
                                            DiffShade& out) {
   const V3 zero = v3(0.0f, 0.0f, 0.0f);
@@ -306,11 +293,25 @@ __device__ __forceinline__ void set3(float* d, V3 v) { d[0] = v.x; d[1] = v.y; d
 __device__ __forceinline__ void set3(float* d, float x, float y, float z) { d[0] = x; d[1] = y; d[2] = z; }
 
 // trace.wgsl (any = false) or trace_shadow.wgsl (any = true) on the drop-in's records.
-__device__ PK_DIFF_CALL void diff_trace(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
-                                        uint32_t& bary, int (*sstack)[TRACE_THREADS], uint32_t* err) {
+__device__ __forceinline__ void diff_trace(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
+                                           uint32_t& bary, int (*sstack)[TRACE_THREADS], uint32_t* err) {
   uint32_t nf = 0, nt = 0;
   traverse_rt<false, TRACE_THREADS, STACK_SMEM>(any, sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf,
                                                 nt);
+}
+// The adjoint calls the shading and the traversal out of line: with them
+// inlined its path loop overflows the instruction cache (ncu: instruction
+// fetch was its largest stall).  Measured on the differentiation workload:
+// adjoint 648 against 587 Mrays/s inlined; the forward kernel is faster
+// inlined (783 against 738), so it keeps them inline.
+__device__ __noinline__ void diff_trace_out(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
+                                            uint32_t& bary, int (*sstack)[TRACE_THREADS], uint32_t* err) {
+  diff_trace(any, sc, o, d, t, idx, bary, sstack, err);
+}
+__device__ __noinline__ void shade_diff_out(const SceneDev& sc, const EnvDev& env, const DiffParams& P, float theta,
+                                            int32_t samples, uint32_t r, float4 o4, float4 d4, float4 t4, uint4 hr,
+                                            DiffShade& out) {
+  shade_diff<true>(sc, env, P, theta, samples, r, o4, d4, t4, hr, out);
 }
 
 // One path of pixel (px, py) with camera.wgsl's sample index `samples`: the
@@ -331,7 +332,8 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
     float t;
     int idx;
     uint32_t bary;
-    diff_trace(false, sc, o4, d4, t, idx, bary, sstack, err);
+    if (REC) diff_trace_out(false, sc, o4, d4, t, idx, bary, sstack, err);
+    else diff_trace(false, sc, o4, d4, t, idx, bary, sstack, err);
     nrays++;
     if (idx < 0) {
       int tex;
@@ -352,8 +354,9 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
       return;
     }
     DiffShade s;
-    shade_diff<REC>(sc, env, P, theta, samples, (uint32_t)bounce, o4, d4, t4,
-                    make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u), s);
+    const uint4 hr = make_uint4(__float_as_uint(t), (uint32_t)idx, bary, 0u);
+    if (REC) shade_diff_out(sc, env, P, theta, samples, (uint32_t)bounce, o4, d4, t4, hr, s);
+    else shade_diff<false>(sc, env, P, theta, samples, (uint32_t)bounce, o4, d4, t4, hr, s);
     float cr = 0.0f, cg = 0.0f, cb = 0.0f;
     if (s.emitted) { cr = s.em.x; cg = s.em.y; cb = s.em.z; }
     int stex = -1;
@@ -362,7 +365,8 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
       float ts;
       int is;
       uint32_t sb;
-      diff_trace(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
+      if (REC) diff_trace_out(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
+      else diff_trace(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
       nrays++;
       if (is < 0) {
         se = diff_env(P, theta, v3(s.sd.x, s.sd.y, s.sd.z), stex);
