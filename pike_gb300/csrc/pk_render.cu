@@ -126,6 +126,16 @@ __global__ void __launch_bounds__(TRACE_THREADS) k_trace(SceneDev sc, EnvDev env
 #endif
 constexpr int REFILL_MIN = PK_REFILL_MIN;
 
+// Traversal stack entries per lane kept in shared memory (the rest of the 64
+// in local memory).  Shared memory and L1 share one array per SM, so the
+// shared stack of 10 resident blocks (DYN_SMEM * 128 * 4 bytes each) is taken
+// from the cache that serves the node records.
+#ifndef PK_DYN_SMEM
+#define PK_DYN_SMEM 32
+#endif
+constexpr int DYN_SMEM = PK_DYN_SMEM;
+constexpr int DYN_LOCAL = 64 - DYN_SMEM;
+
 // Any-hit rays report only whether some triangle is hit, and the set of leaves
 // a ray can reach (every box on the path from the root hit) does not depend
 // on the visiting order, so the production any-hit kernel may postpone leaves
@@ -200,8 +210,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
                                                               float4* __restrict__ color, uint32_t npix,
                                                               uint32_t* __restrict__ ticket, int defer) {
-  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
-  int lstack[STACK_LOCAL];
+  __shared__ int sstack[DYN_SMEM][TRACE_THREADS];
+  int lstack[DYN_LOCAL];
   const uint32_t n = *countp;
   const int lane = threadIdx.x & 31;
   const int tid = threadIdx.x;
@@ -266,8 +276,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
         if (lok && rok) {
           int nearc, farc;
           if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
-          if (sp < STACK_SMEM) sstack[sp][tid] = farc;
-          else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+          if (sp < DYN_SMEM) sstack[sp][tid] = farc;
+          else if (sp < DYN_SMEM + DYN_LOCAL) lstack[sp - DYN_SMEM] = farc;
           else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
           ++sp;
           cur = nearc;
@@ -279,12 +289,12 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
           cur = SPEC_DONE;
         } else {
           --sp;
-          cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+          cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM];
         }
         if (cur < 0 && pl == 0) {
           pl = cur;
           if (sp == 0) cur = SPEC_DONE;
-          else { --sp; cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM]; }
+          else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
         }
         if (__all_sync(__activemask(), pl != 0)) break;
       }
@@ -292,7 +302,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (!fin && pl == 0 && cur < 0) {
         pl = cur;
         if (sp == 0) cur = SPEC_DONE;
-        else { --sp; cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM]; }
+        else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
       }
       while (!fin && pl < 0) {
         const uint32_t word = (uint32_t)pl & 0x7fffffffu;
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
         if (cur < 0) {
           pl = cur;
           if (sp == 0) cur = SPEC_DONE;
-          else { --sp; cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM]; }
+          else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
         }
       }
       if (!fin && pl == 0 && cur == SPEC_DONE) fin = true;
@@ -338,8 +348,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (lok && rok) {
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
-        if (sp < STACK_SMEM) sstack[sp][tid] = farc;
-        else if (sp < STACK_SMEM + STACK_LOCAL) lstack[sp - STACK_SMEM] = farc;
+        if (sp < DYN_SMEM) sstack[sp][tid] = farc;
+        else if (sp < DYN_SMEM + DYN_LOCAL) lstack[sp - DYN_SMEM] = farc;
         else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
         ++sp;
         cur = nearc;
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (rok) { cur = cr; continue; }
       if (sp == 0) { fin = true; break; }
       --sp;
-      cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+      cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM];
     }
     // leaves (at most LEAF_BUDGET before the warp meets, when not 0)
     int lbudget = LEAF_BUDGET;
@@ -386,7 +396,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       if (ANY && best_i != -1) { fin = true; break; }
       if (sp == 0) { fin = true; break; }
       --sp;
-      cur = sp < STACK_SMEM ? sstack[sp][tid] : lstack[sp - STACK_SMEM];
+      cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM];
     }
     if (fin) {
       const bool hit = best_i != -1;
