@@ -16,8 +16,8 @@ resident in HBM; `e2e` runs the same steps through the C ABI with the
 per-step render state and camera (56 bytes, handed to the device as launch
 parameters of the frame's state kernel) and every frame's 8-bit image read
 back asynchronously into pinned host memory, timed by the host clock from the
-first call to the return of the final pk_sync.  Frames render four at a time
-in flight (pk_set_frames_in_flight), bit-identical to one at a time.  The
+first call to the return of the final pk_sync.  Frames render eight at a
+time in flight (pk_set_frames_in_flight), bit-identical to one at a time.  The
 roofline line adds an L2 fraction against an L2 read peak measured in the
 same run (pk_probe_read_bandwidth).  The `forms` block includes the
 8,388,608-triangle soup (the precision workload) unless --no-precision.
