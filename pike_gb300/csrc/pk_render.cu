@@ -131,7 +131,7 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 // shared stack of 10 resident blocks (DYN_SMEM * 128 * 4 bytes each) is taken
 // from the cache that serves the node records.
 #ifndef PK_DYN_SMEM
-#define PK_DYN_SMEM 32
+#define PK_DYN_SMEM 8
 #endif
 constexpr int DYN_SMEM = PK_DYN_SMEM;
 constexpr int DYN_LOCAL = 64 - DYN_SMEM;
@@ -439,8 +439,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
-constexpr int CW_STACK_SMEM = 16;   // group entries per thread in shared memory
-constexpr int CW_STACK_LOCAL = 16;  // overflow entries in local memory
+#ifndef PK_CW_SMEM
+#define PK_CW_SMEM 16
+#endif
+constexpr int CW_STACK_SMEM = PK_CW_SMEM;       // group entries per thread in shared memory
+constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local memory
 #ifndef PK_CW_POSTPONE
 #define PK_CW_POSTPONE 0
 #endif
