@@ -419,7 +419,7 @@ int pk_batch_destroy(pk_batch* batch);
 const char* pk_batch_last_error(pk_batch* batch);
 int pk_batch_set_requests(pk_batch* batch, const pk_batch_request* requests, uint32_t n);
 /* Threads per block (64/128/256), shared-memory traversal stack entries
- * (16/32) and queue chunk (a warp claims chunk*32 paths per atomic, 1..64). */
+ * (8/16/32) and queue chunk (a warp claims chunk*32 paths per atomic, 1..64). */
 int pk_batch_set_config(pk_batch* batch, int block, int stack, int chunk);
 int pk_batch_get_config(pk_batch* batch, int* block, int* stack, int* chunk);
 /* Times every supported configuration on the first sample_paths paths of the

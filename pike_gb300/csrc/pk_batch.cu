@@ -226,7 +226,7 @@ int pk_batch_autotune(pk_batch* b, uint64_t sample_paths, float* best_ms) {
   return bguard(b, [&]() {
     if (b->reqs.empty()) return bfail(b, PK_ERR_STATE, "set requests first");
     const unsigned long long total = sample_paths ? std::min<unsigned long long>(sample_paths, b->total) : b->total;
-    const int blocks[3] = {64, 128, 256}, stacks[2] = {16, 32}, chunks[3] = {1, 4, 16};
+    const int blocks[3] = {64, 128, 256}, stacks[3] = {8, 16, 32}, chunks[3] = {1, 4, 16};
     float best = 1e30f;
     BatchConfig pick = b->cfg;
     for (int bl : blocks)

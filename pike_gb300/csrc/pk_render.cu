@@ -1186,7 +1186,7 @@ __global__ void __launch_bounds__(BLOCK, 1280 / BLOCK) k_batch(const BatchScene*
 
 __global__ void k_batch_next_frame(uint32_t* frame) { *frame += 1u; }
 
-#define PK_BATCH_CONFIGS(X) X(64, 16) X(64, 32) X(128, 16) X(128, 32) X(256, 16) X(256, 32)
+#define PK_BATCH_CONFIGS(X) X(64, 8) X(64, 16) X(64, 32) X(128, 8) X(128, 16) X(128, 32) X(256, 8) X(256, 16) X(256, 32)
 
 bool batch_config_ok(const BatchConfig& c) {
 #define PK_B_OK(B, S) if (c.block == B && c.stack == S) return c.chunk >= 1 && c.chunk <= 64;

@@ -77,7 +77,7 @@ def test_configurations_agree(scenes):
     batch = Batch(ctxs)
     batch.set_requests(reqs)
     ref = None
-    for cfg in [(64, 16, 1), (128, 32, 4), (256, 32, 16), (256, 16, 64)]:
+    for cfg in [(64, 16, 1), (128, 32, 4), (256, 32, 16), (256, 16, 64), (128, 8, 4)]:
         batch.set_config(*cfg)
         batch.reset()
         batch.render(1)
@@ -87,7 +87,7 @@ def test_configurations_agree(scenes):
         for x, y in zip(imgs, ref):
             assert np.allclose(x, y, rtol=1e-5, atol=1e-6), cfg
     best = batch.autotune(0)
-    assert best > 0 and batch.config() in {(b, s, c) for b in (64, 128, 256) for s in (16, 32) for c in (1, 4, 16)}
+    assert best > 0 and batch.config() in {(b, s, c) for b in (64, 128, 256) for s in (8, 16, 32) for c in (1, 4, 16)}
 
 
 def test_bad_requests_are_rejected(scenes):
