@@ -61,6 +61,9 @@ namespace pk {
 
 constexpr int DIFF_THREADS = 128;  // = TRACE_THREADS (traversal stack layout)
 constexpr int DIFF_MAX_DEPTH = 8;
+// traversal stack entries per lane in shared memory (the rest of 64 in local
+// memory): a small shared stack leaves more of the SM's L1 to node records
+constexpr int DIFF_SSTACK = 8;
 // 8 resident blocks per SM (64 registers, some spilled) for both kernels:
 // forward 795 against 764 Mrays/s unconstrained, adjoint 592 against 531
 // (the differentiation workload, same call; 6 blocks: 788 and 557).
@@ -296,7 +299,7 @@ __device__ __forceinline__ void set3(float* d, float x, float y, float z) { d[0]
 __device__ __forceinline__ void diff_trace(bool any, const SceneDev& sc, float4 o, float4 d, float& t, int& idx,
                                            uint32_t& bary, int (*sstack)[TRACE_THREADS], uint32_t* err) {
   uint32_t nf = 0, nt = 0;
-  traverse_rt<false, TRACE_THREADS, STACK_SMEM>(any, sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf,
+  traverse_rt<false, TRACE_THREADS, DIFF_SSTACK>(any, sc, o.x, o.y, o.z, d.x, d.y, d.z, t, idx, bary, sstack, err, nf,
                                                 nt);
 }
 // The adjoint calls the shading and the traversal out of line: with them
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(DIFF_THREADS, PK_DIFF_FWD_BLOCKS) k_diff_forwa
                                                                float theta, uint32_t W, uint32_t H,
                                                                float4* __restrict__ image, uint32_t* err,
                                                                unsigned long long* rays) {
-  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+  __shared__ int sstack[DIFF_SSTACK][TRACE_THREADS];
   const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= W * H) return;
   const uint32_t px = pix % W, py = pix / W;
@@ -445,7 +448,7 @@ __global__ void __launch_bounds__(DIFF_THREADS, PK_DIFF_ADJ_BLOCKS) k_diff_adjoi
                                                                double* __restrict__ g_rough,
                                                                double* __restrict__ g_env, uint32_t* err,
                                                                unsigned long long* rays) {
-  __shared__ int sstack[STACK_SMEM][TRACE_THREADS];
+  __shared__ int sstack[DIFF_SSTACK][TRACE_THREADS];
   extern __shared__ float spart[];  // n_mats x 4: albedo rgb, roughness
   for (uint32_t i = threadIdx.x; i < 4 * P.n_mats; i += blockDim.x) spart[i] = 0.0f;
   __syncthreads();

@@ -131,7 +131,9 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 // shared stack of 10 resident blocks (DYN_SMEM * 128 * 4 bytes each) is taken
 // from the cache that serves the node records.
 // (1080p: 32 entries 3425-3457 Mrays/s, 24: 3447-3449, 16: 3532-3562, 12:
-// 3541-3546, 8: 3552-3572, 4: 3511-3523)
+// 3541-3546, 8: 3552-3572, 4: 3511-3523).  The driver's own carveout for the
+// resulting shared memory was kept: asking for 25% gave 3547-3556, 50%
+// 3495-3514, and 0% (all L1) cut the resident blocks: 975.
 #ifndef PK_DYN_SMEM
 #define PK_DYN_SMEM 8
 #endif
@@ -1220,24 +1222,9 @@ void launch_batch(cudaStream_t s, const BatchConfig& c, unsigned grid, const Bat
 
 void launch_batch_next_frame(cudaStream_t s, uint32_t* frame) { k_batch_next_frame<<<1, 1, 0, s>>>(frame); }
 
-// PK_TRACE_CARVEOUT >= 0: the traversal kernels' preferred shared-memory
-// carveout (percent of the SM's shared memory + L1 array); the rest is L1.
-#ifndef PK_TRACE_CARVEOUT
-#define PK_TRACE_CARVEOUT -1
-#endif
-template <class K>
-static void set_carveout(K kernel) {
-  if (PK_TRACE_CARVEOUT >= 0)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, PK_TRACE_CARVEOUT);
-}
-
 void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact, unsigned* shade,
                   unsigned* trace_wide) {
   int t = 0, c = 0, s = 0, w = 0;
-  set_carveout(k_trace_dyn<false, true, false, false>);
-  set_carveout(k_trace_dyn<true, true, false, false>);
-  set_carveout(k_trace_dyn<false, false, false, false>);
-  set_carveout(k_trace_dyn<true, false, false, false>);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&t, k_trace_dyn<false, true, false, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&w, k_trace_cw<false, true, false>, TRACE_THREADS, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_compact<0, true>, COMPACT_THREADS, 0);

@@ -70,7 +70,7 @@ __device__ __forceinline__ bool mt_test(const SceneDev& sc, int idx, float ox, f
 
 constexpr int TRACE_THREADS = 128;
 constexpr int STACK_SMEM = 32;   // per-thread entries kept in shared memory
-constexpr int STACK_LOCAL = 32;  // overflow entries in local memory (total depth 64)
+// (traverse_rt keeps the remaining 64 - SSTACK entries in local memory)
 
 __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, float ox, float oy, float oz, float ix,
                                                float iy, float iz, float& lh, float& rh, int& cl, int& cr) {
@@ -95,7 +95,7 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
 }
 
 // BLOCK threads per block share `sstack` (SSTACK entries per thread in shared
-// memory, STACK_LOCAL more in local memory).  ANY: any hit (trace_shadow.wgsl)
+// memory, 64 - SSTACK more in local memory).  ANY: any hit (trace_shadow.wgsl)
 // rather than closest hit; a constant at every inlined call site, a run-time
 // value where one out-of-line copy serves both.
 template <bool COUNT, int BLOCK, int SSTACK>
@@ -105,7 +105,8 @@ __device__ __forceinline__ void traverse_rt(const bool ANY, const SceneDev& sc, 
                                             uint32_t& nfetch, uint32_t& ntest) {
   const float eps = ANY ? 1e-7f : 1e-8f;
   const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-  int lstack[STACK_LOCAL];
+  constexpr int LOCAL = 64 - SSTACK;  // 64 entries in all
+  int lstack[LOCAL];
   const int tid = threadIdx.x;
   int sp = 0;
   int cur = sc.root;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void traverse_rt(const bool ANY, const SceneDev& sc, 
         int nearc, farc;
         if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
         if (sp < SSTACK) sstack[sp][tid] = farc;
-        else if (sp < SSTACK + STACK_LOCAL) lstack[sp - SSTACK] = farc;
+        else if (sp < SSTACK + LOCAL) lstack[sp - SSTACK] = farc;
         else { atomicOr(err, ERR_STACK); break; }
         ++sp;
         cur = nearc;
