@@ -630,6 +630,9 @@ def adjoint_form(args, local: int):
     # surfaces, env texels the camera or a bounce sees: non-zero gradient at
     # the start)
     seen_m = (ga[:n_free].abs().sum(-1) > 0)
+    # the 64 materials the image constrains most (largest albedo gradient at the start)
+    top_m = torch.zeros_like(seen_m)
+    top_m[torch.argsort(ga[:n_free].abs().sum(-1), descending=True)[:64]] = True
     seen_e = (ge.abs().sum(-1) > 0)
     rel_env = lambda E: float(((E - env).abs().sum(-1)[seen_e] / env.sum(-1)[seen_e]).mean())
     return {"workload": "icosphere8+openbox 512x512, 16 spp, depth 4; 256 albedos (RGB), 256 roughness, "
@@ -654,9 +657,13 @@ def adjoint_form(args, local: int):
                 "roughness_mae_start": float((r0[:n_free] - rough[:n_free]).abs()[seen_m].mean()),
                 "roughness_mae_end": float((r[:n_free] - rough[:n_free]).abs()[seen_m].mean()),
                 "env_rel_l1_start": rel_env(e0), "env_rel_l1_end": rel_env(e),
+                "albedo_mae_top64_start": float((a0[:n_free] - albedo[:n_free]).abs()[top_m].mean()),
+                "albedo_mae_top64_end": float((a[:n_free] - albedo[:n_free]).abs()[top_m].mean()),
                 "env_known": {"loss_eval_end": eval_loss(a_k, r_k, env),
                               "albedo_mae_end": float((a_k[:n_free] - albedo[:n_free]).abs()[seen_m].mean()),
-                              "roughness_mae_end": float((r_k[:n_free] - rough[:n_free]).abs()[seen_m].mean())}}}
+                              "albedo_mae_top64_end": float((a_k[:n_free] - albedo[:n_free]).abs()[top_m].mean()),
+                              "roughness_mae_end": float((r_k[:n_free] - rough[:n_free]).abs()[seen_m].mean()),
+                              "roughness_mae_top64_end": float((r_k[:n_free] - rough[:n_free]).abs()[top_m].mean())}}}
 
 
 def batch_form(args, local: int):
