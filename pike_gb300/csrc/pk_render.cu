@@ -705,7 +705,10 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
   }
 }
 
-constexpr int SHADE_THREADS = 128;
+#ifndef PK_SHADE_THREADS
+#define PK_SHADE_THREADS 128
+#endif
+constexpr int SHADE_THREADS = PK_SHADE_THREADS;
 
 // main (:407-483).  Tiles of SHADE_THREADS hits are claimed in order; bounce
 // and shadow rays are written at their stable ranks found by a block scan plus
