@@ -452,6 +452,11 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #ifndef PK_CW_POSTPONE
 #define PK_CW_POSTPONE 0
 #endif
+// Idle lanes that make a warp claim new rays (REFILL_MIN of the binary
+// traversal).
+#ifndef PK_CW_REFILL
+#define PK_CW_REFILL REFILL_MIN
+#endif
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
@@ -503,7 +508,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
     const uint32_t busy = __ballot_sync(0xffffffffu, have);
-    if (idle && (__popc(idle) >= REFILL_MIN || busy == 0u)) {
+    if (idle && (__popc(idle) >= PK_CW_REFILL || busy == 0u)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(ticket, (uint32_t)__popc(idle));
@@ -705,18 +710,22 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
   }
 }
 
+// k_shade: shade_hit.wgsl main (:407-483).  Tiles of SHADE_THREADS hits are
+// claimed in order; bounce and shadow rays are written at their stable ranks
+// found by a block scan plus decoupled look-back, so slot order equals the
+// serial order of the reference.  Occupancy is held at 1536 threads per SM
+// (<= 40 registers): more shading warps in flight to cover the attribute,
+// texel and env gathers; some registers spill to L1.  Block size at that
+// occupancy, 1080p frame, two runs each in one call: 64 threads x 24 blocks
+// 3334-3337 Mrays/s, 128 x 12 3519-3526, 256 x 6 3690-3692, 512 x 3
+// 3706-3718, 1024 x 1 3514-3551; fewer resident threads at 256 (5 blocks
+// 3665-3676, 4 blocks 3638-3639).  Larger tiles mean fewer look-back steps
+// per hit.
 #ifndef PK_SHADE_THREADS
-#define PK_SHADE_THREADS 128
+#define PK_SHADE_THREADS 512
 #endif
 constexpr int SHADE_THREADS = PK_SHADE_THREADS;
 
-// main (:407-483).  Tiles of SHADE_THREADS hits are claimed in order; bounce
-// and shadow rays are written at their stable ranks found by a block scan plus
-// decoupled look-back, so slot order equals the serial order of the reference.
-// 12 resident blocks per SM (<= 40 registers): more shading warps in flight to
-// cover the attribute/texel/env gathers; some registers spill to L1 (1080p
-// frame, paired runs: 3007-3013 Mrays/s at 12 blocks, 2943-2946 at 10, 2926
-// at 8, 2990 at 14, 2992 at 16).
 // shade_hit.wgsl:407-483 for one hit: the hit record of slot `r` (its
 // position in the hit list, which seeds the RNG) on ray (o4, d4, t4).
 // Returns whether the surface emits (emission contribution in em); eb/es with
@@ -796,10 +805,10 @@ __device__ __forceinline__ bool shade_one(const SceneDev& sc, const EnvDev& env,
   return emitted;
 }
 
-// (measured again with the warp-wide look-back, 1080p: 10 blocks 3342-3359
-// Mrays/s, 12: 3394-3396, 14: 3392-3407, 16: 3384-3392)
+// Resident blocks per SM (at 128 threads, warp-wide look-back, 1080p: 10
+// blocks 3342-3359 Mrays/s, 12: 3394-3396, 14: 3392-3407, 16: 3384-3392).
 #ifndef PK_SHADE_BLOCKS
-#define PK_SHADE_BLOCKS 12
+#define PK_SHADE_BLOCKS (1536 / SHADE_THREADS)
 #endif
 __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                           const uint32_t* __restrict__ hit_list,

