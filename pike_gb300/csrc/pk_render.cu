@@ -439,7 +439,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
 // p = 8: 2569, p = 0: 2939), so it is off by default.  Lanes take new rays as
 // in k_trace_dyn.  Unlike the binary traversal, letting a lane visit several
 // nodes in a row before the warp meets again did not pay (1080p: one visit
-// 3102-3108 Mrays/s, up to two 2893-2900, up to four 1753-1767).
+// 3102-3108 Mrays/s, up to two 2893-2900, up to four 1753-1767), and the
+// refill threshold of the binary traversal (16 idle lanes) is also best here
+// (1080p: 4 lanes 3275-3285, 8: 3305-3312, 16: 3357-3360, 24: 3315).
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
@@ -452,11 +454,7 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #ifndef PK_CW_POSTPONE
 #define PK_CW_POSTPONE 0
 #endif
-// Idle lanes that make a warp claim new rays (REFILL_MIN of the binary
-// traversal).
-#ifndef PK_CW_REFILL
-#define PK_CW_REFILL REFILL_MIN
-#endif
+
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
@@ -508,7 +506,7 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
     const uint32_t busy = __ballot_sync(0xffffffffu, have);
-    if (idle && (__popc(idle) >= PK_CW_REFILL || busy == 0u)) {
+    if (idle && (__popc(idle) >= REFILL_MIN || busy == 0u)) {
       const int leader = __ffs(idle) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(ticket, (uint32_t)__popc(idle));

@@ -17,7 +17,9 @@ __device__ __forceinline__ float box_hit(float xa, float xb, float ya, float yb,
   const float t1y = (ya - oy) * iy, t2y = (yb - oy) * iy;
   const float t1z = (za - oz) * iz, t2z = (zb - oz) * iz;
   // fminf/fmaxf agree with minNum/maxNum except for the sign of a zero
-  // result, which only ever feeds comparisons here.
+  // result, which only ever feeds comparisons here.  (Three-input min/max
+  // for the outer reductions measured no faster: 3709-3748 against
+  // 3740-3745 Mrays/s.)
   const float tmax = fminf(fminf(fmaxf(t1x, t2x), fmaxf(t1y, t2y)), fmaxf(t1z, t2z));
   const float tmin = fmaxf(fmaxf(fminf(t1x, t2x), fminf(t1y, t2y)), fminf(t1z, t2z));
   return (tmax >= tmin && tmax > 0.0f) ? tmin : MAX_T;
