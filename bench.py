@@ -647,7 +647,7 @@ def adjoint_form(args, local: int):
             "inverse_rendering": {
                 "steps": steps, "seconds": opt_s,
                 "objective": "L2 to a 128-spp target; fresh 16-spp samples every step, the gradient from an independent "
-                             "16-spp replay (Adam, lr 0.02); loss_eval = L2 of a 128-spp render",
+                             "16-spp replay (Adam, lr 0.02 cosine-decayed to 4e-4); loss_eval = L2 of a 128-spp render",
                 "loss_first": hist[0], "loss_last": hist[-1],
                 "loss_eval_start": eval_loss(a0, r0, e0), "loss_eval_end": eval_loss(a, r, e),
                 "loss_eval_at_hidden_params": eval_loss(albedo, rough, env),
@@ -659,6 +659,8 @@ def adjoint_form(args, local: int):
                 "env_rel_l1_start": rel_env(e0), "env_rel_l1_end": rel_env(e),
                 "albedo_mae_top64_start": float((a0[:n_free] - albedo[:n_free]).abs()[top_m].mean()),
                 "albedo_mae_top64_end": float((a[:n_free] - albedo[:n_free]).abs()[top_m].mean()),
+                "roughness_mae_top64_start": float((r0[:n_free] - rough[:n_free]).abs()[top_m].mean()),
+                "roughness_mae_top64_end": float((r[:n_free] - rough[:n_free]).abs()[top_m].mean()),
                 "env_known": {"loss_eval_end": eval_loss(a_k, r_k, env),
                               "albedo_mae_end": float((a_k[:n_free] - albedo[:n_free]).abs()[seen_m].mean()),
                               "albedo_mae_top64_end": float((a_k[:n_free] - albedo[:n_free]).abs()[top_m].mean()),

@@ -174,20 +174,24 @@ def l2_loss(image, target):
 
 def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 200, lr: float = 0.02,
                    n_free: int | None = None, seed_per_step: bool = True, seed: int = 0, env_floor: float = 1e-3,
-                   optimise_env: bool = True):
+                   optimise_env: bool = True, lr_final: float | None = None):
     """Adam on (albedo, roughness, env) towards the target image; materials at
     index >= n_free stay fixed.  With seed_per_step, step k renders with seed
     2k and differentiates with the independent samples of seed 2k + 1
     (decorrelated: unbiased gradients of the expected image's L2 error);
     otherwise every step renders and differentiates `seed` (common random
     numbers: a deterministic objective).  With optimise_env=False the map
-    stays as given and only the materials move.  Returns the parameters and
-    the loss history."""
+    stays as given and only the materials move.  The step size follows a
+    cosine from lr to lr_final (default lr / 50), which lets the parameters
+    settle under Monte Carlo gradient noise.  Returns the parameters and the
+    loss history."""
     import torch
     a = albedo.clone().requires_grad_(True)
     r = rough.clone().requires_grad_(True)
     e = env.clone().requires_grad_(optimise_env)
     opt = torch.optim.Adam([a, r, e] if optimise_env else [a, r], lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, T_max=max(steps, 1),
+                                                       eta_min=lr / 50 if lr_final is None else lr_final)
     keep = None
     if n_free is not None and n_free < a.shape[0]:
         keep = (a.detach()[n_free:].clone(), r.detach()[n_free:].clone())
@@ -201,6 +205,7 @@ def inverse_render(scene: DiffScene, target, albedo, rough, env, steps: int = 20
         loss = l2_loss(img, target)
         loss.backward()
         opt.step()
+        sched.step()
         with torch.no_grad():
             a.clamp_(0.0, 1.0)
             r.clamp_(0.05, 1.0)
