@@ -604,7 +604,10 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
 //           contributions of misses parked in miss_rec when given)
 //   MODE 1: any-hit flags     -> unoccluded shadow rays appended to the miss queue
 // =====================================================================
-constexpr int COMPACT_THREADS = 256;
+#ifndef PK_COMPACT_THREADS
+#define PK_COMPACT_THREADS 256
+#endif
+constexpr int COMPACT_THREADS = PK_COMPACT_THREADS;
 // The compaction and shade kernels take their tile's prefix with a whole warp
 // (lookback2_warp) rather than one thread (lookback2).
 #ifndef PK_LOOKBACK_WARP
