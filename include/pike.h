@@ -272,8 +272,10 @@ int pk_set_accumulation(pk_ctx* ctx, int mode);
 /* Environment light sampling of the shade pass: PK_ENV_HISTOGRAM is
  * env_sampler.js's equal-mass luminance histogram (env_sampler.js:74-157,
  * sampleEnv shade_hit.wgsl:213-227; the default, bit-exact with the
- * reference); PK_ENV_ALIAS draws texels from a Walker/Vose alias table with
- * probability proportional to their radiance, normalised in FP64 (the
+ * reference); PK_ENV_ALIAS draws texels from an alias table (Walker) with
+ * probability proportional to their radiance, built on the GPU: the total
+ * and the normalisation in FP64, then the weights in fixed point and the
+ * sweep of Huebschle-Schneider & Sanders from exact integer prefix sums (the
  * precision form; no reference counterpart).  The alias mode makes the same
  * two hash draws and uses its own pdf texture for envPdf (shade_hit.wgsl:
  * 202-210), so MIS stays consistent.  pk_env_alias_download returns the

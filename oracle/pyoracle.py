@@ -233,6 +233,85 @@ class EnvF32:
             self._h = None
 
 
+def env_alias(rgbe: np.ndarray):
+    """PK_ENV_ALIAS's table restated in numpy (the precision form; no
+    reference counterpart): the radiance of env_sampler.js:43-48 in FP64,
+    its total summed in the GPU builder's grouping (blocks of 1024 texels:
+    four strided values per thread, a shuffle tree per warp, the eight warp
+    sums in order; then 1024 strided partial sums and a halving tree), the
+    weights q = rint(radiance * n 2^f / total) with f = 61 - ceil(log2 n),
+    and the sweep of Huebschle-Schneider & Sanders ("Parallel Weighted
+    Random Sampling", 2022) evaluated from exact integer prefix sums.
+    Returns (table (n, 2) uint32 {keep threshold, alias}, pdf (n,) float32),
+    or None for a black map."""
+    c = np.asarray(rgbe, np.uint8).reshape(-1, 4)
+    cf = c.astype(np.float64)
+    r = np.ldexp(1.0, c[:, 3].astype(np.int64) - 128) * (0.2126 * cf[:, 0] + 0.7152 * cf[:, 1] + 0.0722 * cf[:, 2]) / 255.0
+    n = r.size
+    nb = (n + 1023) // 1024
+    R = np.zeros(nb * 1024)
+    R[:n] = r
+    R = R.reshape(nb, 4, 256)
+    v = ((R[:, 0] + R[:, 1]) + R[:, 2]) + R[:, 3]  # (nb, 256): thread sums (0.0 + x adds nothing)
+    v = v.reshape(nb, 8, 32)
+    for o in (16, 8, 4, 2, 1):  # __shfl_down_sync: a lane past the warp reads its own value
+        src = np.arange(32) + o
+        other = np.where(src < 32, v[:, :, np.minimum(src, 31)], v)
+        v = v + other
+    w = v[:, :, 0]
+    partial = np.zeros(nb)
+    for k in range(8):
+        partial = partial + w[:, k]
+    s = np.zeros(1024)
+    for t0 in range(0, nb, 1024):
+        chunk = partial[t0:t0 + 1024]
+        s[:chunk.size] = s[:chunk.size] + chunk
+    width = 512
+    while width > 0:
+        s[:width] = s[:width] + s[width:2 * width]
+        width //= 2
+    total = s[0]
+    if not (total > 0.0 and total <= 1.7e308):
+        return None
+    lg = 0
+    while (1 << lg) < n:
+        lg += 1
+    frac = 61 - lg
+    one = np.uint64(1 << frac)
+    q = np.rint(r * (np.ldexp(float(n), frac) / total)).astype(np.uint64)
+    light = q < one
+    L = np.nonzero(light)[0]
+    H = np.nonzero(~light)[0]
+    nl, nh = L.size, H.size
+    D = np.concatenate([np.zeros(1, np.uint64), np.cumsum(one - q[L], dtype=np.uint64)])  # D(0..nl)
+    hexc = q[H] - one
+    E = np.concatenate([np.zeros(1, np.uint64), np.cumsum(hexc, dtype=np.uint64)])[:nh]
+    Einc = E + hexc
+
+    def thr(p):
+        t = np.minimum(p >> np.uint64(frac - 32), np.uint64(0xfffffffe))
+        return np.where(p >= one, np.uint64(0xffffffff), t)
+
+    table = np.zeros((n, 2), np.uint64)
+    b = np.searchsorted(Einc, D[:nl], side="left")  # first heavy with E(b + 1) >= D(a)
+    ok = b < nh
+    table[L, 0] = np.where(ok, thr(q[L]), np.uint64(0xffffffff))
+    table[L, 1] = np.where(ok, H[np.minimum(b, max(nh - 1, 0))] if nh else L, L)
+    a = np.searchsorted(D, Einc, side="right")  # first a in [0, nl] with D(a) > E(b + 1)
+    conv = (a <= nl) & (np.arange(nh) + 1 < nh)
+    keep = one + hexc + E - D[np.minimum(a, nl)]
+    table[H, 0] = np.where(conv, thr(np.where(conv, keep, one)), np.uint64(0xffffffff))
+    table[H, 1] = np.where(conv, H[np.minimum(np.arange(nh) + 1, max(nh - 1, 0))], H)
+    table = table.astype(np.uint32)
+    k32 = np.where(table[:, 0] == 0xFFFFFFFF, np.uint64(1 << 32), table[:, 0].astype(np.uint64))
+    mass = k32.copy()
+    part = k32 < np.uint64(1 << 32)
+    np.add.at(mass, table[part, 1].astype(np.int64), np.uint64(1 << 32) - k32[part])
+    pdf = (mass.astype(np.float64) / 4294967296.0 * (1.0 / (2.0 * 3.141592653589793 * 3.141592653589793))).astype(
+        np.float32)
+    return table, pdf
+
+
 def camera_bytes(state: dict, width: int, height: int) -> bytes:
     """CameraStateStuct (structs.js:235-249) with dimsMask = W<<16 | H (camera_pass.js:118-125)."""
     dims = ((width & 0xFFFF) << 16) | (height & 0xFFFF)

@@ -535,18 +535,9 @@ int pk_bvh_download(pk_ctx* c, int32_t* nodes5, int32_t* tri4_leaf, float* verts
 // ---------------- env ----------------
 // The alias table of PK_ENV_ALIAS from the current environment's texels.
 static int build_alias(pk_ctx* c) {
-  const size_t N = (size_t)c->env_w * c->env_h;
-  std::vector<uint8_t> rgbe(4 * N);
-  check(cudaMemcpyAsync(rgbe.data(), c->rgbe.p, 4 * N, cudaMemcpyDeviceToHost, c->stream), "D2H");
-  check(cudaStreamSynchronize(c->stream), "sync");
-  std::vector<uint32_t> table2;
-  std::vector<float> pdf;
   std::string why;
-  if (!build_env_alias(rgbe.data(), c->env_w, c->env_h, table2, pdf, why))
+  if (build_env_alias_gpu(c->stream, c->rgbe.p, c->env_w, c->env_h, c->env_alias, c->alias_pdf, why))
     return fail(c, PK_ERR_ARG, "alias table: " + why);
-  upload(c->env_alias, reinterpret_cast<const uint2*>(table2.data()), N, c->stream);
-  upload(c->alias_pdf, pdf.data(), N, c->stream);
-  check(cudaStreamSynchronize(c->stream), "sync");
   c->alias_ready = true;
   c->invalidate_graph();
   return PK_OK;

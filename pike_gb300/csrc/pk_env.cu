@@ -109,6 +109,163 @@ __global__ void k_env_pdf(const uint32_t* __restrict__ order, uint32_t n, uint32
   coords[i] = make_int2((int)(t % w), (int)(t / w));
 }
 
+// ---------------- alias table (PK_ENV_ALIAS) -----------------------------
+// Radiance in FP64 as k_env_radiance computes it.
+__device__ __forceinline__ double texel_radiance(uchar4 c) {
+  return ldexp(1.0, (int)c.w - 128) * (0.2126 * (double)c.x + 0.7152 * (double)c.y + 0.0722 * (double)c.z) / 255.0;
+}
+
+constexpr int ALIAS_THREADS = 256;
+constexpr int ALIAS_PER_BLOCK = 4 * ALIAS_THREADS;
+
+// Per-block sums of the radiance (fixed grouping: the total is the same
+// double on every run).
+__global__ void __launch_bounds__(ALIAS_THREADS) k_alias_partial(const uchar4* __restrict__ rgbe, uint32_t n,
+                                                                double* __restrict__ partial) {
+  __shared__ double s_warp[ALIAS_THREADS / 32];
+  double v = 0.0;
+  const uint32_t base = blockIdx.x * ALIAS_PER_BLOCK + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const uint32_t i = base + k * ALIAS_THREADS;
+    if (i < n) v += texel_radiance(rgbe[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < ALIAS_THREADS / 32; k++) t += s_warp[k];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// The total (one block, fixed grouping) and the fixed-point scale
+// n * 2^frac / total; status 1 for a black or non-finite map.
+__global__ void k_alias_total(const double* __restrict__ partial, uint32_t m, uint32_t n, int frac,
+                              double* __restrict__ scale, uint32_t* __restrict__ status) {
+  __shared__ double s[1024];
+  double v = 0.0;
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) v += partial[i];
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double t = s[0];
+    const bool ok = t > 0.0 && t <= 1.7e308;
+    *status = ok ? 0u : 1u;
+    *scale = ok ? ldexp((double)n, frac) / t : 0.0;
+  }
+}
+
+// q_i = round(radiance_i * scale): the texel's weight in units of 2^-frac of
+// the mean; light (q < one) or heavy.
+__global__ void k_alias_weights(const uchar4* __restrict__ rgbe, uint32_t n, const double* __restrict__ scale,
+                                unsigned long long one, unsigned long long* __restrict__ q,
+                                uint32_t* __restrict__ light) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long w = __double2ull_rn(texel_radiance(rgbe[i]) * *scale);
+  q[i] = w;
+  light[i] = w < one ? 1u : 0u;
+}
+
+// Light texels in index order with their deficits (one - q), heavy texels
+// with their excesses (q - one).
+__global__ void k_alias_split(const unsigned long long* __restrict__ q, const uint32_t* __restrict__ light,
+                              const uint32_t* __restrict__ lrank, uint32_t n, unsigned long long one,
+                              uint32_t* __restrict__ lidx, unsigned long long* __restrict__ ldef,
+                              uint32_t* __restrict__ hidx, unsigned long long* __restrict__ hexc) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t r = lrank[i];
+  if (light[i]) {
+    lidx[r] = i;
+    ldef[r] = one - q[i];
+  } else {
+    hidx[i - r] = i;
+    hexc[i - r] = q[i] - one;
+  }
+}
+
+__device__ __forceinline__ uint32_t alias_threshold(unsigned long long prob, unsigned long long one, int frac) {
+  if (prob >= one) return 0xffffffffu;
+  const unsigned long long t = prob >> (frac - 32);
+  return t > 0xfffffffeull ? 0xfffffffeu : (uint32_t)t;
+}
+
+// The sweep of Huebschle-Schneider & Sanders ("Parallel Weighted Random
+// Sampling", 2022) without running it: with D(a) the deficits of the first a
+// lights and E(b) the excesses of the first b heavies (exclusive prefix
+// sums), heavy b serves light a iff E(b) < D(a) <= E(b + 1) (b = 0 needs only
+// the right side), and heavy b turns light at the first light a with
+// D(a) > E(b + 1), keeping q_b + E(b) - D(a) and taking heavy b + 1 as its
+// alias; a = n_light (D of all lights) stands for the end of the sweep, where
+// the heavy in hand still turns when its weight has fallen below one.
+// Lights the heavies cannot serve, the last heavy and heavies that never
+// turn keep probability 1 (they differ from 1 only by the rounding of the
+// weights).
+__global__ void k_alias_lights(const uint32_t* __restrict__ lidx, const unsigned long long* __restrict__ dsum,
+                               uint32_t nl, const uint32_t* __restrict__ hidx,
+                               const unsigned long long* __restrict__ esum, const unsigned long long* __restrict__ hexc,
+                               uint32_t nh, const unsigned long long* __restrict__ q, unsigned long long one, int frac,
+                               uint2* __restrict__ table) {
+  const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nl) return;
+  const unsigned long long d = dsum[a];
+  uint32_t lo = 0, hi = nh;  // first b with E(b + 1) >= D(a)
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (esum[mid] + hexc[mid] >= d) hi = mid; else lo = mid + 1;
+  }
+  const uint32_t t = lidx[a];
+  table[t] = lo < nh ? make_uint2(alias_threshold(q[t], one, frac), hidx[lo]) : make_uint2(0xffffffffu, t);
+}
+
+__global__ void k_alias_heavies(const uint32_t* __restrict__ hidx, const unsigned long long* __restrict__ esum,
+                                const unsigned long long* __restrict__ hexc, uint32_t nh,
+                                const unsigned long long* __restrict__ dsum, uint32_t nl, unsigned long long one,
+                                int frac, uint2* __restrict__ table) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nh) return;
+  const unsigned long long e1 = esum[b] + hexc[b];
+  uint32_t lo = 0, hi = nl + 1;  // first a in [0, nl] with D(a) > E(b + 1); D(nl) = all deficits
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (dsum[mid] > e1) hi = mid; else lo = mid + 1;
+  }
+  const uint32_t t = hidx[b];
+  if (lo <= nl && b + 1 < nh) {
+    const unsigned long long keep = one + hexc[b] + esum[b] - dsum[lo];  // q_b + E(b) - D(a), in [0, one)
+    table[t] = make_uint2(alias_threshold(keep, one, frac), hidx[b + 1]);
+  } else {
+    table[t] = make_uint2(0xffffffffu, t);
+  }
+}
+
+// Exact selection mass of each texel under the quantised table, in units of
+// 2^-32: its kept share plus what the entries aliased to it pass on.
+__global__ void k_alias_mass(const uint2* __restrict__ table, uint32_t n, unsigned long long* __restrict__ mass) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint2 e = table[i];
+  const unsigned long long keep = e.x == 0xffffffffu ? (1ull << 32) : (unsigned long long)e.x;
+  atomicAdd(mass + i, keep);
+  if (keep < (1ull << 32)) atomicAdd(mass + e.y, (1ull << 32) - keep);
+}
+
+// mass / 2^32 is the texel's density in (u, v); / (2 pi^2) gives the unit of
+// the histogram pdf texture (solid angle once divided by sin(phi)).
+__global__ void k_alias_pdf(const unsigned long long* __restrict__ mass, uint32_t n, float* __restrict__ pdf) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double unit = 1.0 / (2.0 * 3.141592653589793 * 3.141592653589793);
+  pdf[i] = (float)((double)mass[i] / 4294967296.0 * unit);
+}
+
 double js_min(double a, double b) { return (a != a || b != b) ? NAN : (a < b ? a : (b < a ? b : (std::signbit(a) ? a : b))); }
 double js_max(double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : (b > a ? b : (std::signbit(a) ? b : a))); }
 
@@ -167,6 +324,55 @@ int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_
   DevBuf<uint32_t> vals(n);
   k_env_radiance<<<(n + 255) / 256, 256, 0, s>>>(rgbe, n, rad.p, keys.p, vals.p);
   return build_from_radiance(s, w, h, rad, keys, vals, bins_out, nb_out, coords_out, pdf_out, why);
+}
+
+// PK_ENV_ALIAS's table for a w x h RGBE image on the device: per texel
+// {keep threshold, alias} (keep the uniformly drawn texel when the next 32-bit
+// random number is below the threshold, always when it is 0xffffffff) and
+// the pdf texture of its exact selection probabilities.  The radiance total
+// and the normalisation are FP64; the weights are then fixed point (2^-frac
+// of the mean, frac = 61 - ceil(log2 n)), so the prefix sums of the sweep are
+// exact integers.
+int build_env_alias_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<uint2>& table_out,
+                        DevBuf<float>& pdf_out, std::string& why) {
+  const uint32_t n = w * h;
+  if (n == 0 || n > (1u << 29)) { why = "environment size out of range"; return 1; }
+  int lg = 0;
+  while ((1ull << lg) < n) lg++;
+  const int frac = 61 - lg;  // >= 32
+  const unsigned long long one = 1ull << frac;
+  const unsigned nblk = (n + ALIAS_PER_BLOCK - 1) / ALIAS_PER_BLOCK, grid = (n + 255) / 256;
+  DevBuf<double> partial(nblk), scale(1);
+  DevBuf<uint32_t> status(1), light(n), lrank(n), nl_dev(1), lidx(n), hidx(n);
+  DevBuf<unsigned long long> q(n), ldef(n + 1), hexc(n), esum(n), mass(n);
+  k_alias_partial<<<nblk, ALIAS_THREADS, 0, s>>>(rgbe, n, partial.p);
+  k_alias_total<<<1, 1024, 0, s>>>(partial.p, nblk, n, frac, scale.p, status.p);
+  k_alias_weights<<<grid, 256, 0, s>>>(rgbe, n, scale.p, one, q.p, light.p);
+  check(cudaGetLastError(), "alias weights");
+  scan_exclusive_u32(s, light.p, lrank.p, n, nl_dev.p);  // synchronises
+  uint32_t st = 0, nl = 0;
+  check(cudaMemcpyAsync(&st, status.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaMemcpyAsync(&nl, nl_dev.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
+  check(cudaStreamSynchronize(s), "sync");
+  if (st) { why = "black or non-finite environment"; return 1; }
+  const uint32_t nh = n - nl;
+  check(cudaMemsetAsync(ldef.p + nl, 0, 8, s), "memset");  // D(nl) after the scan: all deficits
+  k_alias_split<<<grid, 256, 0, s>>>(q.p, light.p, lrank.p, n, one, lidx.p, ldef.p, hidx.p, hexc.p);
+  check(cudaGetLastError(), "alias split");
+  scan_exclusive_u64(s, ldef.p, ldef.p, (size_t)nl + 1);  // D(a), a = 0..nl
+  scan_exclusive_u64(s, hexc.p, esum.p, nh);  // E(b)
+  table_out.alloc(n);
+  pdf_out.alloc(n);
+  if (nl) k_alias_lights<<<(nl + 255) / 256, 256, 0, s>>>(lidx.p, ldef.p, nl, hidx.p, esum.p, hexc.p, nh, q.p, one,
+                                                          frac, table_out.p);
+  if (nh) k_alias_heavies<<<(nh + 255) / 256, 256, 0, s>>>(hidx.p, esum.p, hexc.p, nh, ldef.p, nl, one, frac,
+                                                           table_out.p);
+  check(cudaMemsetAsync(mass.p, 0, mass.bytes(), s), "memset");
+  k_alias_mass<<<grid, 256, 0, s>>>(table_out.p, n, mass.p);
+  k_alias_pdf<<<grid, 256, 0, s>>>(mass.p, n, pdf_out.p);
+  check(cudaGetLastError(), "alias table");
+  check(cudaStreamSynchronize(s), "sync");
+  return 0;
 }
 
 // The same tables for an FP32 RGB map (w x h x 3 on the device).

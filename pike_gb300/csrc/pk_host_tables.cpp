@@ -52,72 +52,4 @@ void build_material_layers(const double* mats9, uint32_t n_mats, std::vector<int
   }
 }
 
-bool build_env_alias(const uint8_t* rgbe, uint32_t w, uint32_t h, std::vector<uint32_t>& table2,
-                     std::vector<float>& pdf, std::string& why) {
-  const size_t N = (size_t)w * h;
-  std::vector<double> q(N);
-  double sum = 0.0, comp = 0.0;  // Neumaier's compensated sum
-  for (size_t i = 0; i < N; i++) {
-    const uint8_t* c = rgbe + 4 * i;
-    const double r = std::ldexp(1.0, (int)c[3] - 128) * (0.2126 * c[0] + 0.7152 * c[1] + 0.0722 * c[2]) / 255.0;
-    q[i] = r;
-    const double t = sum + r;
-    comp += std::fabs(sum) >= std::fabs(r) ? (sum - t) + r : (r - t) + sum;
-    sum = t;
-  }
-  sum += comp;
-  if (!(sum > 0.0) || !std::isfinite(sum)) {
-    why = "black or non-finite environment";
-    return false;
-  }
-  const double scale = (double)N / sum;
-  std::vector<uint32_t> small, large;
-  small.reserve(N);
-  large.reserve(N);
-  for (size_t i = 0; i < N; i++) {
-    q[i] *= scale;
-    (q[i] < 1.0 ? small : large).push_back((uint32_t)i);
-  }
-  std::vector<double> prob(N, 1.0);
-  std::vector<uint32_t> alias(N);
-  for (size_t i = 0; i < N; i++) alias[i] = (uint32_t)i;
-  while (!small.empty() && !large.empty()) {
-    const uint32_t s = small.back(), l = large.back();
-    small.pop_back();
-    large.pop_back();
-    prob[s] = q[s];
-    alias[s] = l;
-    q[l] = (q[l] + q[s]) - 1.0;
-    (q[l] < 1.0 ? small : large).push_back(l);
-  }
-  // what remains in either list has probability 1 up to rounding
-  table2.assign(2 * N, 0u);
-  std::vector<double> keep(N);
-  for (size_t i = 0; i < N; i++) {
-    uint32_t thr;
-    if (prob[i] >= 1.0) {
-      thr = 0xffffffffu;
-      keep[i] = 1.0;
-    } else {
-      const double t = std::floor(prob[i] * 4294967296.0);
-      thr = (uint32_t)std::min(t, 4294967294.0);
-      keep[i] = (double)thr / 4294967296.0;
-    }
-    table2[2 * i] = thr;
-    table2[2 * i + 1] = alias[i];
-  }
-  // exact selection probability of each texel under the quantised table
-  std::vector<double> p(N, 0.0);
-  for (size_t i = 0; i < N; i++) {
-    p[i] += keep[i];
-    if (keep[i] < 1.0) p[alias[i]] += 1.0 - keep[i];
-  }
-  pdf.assign(N, 0.0f);
-  // p[k] / N is texel k's probability, so p[k] is its density in (u, v);
-  // / (2 pi^2) gives the histogram pdf's unit (solid angle once / sin(phi))
-  const double unit = 1.0 / (2.0 * M_PI * M_PI);
-  for (size_t i = 0; i < N; i++) pdf[i] = (float)(p[i] * unit);
-  return true;
-}
-
 }  // namespace pk

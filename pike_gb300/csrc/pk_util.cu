@@ -74,6 +74,68 @@ void scan_exclusive_u32(cudaStream_t s, const uint32_t* in, uint32_t* out, uint3
   if (err) throw CudaError("scan_exclusive_u32: look-back timed out");
 }
 
+// ---------------- exclusive scan of u64 values (three phases) ---------------
+// Tiles of SCAN_TILE values: each block scans its tile and writes the tile's
+// sum; the tile sums are scanned recursively; a last pass adds each tile's
+// offset.  Integer sums, so the result does not depend on the grouping.
+__device__ __forceinline__ unsigned long long warp_scan_incl_u64(unsigned long long v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long x = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += x;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_u64_tiles(const unsigned long long* in,
+                                                                unsigned long long* out, size_t n,
+                                                                unsigned long long* __restrict__ tile_sums) {
+  __shared__ unsigned long long s_warp[SCAN_THREADS / 32];
+  const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  unsigned long long v[SCAN_ITEMS], sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    v[k] = base + k < n ? in[base + k] : 0ull;
+    sum += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned long long incl = warp_scan_incl_u64(sum);
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  unsigned long long woff = 0, tot = 0;
+  for (int k = 0; k < SCAN_THREADS / 32; k++) {
+    if (k < warp) woff += s_warp[k];
+    tot += s_warp[k];
+  }
+  unsigned long long run = woff + incl - sum;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_u64_add(unsigned long long* out, size_t n, const unsigned long long* __restrict__ tile_offs) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += tile_offs[i / SCAN_TILE];
+}
+
+void scan_exclusive_u64(cudaStream_t s, const unsigned long long* in, unsigned long long* out, size_t n) {
+  if (n == 0) return;
+  const size_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  DevBuf<unsigned long long> sums(ntiles);
+  k_scan_u64_tiles<<<(unsigned)ntiles, SCAN_THREADS, 0, s>>>(in, out, n, sums.p);
+  check(cudaGetLastError(), "k_scan_u64_tiles");
+  if (ntiles > 1) {
+    scan_exclusive_u64(s, sums.p, sums.p, ntiles);
+    k_scan_u64_add<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums.p);
+    check(cudaGetLastError(), "k_scan_u64_add");
+  }
+  check(cudaStreamSynchronize(s), "scan sync");  // the tile sums are freed on return
+}
+
 // ---------------- stable LSD radix sort -------------------------------------
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;

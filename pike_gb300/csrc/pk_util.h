@@ -49,6 +49,10 @@ struct DevBuf {
 // null it receives the sum (device pointer).  Counts must stay below 2^31.
 void scan_exclusive_u32(cudaStream_t s, const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total);
 
+// Exclusive prefix sum of n u64 values (in may alias out); returns after the
+// stream has finished it.
+void scan_exclusive_u64(cudaStream_t s, const unsigned long long* in, unsigned long long* out, size_t n);
+
 // Stable LSD radix sort of (key, value) pairs by the low `bits` bits of the
 // 64-bit keys, ascending.  Sorts in place using the given scratch buffers.
 void radix_sort_pairs_u64(cudaStream_t s, uint64_t* keys, uint32_t* vals, uint64_t* keys_tmp, uint32_t* vals_tmp,
@@ -69,5 +73,11 @@ int build_env_tables_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_
 // stored values in double (the differentiable renderer's sampling tables).
 int build_env_tables_gpu_f32(cudaStream_t s, const float* rgb, uint32_t w, uint32_t h, DevBuf<int2>& bins_out,
                              uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why);
+
+// PK_ENV_ALIAS's alias table for a w x h RGBE image on the device (pk_env.cu):
+// {keep threshold, alias} per texel and the pdf texture of the table's exact
+// selection probabilities.  Returns non-zero with a reason on failure.
+int build_env_alias_gpu(cudaStream_t s, const uchar4* rgbe, uint32_t w, uint32_t h, DevBuf<uint2>& table_out,
+                        DevBuf<float>& pdf_out, std::string& why);
 
 }  // namespace pk

@@ -1,9 +1,11 @@
-"""PK_ENV_ALIAS: environment sampling from a Walker/Vose alias table with
-FP64 normalisation (the precision form's alternative to env_sampler.js's
-equal-mass histogram; no reference counterpart).  The table's exact
-selection probabilities equal the texels' share of the radiance, its pdf
-texture matches them, and frames rendered with it equal the oracle's (run on
-the downloaded table) bit for bit."""
+"""PK_ENV_ALIAS: environment sampling from an alias table built on the GPU
+(FP64 normalisation, fixed-point weights, the parallel sweep from exact
+integer prefix sums; the precision form's alternative to env_sampler.js's
+equal-mass histogram; no reference counterpart).  The table and its pdf
+texture equal the oracle's numpy restatement bit for bit, the table's exact
+selection probabilities equal the texels' share of the radiance, and frames
+rendered with it equal the oracle's (run on the downloaded table) bit for
+bit."""
 import numpy as np
 import pytest
 
@@ -51,6 +53,21 @@ def test_alias_table_probabilities(oracle, pk_built, env_size):
     # pdf texture: probability * n / (2 pi^2), in binary32
     np.testing.assert_allclose(pdf.astype(np.float64), p * n / (2.0 * np.pi ** 2), rtol=2e-7, atol=0)
     assert ((pdf > 0) == (want > 0)).all()
+
+
+@pytest.mark.parametrize("env_size,sun", [((2048, 1024), 100.0), ((96, 48), 100.0), ((64, 32), 0.0)])
+def test_alias_table_equals_restatement(oracle, pk_built, env_size, sun):
+    from oracle import pyoracle
+    src = synth.displaced_sphere_scene(subdivisions=4, width=16, height=16, env_size=env_size)
+    rgbe = np.ascontiguousarray(synth.rgbe_encode(synth.hdr_env(synth.SEED_BASE + 3, env_size[0], env_size[1],
+                                                                sun=1.0)) if sun == 0.0 else src.env_rgbe, np.uint8)
+    pair = Pair(src, oracle)
+    pair.ctx.call("pk_env_build", ptr(rgbe), env_size[0], env_size[1])
+    pair.ctx.call("pk_set_env_sampling", _lib.PK_ENV_ALIAS)
+    table, pdf = alias_tables(pair.ctx, env_size[0] * env_size[1])
+    want_table, want_pdf = pyoracle.env_alias(rgbe)
+    assert np.array_equal(table, want_table)
+    assert np.array_equal(pdf.view(np.uint32), want_pdf.view(np.uint32))
 
 
 def test_alias_frames_match_oracle(oracle, pk_built):
