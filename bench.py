@@ -775,10 +775,19 @@ def alias_env_form(args, local: int):
     ctx.call("pk_set_camera", camera_struct(src))
     ctx.call("pk_set_frames_in_flight", 1)
     B = args.bounces
+    rgbe = np.ascontiguousarray(src.env_rgbe, np.uint8)
     for name, mode in (("histogram", _lib.PK_ENV_HISTOGRAM), ("alias", _lib.PK_ENV_ALIAS)):
+        # table build: pk_env_build in histogram mode (upload of the texels
+        # and env_sampler.js's tables), and the switch to alias mode (the
+        # alias table from the texels already on the device)
+        ctx.call("pk_set_env_sampling", _lib.PK_ENV_HISTOGRAM)
+        ctx.call("pk_env_build", ptr(rgbe), rgbe.shape[1], rgbe.shape[0])
         ctx.call("pk_sync")
         ctx.timer_start()
-        ctx.call("pk_set_env_sampling", mode)
+        if mode == _lib.PK_ENV_HISTOGRAM:
+            ctx.call("pk_env_build", ptr(rgbe), rgbe.shape[1], rgbe.shape[0])
+        else:
+            ctx.call("pk_set_env_sampling", mode)
         build_ms = ctx.timer_stop()
         ctx.call("pk_set_render_state", 0, 0.0)
         ctx.call("pk_render_frames", 2, B)
