@@ -1,14 +1,19 @@
-// pk_env.cu -- EnvironmentGenerator tables on the GPU (render/env_sampler.js:43-157):
+// pk_env.cu -- EnvironmentGenerator tables (render/env_sampler.js:43-157):
 // per-texel radiance, stable sort by descending radiance, equal-mass luminance
-// bins and the per-texel pdf.  The total radiance (row-major sum) and the bin
-// walk (a running sum reset at every bin) are sequentially rounded double sums
-// in the reference, so each is computed by one warp in order: the warp streams
-// 32 values at a time into registers and lane 0 adds them one by one.
+// bins and the per-texel pdf; and PK_ENV_ALIAS's alias table.  The total
+// radiance (row-major sum) and the bin walk (a running sum reset at every bin)
+// are sequentially rounded double sums in the reference, so they are one
+// chain of dependent FP64 additions each.  On GB300 a chain of FP64 additions
+// on one GPU lane runs about a hundred times slower than on a Grace core
+// (2048x1024: 380 ms for the tables with both walks on one warp), so the two
+// walks run on the host over the radiance the GPU computed; the radiance, the
+// sort, the pdf texture and the coordinates stay on the GPU.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include "pk_internal.cuh"
 #include "pk_util.h"
@@ -44,50 +49,6 @@ __global__ void k_env_radiance_f32(const float* __restrict__ rgb, uint32_t n, do
   rad[i] = v;
   keys[i] = ~(unsigned long long)__double_as_longlong(v);
   vals[i] = i;
-}
-
-// totalRadiance += rad (row-major) and brightestTexel = max(rad, brightest).
-__global__ void k_env_total(const double* __restrict__ rad, uint32_t n, double* __restrict__ out2) {
-  const int lane = threadIdx.x;
-  double total = 0.0, brightest = 0.0;
-  for (uint32_t base = 0; base < n; base += 32) {
-    const double v = base + lane < n ? rad[base + lane] : 0.0;
-    const uint32_t m = min(32u, n - base);
-    for (uint32_t k = 0; k < m; k++) {
-      const double x = __shfl_sync(0xffffffffu, v, (int)k);
-      brightest = fmax(x, brightest);
-      total = total + x;
-    }
-  }
-  if (lane == 0) { out2[0] = total; out2[1] = brightest; }
-}
-
-// createLuminanceHistogram (env_sampler.js:74-94): walk the sorted texels,
-// closing a bin when the running sum reaches binSize, then resetting it.
-__global__ void k_env_bins(const double* __restrict__ rad, const uint32_t* __restrict__ order, uint32_t n,
-                           double bin_size, int2* __restrict__ bins, uint32_t max_bins, uint32_t* __restrict__ nb_out) {
-  const int lane = threadIdx.x;
-  double current = 0.0;
-  uint32_t nb = 0;
-  int32_t prev = 0;
-  for (uint32_t base = 0; base < n; base += 32) {
-    const double v = base + lane < n ? rad[order[base + lane]] : 0.0;
-    const uint32_t m = min(32u, n - base);
-    for (uint32_t k = 0; k < m; k++) {
-      const double x = __shfl_sync(0xffffffffu, v, (int)k);
-      if (current >= bin_size) {
-        if (lane == 0 && nb < max_bins) bins[nb] = make_int2(prev, (int)(base + k));
-        prev = (int)(base + k);
-        nb++;
-        current = 0.0;
-      }
-      current = current + x;
-    }
-  }
-  if (lane == 0) {
-    if (nb < max_bins) bins[nb] = make_int2(prev, (int)n);
-    *nb_out = nb + 1;
-  }
 }
 
 // createPdfTexture / createEnvCoordBuffer (env_sampler.js:104-157).
@@ -279,35 +240,49 @@ int build_from_radiance(cudaStream_t s, uint32_t w, uint32_t h, DevBuf<double>& 
                         DevBuf<unsigned long long>& keys, DevBuf<uint32_t>& vals, DevBuf<int2>& bins_out,
                         uint32_t& nb_out, DevBuf<int2>& coords_out, DevBuf<float>& pdf_out, std::string& why) {
   const uint32_t n = w * h;
-  DevBuf<double> tot(2);
   DevBuf<unsigned long long> keys_tmp(n);
-  DevBuf<uint32_t> vals_tmp(n), nb(1);
-  k_env_total<<<1, 32, 0, s>>>(rad.p, n, tot.p);
-  check(cudaGetLastError(), "env radiance");
+  DevBuf<uint32_t> vals_tmp(n);
+  std::vector<double> r(n);
+  check(cudaMemcpyAsync(r.data(), rad.p, (size_t)n * 8, cudaMemcpyDeviceToHost, s), "D2H");
   radix_sort_pairs_u64(s, reinterpret_cast<uint64_t*>(keys.p), vals.p, reinterpret_cast<uint64_t*>(keys_tmp.p),
                        vals_tmp.p, n, 64);
-  double th[2];
-  check(cudaMemcpyAsync(th, tot.p, 16, cudaMemcpyDeviceToHost, s), "D2H");
+  std::vector<uint32_t> order(n);
+  check(cudaMemcpyAsync(order.data(), vals.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s), "D2H");
   check(cudaStreamSynchronize(s), "sync");
+  // totalRadiance += rad (row-major) and brightestTexel = max(rad, brightest)
+  double total = 0.0, brightest = 0.0;
+  for (uint32_t i = 0; i < n; i++) {
+    brightest = std::fmax(r[i], brightest);
+    total = total + r[i];
+  }
   // numBins = min(256, max(32, 2 * ceil(total / brightest))); binSize = total / numBins
-  const double num_bins = js_min(256.0, js_max(32.0, 2.0 * std::ceil(th[0] / th[1])));
+  const double num_bins = js_min(256.0, js_max(32.0, 2.0 * std::ceil(total / brightest)));
   if (num_bins != num_bins) { why = "environment has no radiance"; return 1; }
-  const double bin_size = th[0] / num_bins;
-  const uint32_t max_bins = 1024;
-  DevBuf<int2> bins(max_bins);
-  k_env_bins<<<1, 32, 0, s>>>(rad.p, vals.p, n, bin_size, bins.p, max_bins, nb.p);
-  uint32_t nbh = 0;
-  check(cudaMemcpyAsync(&nbh, nb.p, 4, cudaMemcpyDeviceToHost, s), "D2H");
-  check(cudaStreamSynchronize(s), "sync");
+  const double bin_size = total / num_bins;
+  // createLuminanceHistogram (env_sampler.js:74-94): walk the sorted texels,
+  // closing a bin when the running sum reaches binSize, then resetting it.
+  std::vector<int2> bins;
+  double current = 0.0;
+  int32_t prev = 0;
+  for (uint32_t k = 0; k < n; k++) {
+    if (current >= bin_size) {
+      bins.push_back(make_int2(prev, (int)k));
+      prev = (int)k;
+      current = 0.0;
+    }
+    current = current + r[order[k]];
+  }
+  bins.push_back(make_int2(prev, (int)n));
+  const uint32_t nbh = (uint32_t)bins.size();
   if (nbh < 2) { why = "environment yields a single luminance bin"; return 1; }
-  if (nbh > max_bins) { why = "too many luminance bins"; return 1; }
+  if (nbh > 1024) { why = "too many luminance bins"; return 1; }
+  bins_out.alloc(nbh);
+  check(cudaMemcpyAsync(bins_out.p, bins.data(), (size_t)nbh * 8, cudaMemcpyHostToDevice, s), "H2D");
   coords_out.alloc(n);
   pdf_out.alloc(n);
-  k_env_pdf<<<(n + 255) / 256, 256, 0, s>>>(vals.p, n, w, bins.p, nbh, coords_out.p, pdf_out.p);
+  k_env_pdf<<<(n + 255) / 256, 256, 0, s>>>(vals.p, n, w, bins_out.p, nbh, coords_out.p, pdf_out.p);
   check(cudaGetLastError(), "env pdf");
-  bins_out.alloc(nbh);
-  check(cudaMemcpyAsync(bins_out.p, bins.p, (size_t)nbh * 8, cudaMemcpyDeviceToDevice, s), "D2D");
-  check(cudaStreamSynchronize(s), "sync");
+  check(cudaStreamSynchronize(s), "sync");  // the host vectors are freed on return
   nb_out = nbh;
   return 0;
 }
