@@ -103,7 +103,10 @@ __device__ __forceinline__ float decode(float p, float s, int q) {
 }
 
 constexpr uint32_t LEAF_MAX = 3;
-constexpr float COST_NODE = 1.0f, COST_TRI = 0.3f;
+#ifndef PK_WIDE_COST_TRI
+#define PK_WIDE_COST_TRI 0.3f
+#endif
+constexpr float COST_NODE = 1.0f, COST_TRI = PK_WIDE_COST_TRI;
 constexpr uint8_t OPT_LEAF = 0xf0, OPT_INNER = 0xf1;  // else: split, j slots to the left child
 constexpr uint32_t E_VERTEX = 1, E_LEAF = 2, E_ORDER = 4, E_FIT = 8;
 
