@@ -1247,9 +1247,6 @@ void kernel_grids(int sms, uint32_t capacity, unsigned* trace, unsigned* compact
   *trace = std::max(1u, std::min((unsigned)(sms * std::max(t, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
   *compact = std::max(1u, std::min((unsigned)(sms * std::max(c, 1)), compact_tiles(capacity)));
   *shade = std::max(1u, std::min((unsigned)(sms * std::max(s, 1)), shade_tiles(capacity)));
-#ifdef PK_CW_GRID_BLOCKS
-  w = std::min(w, PK_CW_GRID_BLOCKS);
-#endif
   *trace_wide =
       std::max(1u, std::min((unsigned)(sms * std::max(w, 1)), (warps + TRACE_THREADS / 32 - 1) / (TRACE_THREADS / 32)));
 }
