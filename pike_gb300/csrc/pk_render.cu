@@ -456,6 +456,9 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #endif
 
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
+#ifndef PK_CW_PREFETCH
+#define PK_CW_PREFETCH 0
+#endif
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -546,6 +549,14 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
       cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
       G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
       T = make_uint2(tb, th);
+#if PK_CW_PREFETCH
+      if (ih && th) {  // the next node's record towards L1 while the triangles are tested
+        const uint32_t nslot = ((uint32_t)__ffs(ih) - 1u) ^ oct;
+        const float4* nr = sc.wide + 5 * (size_t)(cb + (uint32_t)__popc(im & ((1u << nslot) - 1u)));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(nr));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(nr + 4));
+      }
+#endif
     } else {  // a triangle group taken from the stack
       T = G;
       G = make_uint2(0u, 0u);

@@ -7,6 +7,10 @@ namespace pk {
 
 constexpr float MAX_T = 100000.0f;
 
+#ifndef PK_PREFETCH
+#define PK_PREFETCH 0
+#endif
+
 // =====================================================================
 // trace.wgsl:83-189 / trace_shadow.wgsl:82-190: BVH traversal.
 // =====================================================================
@@ -89,6 +93,19 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
     const float4* rec = sc.inner + 4 * (size_t)cur;
     const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
     const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
+#if PK_PREFETCH
+    // both children's records towards L1 while the boxes are tested
+    if (ch.x >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.inner + 4 * (size_t)ch.x));
+#if PK_PREFETCH > 1
+    else if (((uint32_t)ch.x >> 24) & 0x7fu)  // a leaf with triangles: base < n_tris
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.tris + 3 * (size_t)(ch.x & 0x00ffffff)));
+#endif
+    if (ch.y >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.inner + 4 * (size_t)ch.y));
+#if PK_PREFETCH > 1
+    else if (((uint32_t)ch.y >> 24) & 0x7fu)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.tris + 3 * (size_t)(ch.y & 0x00ffffff)));
+#endif
+#endif
     lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
     rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
     cl = ch.x;
