@@ -7,10 +7,6 @@ namespace pk {
 
 constexpr float MAX_T = 100000.0f;
 
-#ifndef PK_PREFETCH
-#define PK_PREFETCH 0
-#endif
-
 // =====================================================================
 // trace.wgsl:83-189 / trace_shadow.wgsl:82-190: BVH traversal.
 // =====================================================================
@@ -47,6 +43,9 @@ __device__ __forceinline__ float snorm_hi(int m) { return snorm16_decode((int)(i
 // 32-byte records keep the reference's snorm16 boxes {Lx, Ly, Lz, Rx}{Ry, Rz,
 // codeL, codeR}; 64-byte records (the default: fewer instructions per step,
 // which matters more than bytes here) hold the same boxes decoded.
+// (Prefetching both children's records into L1 while the boxes are tested
+// measured far slower at 1080p: 3188-3197 Mrays/s against 3738-3746, and
+// 2766-2769 with the leaves' first triangle too.)
 __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, float ox, float oy, float oz, float ix,
                                                float iy, float iz, float& lh, float& rh, int& cl, int& cr);
 
@@ -93,19 +92,6 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
     const float4* rec = sc.inner + 4 * (size_t)cur;
     const float4 a = __ldg(rec), b = __ldg(rec + 1), c4 = __ldg(rec + 2);
     const int4 ch = __ldg(reinterpret_cast<const int4*>(rec) + 3);
-#if PK_PREFETCH
-    // both children's records towards L1 while the boxes are tested
-    if (ch.x >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.inner + 4 * (size_t)ch.x));
-#if PK_PREFETCH > 1
-    else if (((uint32_t)ch.x >> 24) & 0x7fu)  // a leaf with triangles: base < n_tris
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.tris + 3 * (size_t)(ch.x & 0x00ffffff)));
-#endif
-    if (ch.y >= 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.inner + 4 * (size_t)ch.y));
-#if PK_PREFETCH > 1
-    else if (((uint32_t)ch.y >> 24) & 0x7fu)
-      asm volatile("prefetch.global.L1 [%0];" ::"l"(sc.tris + 3 * (size_t)(ch.y & 0x00ffffff)));
-#endif
-#endif
     lh = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, ox, oy, oz, ix, iy, iz);
     rh = box_hit(b.z, b.w, c4.x, c4.y, c4.z, c4.w, ox, oy, oz, ix, iy, iz);
     cl = ch.x;
