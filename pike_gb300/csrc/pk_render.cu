@@ -166,7 +166,8 @@ constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
 // refill.  Measured at 1080p, Mrays/s: unbounded 3137-3140; 1 step
 // 2749-2754, 2: 3082, 3: 3171-3190, 4: 3288-3342, 6: 3281-3294, 8:
 // 3365-3418, 12: 3345-3349, 16: 3248-3267, 24: 3165-3167.  PK_ANY_BUDGET
-// is the any-hit kernel's (default: the same).
+// is the any-hit kernel's (default: the same; 0, 4, 12 and 16 measured within
+// the noise of 8: 3702-3745 Mrays/s).
 #ifndef PK_INNER_BUDGET
 #define PK_INNER_BUDGET 8
 #endif
@@ -442,6 +443,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
 // 3102-3108 Mrays/s, up to two 2893-2900, up to four 1753-1767), and the
 // refill threshold of the binary traversal (16 idle lanes) is also best here
 // (1080p: 4 lanes 3275-3285, 8: 3305-3312, 16: 3357-3360, 24: 3315).
+// Prefetching the next node's record into L1 before the triangle tests
+// measured slightly slower (3320-3334 against 3347).
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
@@ -456,9 +459,6 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #endif
 
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
-#ifndef PK_CW_PREFETCH
-#define PK_CW_PREFETCH 0
-#endif
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -549,14 +549,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
       cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
       G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
       T = make_uint2(tb, th);
-#if PK_CW_PREFETCH
-      if (ih && th) {  // the next node's record towards L1 while the triangles are tested
-        const uint32_t nslot = ((uint32_t)__ffs(ih) - 1u) ^ oct;
-        const float4* nr = sc.wide + 5 * (size_t)(cb + (uint32_t)__popc(im & ((1u << nslot) - 1u)));
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(nr));
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(nr + 4));
-      }
-#endif
     } else {  // a triangle group taken from the stack
       T = G;
       G = make_uint2(0u, 0u);
