@@ -731,9 +731,6 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
 #ifndef PK_SHADE_THREADS
 #define PK_SHADE_THREADS 512
 #endif
-#ifndef PK_SHADE_WARP
-#define PK_SHADE_WARP 0
-#endif
 constexpr int SHADE_THREADS = PK_SHADE_THREADS;
 
 // shade_hit.wgsl:407-483 for one hit: the hit record of slot `r` (its
@@ -826,30 +823,12 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
                                                           RayQ S, uint32_t capacity, float4* __restrict__ color,
                                                           uint32_t npix, uint32_t* __restrict__ ticket,
                                                           unsigned long long* __restrict__ tiles) {
-#if !PK_SHADE_WARP
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warp[SHADE_THREADS / 32 + 1][2];
   __shared__ unsigned long long s_excl;
-#endif
   const uint32_t nh = ctr->num_hits;
   const int32_t samples = ctr->samples;
   const float theta = ctr->env_theta;
-#if PK_SHADE_WARP
-  // One warp per tile of 32 hits: ranks from ballots and the warp's own
-  // look-back, no block barrier.
-  const uint32_t ntiles = (nh + 31u) / 32u;
-  if (ntiles == 0) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) { ctr->num_rays = 0; ctr->num_shadow = 0; }
-    return;
-  }
-  const uint32_t lane = threadIdx.x & 31u, ltmask = (1u << lane) - 1u;
-  for (;;) {
-    uint32_t tile = 0;
-    if (lane == 0) tile = atomicAdd(ticket, 1u);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile >= ntiles) break;
-    const uint32_t r = tile * 32u + lane;
-#else
   const uint32_t ntiles = (nh + SHADE_THREADS - 1) / SHADE_THREADS;
   if (ntiles == 0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) { ctr->num_rays = 0; ctr->num_shadow = 0; }
@@ -861,7 +840,6 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
     const uint32_t tile = s_tile;
     if (tile >= ntiles) break;
     const uint32_t r = tile * SHADE_THREADS + threadIdx.x;
-#endif
     bool eb = false, es = false;
     float4 bo, bd, bt, so, sd, st;
     uint32_t j = 0;
@@ -878,13 +856,6 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
       if (shade_one(sc, env, theta, samples, r, o4, d4, t4, hr, em, eb, bo, bd, bt, es, so, sd, st))
         add_color(color, npix, __float_as_uint(t4.w) & 0x0fffffffu, em.x, em.y, em.z, 1.0f, &ctr->err);
     }
-#if PK_SHADE_WARP
-    const uint32_t bb = __ballot_sync(0xffffffffu, eb), bs = __ballot_sync(0xffffffffu, es);
-    const uint32_t ta = (uint32_t)__popc(bb), tb = (uint32_t)__popc(bs);
-    const unsigned long long excl = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
-    const uint32_t pb = unpack_a(excl) + (uint32_t)__popc(bb & ltmask);
-    const uint32_t ps = unpack_b(excl) + (uint32_t)__popc(bs & ltmask);
-#else
     uint32_t ea, es2, ta, tb;
     block_scan2<SHADE_THREADS / 32>(eb ? 1u : 0u, es ? 1u : 0u, ea, es2, ta, tb, s_warp);
     if (LOOKBACK_WARP) {
@@ -896,9 +867,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
       s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
     }
     __syncthreads();
-    const unsigned long long excl = s_excl;
-    const uint32_t pb = unpack_a(excl) + ea, ps = unpack_b(excl) + es2;
-#endif
+    const uint32_t pb = unpack_a(s_excl) + ea, ps = unpack_b(s_excl) + es2;
     if (eb) {
       if (pb < capacity) {  // read once by the next traversal: streaming stores
         __stcs(Rout.o + pb, bo);
@@ -915,22 +884,13 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
       }
       else atomicOr(&ctr->err, ERR_QUEUE);
     }
-#if PK_SHADE_WARP
-    if (tile == ntiles - 1 && lane == 0) {
-      ctr->num_rays = unpack_a(excl) + ta;
-      ctr->num_shadow = unpack_b(excl) + tb;
-    }
-  }
-}
-#else
     if (tile == ntiles - 1 && threadIdx.x == 0) {
-      ctr->num_rays = unpack_a(excl) + ta;
-      ctr->num_shadow = unpack_b(excl) + tb;
+      ctr->num_rays = unpack_a(s_excl) + ta;
+      ctr->num_shadow = unpack_b(s_excl) + tb;
     }
     __syncthreads();
   }
 }
-#endif
 
 // shade_miss.wgsl:45-57 over the materialised miss queue.
 __global__ void __launch_bounds__(128) k_shade_miss(EnvDev env, Counters* __restrict__ ctr, RayQ M,
@@ -1066,7 +1026,7 @@ __global__ void k_math(int fn, const float* __restrict__ x, const float* __restr
 static unsigned grid_for(uint32_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
 
 uint32_t compact_tiles(uint32_t capacity) { return ((capacity + 31u) / 32u + COMPACT_THREADS - 1) / COMPACT_THREADS; }
-uint32_t shade_tiles(uint32_t capacity) { return PK_SHADE_WARP ? (capacity + 31) / 32 : (capacity + SHADE_THREADS - 1) / SHADE_THREADS; }
+uint32_t shade_tiles(uint32_t capacity) { return (capacity + SHADE_THREADS - 1) / SHADE_THREADS; }
 
 // Persistent grids: enough resident blocks to fill every multiprocessor, never
 // more blocks than there can be work items.
