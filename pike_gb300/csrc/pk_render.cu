@@ -178,6 +178,10 @@ constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 #ifndef PK_LEAF_BUDGET
 #define PK_LEAF_BUDGET 0
 #endif
+#ifndef PK_LEAF_UNROLL
+#define PK_LEAF_UNROLL 0
+#endif
+constexpr int LEAF_UNROLL = PK_LEAF_UNROLL;
 constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
 
 constexpr int ANY_BUDGET = PK_ANY_BUDGET;
@@ -209,8 +213,11 @@ __device__ __forceinline__ void inner_children_exact(const SceneDev& sc, int cur
 // 10 resident blocks per SM (<= 48 registers): with several frames in
 // flight this beats the unconstrained 55 registers (2607-2611 vs 2579-2581
 // Mrays/s at 1080p, paired runs) and 12 blocks (2494).
+#ifndef PK_DYN_MINBLOCKS
+#define PK_DYN_MINBLOCKS 10
+#endif
 template <bool ANY, bool FUSED, bool COUNT, bool EXACT>
-__global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
+__global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(SceneDev sc, EnvDev env, Counters* __restrict__ ctr,
                                                               const uint32_t* __restrict__ countp, RayQ R,
                                                               uint4* __restrict__ hrec, uint32_t* __restrict__ flags,
                                                               float4* __restrict__ color, uint32_t npix,
@@ -373,6 +380,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, 10) k_trace_dyn(SceneDev sc, En
       const uint32_t word = (uint32_t)cur & 0x7fffffffu;
       const int size = (int)(word >> 24);
       const int base = (int)(word & 0x00ffffffu);
+#if PK_LEAF_UNROLL
+#pragma unroll LEAF_UNROLL
+#endif
       for (int i = 0; i < size; i++) {
         if (COUNT) ntest += 1;
         if (EXACT) {  // the watertight test of form (1), min (t, slot)
