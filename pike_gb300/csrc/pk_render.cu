@@ -178,8 +178,12 @@ constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 #ifndef PK_LEAF_BUDGET
 #define PK_LEAF_BUDGET 0
 #endif
+// Unroll of the leaf loop (the compiler then issues the next triangle's loads
+// early).  1080p, three paired runs: unrolled by 4 3753-3769 Mrays/s and a
+// 0.357-0.359 ms closest-hit launch, not unrolled 3727-3747 and 0.364-0.366
+// ms, by 2 3726-3734, by 8 3663-3673.
 #ifndef PK_LEAF_UNROLL
-#define PK_LEAF_UNROLL 0
+#define PK_LEAF_UNROLL 4
 #endif
 constexpr int LEAF_UNROLL = PK_LEAF_UNROLL;
 constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
@@ -213,6 +217,7 @@ __device__ __forceinline__ void inner_children_exact(const SceneDev& sc, int cur
 // 10 resident blocks per SM (<= 48 registers): with several frames in
 // flight this beats the unconstrained 55 registers (2607-2611 vs 2579-2581
 // Mrays/s at 1080p, paired runs) and 12 blocks (2494).
+// (9 blocks 3721-3728 Mrays/s, 11: 3669-3700, 10: 3738-3762)
 #ifndef PK_DYN_MINBLOCKS
 #define PK_DYN_MINBLOCKS 10
 #endif
