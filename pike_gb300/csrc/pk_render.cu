@@ -474,6 +474,10 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #endif
 
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
+#ifndef PK_CW_TRI_UNROLL
+#define PK_CW_TRI_UNROLL 0
+#endif
+constexpr int CW_TRI_UNROLL = PK_CW_TRI_UNROLL;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -568,6 +572,9 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
       T = G;
       G = make_uint2(0u, 0u);
     }
+#if PK_CW_TRI_UNROLL
+#pragma unroll CW_TRI_UNROLL
+#endif
     while (!fin && T.y != 0u) {
       if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
         if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }

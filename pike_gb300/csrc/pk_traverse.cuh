@@ -99,6 +99,11 @@ __device__ __forceinline__ void inner_children(const SceneDev& sc, int cur, floa
   }
 }
 
+#ifndef PK_RT_LEAF_UNROLL
+#define PK_RT_LEAF_UNROLL 0
+#endif
+constexpr int RT_LEAF_UNROLL = PK_RT_LEAF_UNROLL;
+
 // BLOCK threads per block share `sstack` (SSTACK entries per thread in shared
 // memory, 64 - SSTACK more in local memory).  ANY: any hit (trace_shadow.wgsl)
 // rather than closest hit; a constant at every inlined call site, a run-time
@@ -142,6 +147,9 @@ __device__ __forceinline__ void traverse_rt(const bool ANY, const SceneDev& sc, 
       const uint32_t word = (uint32_t)cur & 0x7fffffffu;
       const int size = (int)(word >> 24);
       const int base = (int)(word & 0x00ffffffu);
+#if PK_RT_LEAF_UNROLL
+#pragma unroll RT_LEAF_UNROLL
+#endif
       for (int i = 0; i < size; i++) {
         if (COUNT) ntest += 1;
         float res, u, v;
