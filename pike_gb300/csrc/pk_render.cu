@@ -459,7 +459,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
 // refill threshold of the binary traversal (16 idle lanes) is also best here
 // (1080p: 4 lanes 3275-3285, 8: 3305-3312, 16: 3357-3360, 24: 3315).
 // Prefetching the next node's record into L1 before the triangle tests
-// measured slightly slower (3320-3334 against 3347).
+// measured slightly slower (3320-3334 against 3347), and so did unrolling the
+// triangle loop (by 2: 3308-3326, by 4: 3171-3193, against 3347-3355).
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
@@ -474,10 +475,6 @@ constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local me
 #endif
 
 constexpr int CW_POSTPONE = PK_CW_POSTPONE;
-#ifndef PK_CW_TRI_UNROLL
-#define PK_CW_TRI_UNROLL 0
-#endif
-constexpr int CW_TRI_UNROLL = PK_CW_TRI_UNROLL;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -572,9 +569,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
       T = G;
       G = make_uint2(0u, 0u);
     }
-#if PK_CW_TRI_UNROLL
-#pragma unroll CW_TRI_UNROLL
-#endif
     while (!fin && T.y != 0u) {
       if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
         if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
