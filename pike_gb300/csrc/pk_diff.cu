@@ -64,12 +64,12 @@ constexpr int DIFF_MAX_DEPTH = 8;
 // traversal stack entries per lane in shared memory (the rest of 64 in local
 // memory): a small shared stack leaves more of the SM's L1 to node records
 constexpr int DIFF_SSTACK = 8;
+// The forward inlines its traversal (twice: closest and shadow rays); the
+// out-of-line copy the adjoint calls measured slower there (771-780 against
+// 866-872 Mrays/s on the differentiation workload).
 // 8 resident blocks per SM (64 registers, some spilled) for both kernels:
 // forward 795 against 764 Mrays/s unconstrained, adjoint 592 against 531
 // (the differentiation workload, same call; 6 blocks: 788 and 557).
-#ifndef PK_DIFF_FWD_OUTLINE
-#define PK_DIFF_FWD_OUTLINE 0
-#endif
 #ifndef PK_DIFF_FWD_BLOCKS
 #define PK_DIFF_FWD_BLOCKS 8
 #endif
@@ -338,7 +338,7 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
     float t;
     int idx;
     uint32_t bary;
-    if (REC || PK_DIFF_FWD_OUTLINE) diff_trace_out(false, sc, o4, d4, t, idx, bary, sstack, err);
+    if (REC) diff_trace_out(false, sc, o4, d4, t, idx, bary, sstack, err);
     else diff_trace(false, sc, o4, d4, t, idx, bary, sstack, err);
     nrays++;
     if (idx < 0) {
@@ -371,7 +371,7 @@ __device__ __forceinline__ void diff_path(const SceneDev& sc, const EnvDev& env,
       float ts;
       int is;
       uint32_t sb;
-      if (REC || PK_DIFF_FWD_OUTLINE) diff_trace_out(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
+      if (REC) diff_trace_out(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
       else diff_trace(true, sc, s.so, s.sd, ts, is, sb, sstack, err);
       nrays++;
       if (is < 0) {
