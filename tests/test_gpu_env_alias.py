@@ -55,12 +55,21 @@ def test_alias_table_probabilities(oracle, pk_built, env_size):
     assert ((pdf > 0) == (want > 0)).all()
 
 
-@pytest.mark.parametrize("env_size,sun", [((2048, 1024), 100.0), ((96, 48), 100.0), ((64, 32), 0.0)])
-def test_alias_table_equals_restatement(oracle, pk_built, env_size, sun):
+@pytest.mark.parametrize("env_size,kind", [((2048, 1024), "sun"), ((96, 48), "sun"), ((64, 32), "sky"),
+                                           ((48, 24), "uniform")])
+def test_alias_table_equals_restatement(oracle, pk_built, env_size, kind):
+    """Bit-exact table and pdf; "uniform" (every texel equal) puts every weight
+    within rounding of the mean, so lights and heavies differ by a few units."""
     from oracle import pyoracle
     src = synth.displaced_sphere_scene(subdivisions=4, width=16, height=16, env_size=env_size)
-    rgbe = np.ascontiguousarray(synth.rgbe_encode(synth.hdr_env(synth.SEED_BASE + 3, env_size[0], env_size[1],
-                                                                sun=1.0)) if sun == 0.0 else src.env_rgbe, np.uint8)
+    if kind == "sun":
+        rgbe = np.ascontiguousarray(src.env_rgbe, np.uint8)
+    elif kind == "sky":
+        rgbe = np.ascontiguousarray(synth.rgbe_encode(synth.hdr_env(synth.SEED_BASE + 3, env_size[0], env_size[1],
+                                                                    sun=1.0)), np.uint8)
+    else:
+        rgbe = np.zeros((env_size[1], env_size[0], 4), np.uint8)
+        rgbe[...] = (200, 150, 100, 129)
     pair = Pair(src, oracle)
     pair.ctx.call("pk_env_build", ptr(rgbe), env_size[0], env_size[1])
     pair.ctx.call("pk_set_env_sampling", _lib.PK_ENV_ALIAS)
