@@ -14,6 +14,11 @@ oracle (the oracle is what the fixtures check).
    component; scene.js _quantizeVec3ToInt (scene.js:104-111) stores each
    component into an Int8Array, and ToInt8(NaN) = 0, so the tangent and the
    bitangent words are 0; the normal (0,1,0) stores bytes {0, 127, 0, 0}.
+4. The typed-array quantisers of the scene tables (render/scene.js:104-118):
+   UV pairs go through Int16Array (ToInt16: truncation, then wrap modulo
+   2^16), so UVs outside [0, 1] wrap; normals through Int8Array after
+   Vec3.normalize.  The expected words follow the ECMAScript conversions
+   (js_toint below), not the oracle.
 3. The environment rotation theta in sampleEnv and envPdf
    (render/shader/shade_hit.wgsl:202-227): sampleEnv puts texel (cx, cy) at
    azimuth u = -theta + (cx + 0.5)/W, and envPdf reads u' = (1 + theta +
@@ -54,6 +59,48 @@ def rand_one():
     raise RuntimeError("no seed found")
 
 
+def js_toint(x: float, bits: int) -> int:
+    """ECMAScript ToInt8 / ToInt16 (the conversion a typed-array store
+    applies): NaN and infinities give 0; otherwise truncate toward zero and
+    wrap modulo 2^bits into [-2^(bits-1), 2^(bits-1))."""
+    if x != x or x in (math.inf, -math.inf):
+        return 0
+    i = int(math.copysign(math.floor(abs(x)), x))
+    i %= 1 << bits
+    return i - (1 << bits) if i >= 1 << (bits - 1) else i
+
+
+def uv_word(u: float, v: float) -> int:
+    """scene.js:113-118 _quantizeVec2ToInt: Int16Array{u * (u > 0 ? 32767 :
+    32768), v * ...} read back as one little-endian u32."""
+    a = js_toint(u * (32767 if u > 0 else 32768), 16)
+    b = js_toint(v * (32767 if v > 0 else 32768), 16)
+    return (a & 0xFFFF) | ((b & 0xFFFF) << 16)
+
+
+def normal_word(n) -> int:
+    """scene.js:104-111 _quantizeVec3ToInt of Vec3.normalize(n): Int8Array
+    bytes n_i * (n_i > 0 ? 127 : 128), the fourth byte 0."""
+    m = math.sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2])
+    k = 1.0 / m
+    w = 0
+    for i in range(3):
+        c = n[i] * k
+        w |= (js_toint(c * (127 if c > 0 else 128), 8) & 0xFF) << (8 * i)
+    return w
+
+
+def quantizers():
+    """UVs outside [0, 1] wrap: 1.5 * 32767 = 49150.5 truncates to 49150,
+    which Int16 stores as 49150 - 65536 = -16386 (a repeating texture's UV
+    decodes near -0.5); -1.5 * 32768 = -49152 stores as 16384."""
+    uvs = [[0.5, 0.25], [1.0, 0.0], [1.5, 2.25], [-0.25, -1.5], [3.0, -0.0], [1e-5, 0.999999]]
+    normals = [[0.0, 0.0, -1.0], [0.6, 0.8, 0.0], [-0.6, -0.8, 0.0], [0.0, 2.0, 0.0]]
+    return {"uv": [{"uv": uv, "word": uv_word(*uv)} for uv in uvs],
+            "normal": [{"normal": n, "word": normal_word(n)} for n in normals],
+            "why": "typed-array stores truncate toward zero and wrap modulo 2^16 / 2^8"}
+
+
 def main():
     c, s = math.cos(3 * math.pi / 8), math.sin(3 * math.pi / 8)
     out = {
@@ -64,6 +111,7 @@ def main():
         "env_theta_roundtrip": {"w": 8, "h": 4, "theta": 0.25, "texel": [3, 1], "u": 0.1875, "v": 0.375,
                                 "direction": [c * s, c, s * s], "pdf_texel": [3, 1],
                                 "why": "sampleEnv subtracts theta, envPdf adds it back"},
+        "quantizers": quantizers(),
     }
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "wgsl_quirks.json")
     with open(path, "w") as f:

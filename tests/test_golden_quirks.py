@@ -2,9 +2,10 @@
 tests/golden/make_wgsl_quirks.py from the reference's source text and the
 WGSL / JavaScript rules, not from the oracle) checked against the oracle:
 rand() returning exactly 1.0 (camera.wgsl:54-56), the NaN fallback tangent
-of a +y normal stored as 0 (gltf_loader.js:275, scene.js:104-111), and the
+of a +y normal stored as 0 (gltf_loader.js:275, scene.js:104-111), the
 environment rotation undone between sampleEnv and envPdf (shade_hit.wgsl:
-202-227)."""
+202-227), and the typed-array quantisers of the scene tables, UVs outside
+[0, 1] wrapping modulo 2^16 (scene.js:104-118)."""
 import json
 import os
 
@@ -72,3 +73,20 @@ def test_env_theta_roundtrip(oracle):
     d, texel = r.env_roundtrip(*q["texel"])
     assert np.allclose(d, q["direction"], atol=1e-6), (d, q["direction"])
     assert list(texel) == q["pdf_texel"]
+
+
+def test_scene_table_quantizers(oracle):
+    from types import SimpleNamespace
+    q = Q["quantizers"]
+    uv = np.array([e["uv"] for e in q["uv"]], np.float64)
+    n = uv.shape[0]
+    src = SimpleNamespace(pos=np.zeros((n, 3)), normal=np.tile([0.0, 0.0, 1.0], (n, 1)),
+                          tangent=np.tile([1.0, 0.0, 0.0, 1.0], (n, 1)), uv=uv)
+    _, attrs = oracle.flatten(src)
+    assert [int(w) for w in attrs[:, 3]] == [e["word"] for e in q["uv"]]
+    nrm = np.array([e["normal"] for e in q["normal"]], np.float64)
+    m = nrm.shape[0]
+    src = SimpleNamespace(pos=np.zeros((m, 3)), normal=nrm, tangent=np.tile([1.0, 0.0, 0.0, 1.0], (m, 1)),
+                          uv=np.zeros((m, 2)))
+    _, attrs = oracle.flatten(src)
+    assert [int(w) for w in attrs[:, 2]] == [e["word"] for e in q["normal"]]

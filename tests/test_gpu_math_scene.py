@@ -79,6 +79,31 @@ def test_scene_flatten_matches_oracle(ctx, oracle):
     assert np.array_equal(attrs, attrs_o)
 
 
+def test_scene_flatten_quantizer_known_answers(ctx):
+    """The GPU scene tables against the reference-derived words of
+    tests/golden/wgsl_quirks.json (typed-array stores of scene.js:104-118;
+    UVs outside [0, 1] wrap modulo 2^16)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "wgsl_quirks.json")) as f:
+        q = json.load(f)["quantizers"]
+    uv = np.array([e["uv"] for e in q["uv"]] + [[0.0, 0.0]] * len(q["normal"]), np.float64)
+    nrm = np.array([[0.0, 0.0, 1.0]] * len(q["uv"]) + [e["normal"] for e in q["normal"]], np.float64)
+    n = uv.shape[0]
+    pos = np.ascontiguousarray(np.arange(3 * n, dtype=np.float64).reshape(n, 3))
+    tan = np.ascontiguousarray(np.tile([1.0, 0.0, 0.0, 1.0], (n, 1)))
+    tris = np.arange(n - n % 3, dtype=np.int32).reshape(-1, 3)
+    tr = np.zeros(3)
+    ctx.call("pk_configure", 16, 16, 256)
+    ctx.call("pk_scene_flatten", ptr(pos), ptr(nrm), ptr(tan), ptr(uv), n, ptr(tris), tris.shape[0], 1.0, ptr(tr))
+    pos_d = np.zeros((n, 3), np.float64)
+    attrs = np.zeros((n, 4), np.uint32)
+    ctx.call("pk_scene_download", ptr(pos_d), ptr(attrs))
+    k = len(q["uv"])
+    assert [int(w) for w in attrs[:k, 3]] == [e["word"] for e in q["uv"]]
+    assert [int(w) for w in attrs[k:, 2]] == [e["word"] for e in q["normal"]]
+
+
 def test_materials_match_oracle(ctx, oracle):
     src = synth.displaced_sphere_scene(subdivisions=2, width=8, height=8)
     idx_o, layers_o = oracle.materials(src.materials)
