@@ -14,6 +14,11 @@ oracle (the oracle is what the fixtures check).
    component; scene.js _quantizeVec3ToInt (scene.js:104-111) stores each
    component into an Int8Array, and ToInt8(NaN) = 0, so the tangent and the
    bitangent words are 0; the normal (0,1,0) stores bytes {0, 127, 0, 0}.
+5. A black texel gets a luminance bin of its own (render/env_sampler.js:
+   74-95): the histogram walk closes a bin before adding the next texel and
+   pushes the last bin after the loop, so with every lit texel above binSize
+   each texel ends up alone in a bin and the black one is sampled as often
+   as any other (worked example in env_black_bin below).
 4. The typed-array quantisers of the scene tables (render/scene.js:104-118):
    UV pairs go through Int16Array (ToInt16: truncation, then wrap modulo
    2^16), so UVs outside [0, 1] wrap; normals through Int8Array after
@@ -101,6 +106,24 @@ def quantizers():
             "why": "typed-array stores truncate toward zero and wrap modulo 2^16 / 2^8"}
 
 
+def env_black_bin():
+    """env_sampler.js:59-95 on a 4 x 2 map of white texels with exponents
+    128 + k (radiance 2^k v, v = luma(255,255,255)/255) and one black texel.
+    The sort (b.rad - a.rad; Array.prototype.sort is stable) orders equal
+    radiances row-major.  numBins = max(32, 2 ceil(19v / 8v)) = 32, so
+    binSize = 19v/32 < v: every texel with light closes a bin at the next
+    step, and the closing push after the loop gives the black texel a bin of
+    its own.  Eight one-texel bins: every texel, the black one included, has
+    pdf (1/8) (8/1) / (2 pi^2)."""
+    ks = [[0, 0, 1, 1], [2, None, 0, 3]]
+    rgbe = [[[255, 255, 255, 128 + k] if k is not None else [0, 0, 0, 128] for k in row] for row in ks]
+    order = [(3, 1), (0, 1), (2, 0), (3, 0), (0, 0), (1, 0), (2, 1), (1, 1)]
+    pdf = (1.0 / 8.0) * (8.0 / 1.0) * (1.0 / (math.pi * math.pi * 2.0))
+    return {"rgbe": rgbe, "bins": [[i, i + 1] for i in range(8)], "coords": [list(c) for c in order],
+            "pdf_f32_bits": "0x%08x" % int(np.float32(pdf).view(np.uint32)),
+            "why": "the bin walk closes bins before adding; the last bin is pushed unconditionally"}
+
+
 def main():
     c, s = math.cos(3 * math.pi / 8), math.sin(3 * math.pi / 8)
     out = {
@@ -112,6 +135,7 @@ def main():
                                 "direction": [c * s, c, s * s], "pdf_texel": [3, 1],
                                 "why": "sampleEnv subtracts theta, envPdf adds it back"},
         "quantizers": quantizers(),
+        "env_black_bin": env_black_bin(),
     }
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "wgsl_quirks.json")
     with open(path, "w") as f:

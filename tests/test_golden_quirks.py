@@ -4,8 +4,9 @@ WGSL / JavaScript rules, not from the oracle) checked against the oracle:
 rand() returning exactly 1.0 (camera.wgsl:54-56), the NaN fallback tangent
 of a +y normal stored as 0 (gltf_loader.js:275, scene.js:104-111), the
 environment rotation undone between sampleEnv and envPdf (shade_hit.wgsl:
-202-227), and the typed-array quantisers of the scene tables, UVs outside
-[0, 1] wrapping modulo 2^16 (scene.js:104-118)."""
+202-227), the typed-array quantisers of the scene tables, UVs outside
+[0, 1] wrapping modulo 2^16 (scene.js:104-118), and a black texel given a
+luminance bin of its own (env_sampler.js:74-95)."""
 import json
 import os
 
@@ -90,3 +91,11 @@ def test_scene_table_quantizers(oracle):
                           uv=np.zeros((m, 2)))
     _, attrs = oracle.flatten(src)
     assert [int(w) for w in attrs[:, 2]] == [e["word"] for e in q["normal"]]
+
+
+def test_env_black_texel_bin(oracle):
+    q = Q["env_black_bin"]
+    env = oracle.Env(np.array(q["rgbe"], np.uint8))
+    assert env.bins.tolist() == q["bins"]
+    assert env.coords.tolist() == q["coords"]
+    assert (env.pdf.view(np.uint32) == int(q["pdf_f32_bits"], 16)).all()

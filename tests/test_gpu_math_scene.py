@@ -104,6 +104,28 @@ def test_scene_flatten_quantizer_known_answers(ctx):
     assert [int(w) for w in attrs[k:, 2]] == [e["word"] for e in q["normal"]]
 
 
+def test_env_black_texel_bin_known_answer(ctx):
+    """The GPU env tables against the reference-derived bins, coordinates and
+    pdf of tests/golden/wgsl_quirks.json (a black texel gets a bin of its
+    own, env_sampler.js:74-95)."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "wgsl_quirks.json")) as f:
+        q = json.load(f)["env_black_bin"]
+    rgbe = np.ascontiguousarray(np.array(q["rgbe"], np.uint8))
+    h, w = rgbe.shape[:2]
+    ctx.call("pk_env_build", ptr(rgbe), w, h)
+    ww, hh, nb = (np.zeros(1, np.uint32) for _ in range(3))
+    ctx.call("pk_env_info", ptr(ww), ptr(hh), ptr(nb))
+    assert int(nb[0]) == len(q["bins"])
+    bins = np.zeros((len(q["bins"]), 2), np.int32)
+    coords = np.zeros((w * h, 2), np.int32)
+    pdf = np.zeros((h, w), np.float32)
+    ctx.call("pk_env_download", ptr(bins), ptr(coords), ptr(pdf))
+    assert bins.tolist() == q["bins"] and coords.tolist() == q["coords"]
+    assert (pdf.view(np.uint32) == int(q["pdf_f32_bits"], 16)).all()
+
+
 def test_materials_match_oracle(ctx, oracle):
     src = synth.displaced_sphere_scene(subdivisions=2, width=8, height=8)
     idx_o, layers_o = oracle.materials(src.materials)
