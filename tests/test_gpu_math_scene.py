@@ -92,7 +92,9 @@ def test_scene_flatten_quantizer_known_answers(ctx):
     n = uv.shape[0]
     pos = np.ascontiguousarray(np.arange(3 * n, dtype=np.float64).reshape(n, 3))
     tan = np.ascontiguousarray(np.tile([1.0, 0.0, 0.0, 1.0], (n, 1)))
-    tris = np.arange(n - n % 3, dtype=np.int32).reshape(-1, 3)
+    k3 = n - n % 3
+    tris = np.zeros((k3 // 3, 4), np.int32)  # {i0, i1, i2, material}
+    tris[:, :3] = np.arange(k3, dtype=np.int32).reshape(-1, 3)
     tr = np.zeros(3)
     ctx.call("pk_configure", 16, 16, 256)
     ctx.call("pk_scene_flatten", ptr(pos), ptr(nrm), ptr(tan), ptr(uv), n, ptr(tris), tris.shape[0], 1.0, ptr(tr))
