@@ -271,7 +271,7 @@ def env_alias(rgbe: np.ndarray):
         s[:width] = s[:width] + s[width:2 * width]
         width //= 2
     total = s[0]
-    if not (total > 0.0 and total <= 1.7e308):
+    if not (total > 0.0 and np.isfinite(total)):
         return None
     lg = 0
     while (1 << lg) < n:

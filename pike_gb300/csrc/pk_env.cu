@@ -116,7 +116,7 @@ __global__ void k_alias_total(const double* __restrict__ partial, uint32_t m, ui
   }
   if (threadIdx.x == 0) {
     const double t = s[0];
-    const bool ok = t > 0.0 && t <= 1.7e308;
+    const bool ok = t > 0.0 && isfinite(t);
     *status = ok ? 0u : 1u;
     *scale = ok ? ldexp((double)n, frac) / t : 0.0;
   }
