@@ -508,6 +508,18 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
     ctx.call("pk_render_frames", steps, B)
     ems = ctx.timer_stop()
     erays = read_stats(ctx)["rays_traced"]
+    # the plain schedule of the drop-in: each warp takes 32 consecutive rays
+    # and traces them to the end (one ray per lane, as trace.wgsl runs one
+    # invocation per ray), no refill or bounded inner loop
+    ctx.call("pk_set_trace_mode", _lib.PK_TRACE_CHUNKED)
+    warm_graphs(ctx, first_sample, B)
+    ctx.call("pk_reset_stats")
+    ctx.call("pk_set_render_state", first_sample, 0.0)
+    ctx.call("pk_sync")
+    ctx.timer_start()
+    ctx.call("pk_render_frames", steps, B)
+    cms = ctx.timer_stop()
+    crays = read_stats(ctx)["rays_traced"]
     ctx.call("pk_set_trace_mode", plain_mode)
     tr = kt["trace"]
     R = max(counts["closest_rays"], 1)
@@ -527,7 +539,12 @@ def wide_form(ctx, args, B: int, first_sample: int, plain_mode: int):
                             "node_bytes": 64,
                             "fetch_units_per_ray": ecounts["closest_fetch"] / max(ecounts["closest_rays"], 1),
                             "closest_hit_agreement_with_wide": {"rays": etotal, "differ": ediffer,
-                                                                "fraction_equal": 1.0 - ediffer / max(etotal, 1)}}}
+                                                                "fraction_equal": 1.0 - ediffer / max(etotal, 1)}},
+            "chunked_dropin": {"value": crays / (cms / 1000.0) / 1e6, "unit": UNIT, "ms_per_step": cms / steps,
+                               "wide_over_chunked": (rays / ms) / max(crays / cms, 1e-9),
+                               "schedule": "the drop-in's kernels with 32 consecutive rays per warp traced to the "
+                                           "end (one ray per lane, no refill, no bounded inner loop); same "
+                                           "frame pipeline"}}
 
 
 def adjoint_form(args, local: int):
