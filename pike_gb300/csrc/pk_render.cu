@@ -1283,7 +1283,11 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads, int64_t offse
 
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
-  const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
+#ifndef PK_ANY_GRID_TENTHS
+#define PK_ANY_GRID_TENTHS 10
+#endif
+  const dim3 grid(any_hit ? std::max(1u, L.trace_blocks * PK_ANY_GRID_TENTHS / 10u) : L.trace_blocks),
+      block(TRACE_THREADS);
   const int defer = (L.defer_miss && fused && !any_hit) ? 1 : 0;
   if (L.trace_mode & TRACE_WIDE) {
     const dim3 grid(L.trace_blocks_wide);
