@@ -1286,7 +1286,10 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
 #ifndef PK_ANY_GRID_TENTHS
 #define PK_ANY_GRID_TENTHS 10
 #endif
-  const dim3 grid(any_hit ? std::max(1u, L.trace_blocks * PK_ANY_GRID_TENTHS / 10u) : L.trace_blocks),
+#ifndef PK_CLOSEST_GRID_TENTHS
+#define PK_CLOSEST_GRID_TENTHS 10
+#endif
+  const dim3 grid(std::max(1u, L.trace_blocks * (any_hit ? PK_ANY_GRID_TENTHS : PK_CLOSEST_GRID_TENTHS) / 10u)),
       block(TRACE_THREADS);
   const int defer = (L.defer_miss && fused && !any_hit) ? 1 : 0;
   if (L.trace_mode & TRACE_WIDE) {
