@@ -829,6 +829,19 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   const bool want = c->overlap == PK_OVERLAP_AUTO ? (c->in_flight == 1 || c->cap < (1u << 20)) : c->overlap != 0;
   const bool ov = want && !c->timing && (c->trace_mode & (pk::TRACE_PERSISTENT | pk::TRACE_WIDE)) != 0;
   L.defer_miss = ov;
+  // Persistent traversal grids beside concurrent work (1080p, eight frames in
+  // flight, tenths of the full grid for closest-hit / any-hit: 10/10
+  // 3756-3780 Mrays/s, 10/4 3811, 10/2 3878-3887, 6/4 3907-3920, 5/3
+  // 3910-3930, 6/2 3905-3914, 6/1 3908-3940, 4/2 3876-3908, 3/2 3847-3871;
+  // one frame with overlap: 10/10 2351, 10/4 2373, 6/2 2286, 4/2 2119).  A
+  // persistent kernel that fills every SM until its last rays finish keeps
+  // the other frames' kernels waiting; a smaller grid leaves them room.
+  if (c->in_flight > 1 && !c->timing) {
+    L.closest_tenths = 6;
+    L.any_tenths = 4;
+  } else if (ov) {
+    L.any_tenths = 4;
+  }
   LaunchCtx Ls = L;
   Ls.stream = fs.side;
   bool forked = false;

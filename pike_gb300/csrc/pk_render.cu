@@ -1283,14 +1283,7 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads, int64_t offse
 
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
-#ifndef PK_ANY_GRID_TENTHS
-#define PK_ANY_GRID_TENTHS 10
-#endif
-#ifndef PK_CLOSEST_GRID_TENTHS
-#define PK_CLOSEST_GRID_TENTHS 10
-#endif
-  const dim3 grid(std::max(1u, L.trace_blocks * (any_hit ? PK_ANY_GRID_TENTHS : PK_CLOSEST_GRID_TENTHS) / 10u)),
-      block(TRACE_THREADS);
+  const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
   const int defer = (L.defer_miss && fused && !any_hit) ? 1 : 0;
   if (L.trace_mode & TRACE_WIDE) {
     const dim3 grid(L.trace_blocks_wide);
@@ -1310,6 +1303,7 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
     return;
   }
   if (L.trace_mode & TRACE_PERSISTENT) {
+    const dim3 grid(std::max(1u, L.trace_blocks * (any_hit ? L.any_tenths : L.closest_tenths) / 10u));
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
 #define PK_TRACED(A, F, C)                                                                                         \

@@ -32,6 +32,9 @@ struct LaunchCtx {
   // Closest-hit misses park their contribution in the hit record for the
   // compaction to add (frames whose shadow traversal overlaps the next bounce).
   bool defer_miss = false;
+  // Persistent grid of the binary traversals in tenths of trace_blocks:
+  // smaller when other work runs beside them (frames in flight, overlap).
+  unsigned closest_tenths = 10, any_tenths = 10;
 };
 
 // offset >= 0: invocation offset of the rays (else the camera state's own)
