@@ -839,6 +839,9 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   if (c->in_flight > 1 && !c->timing) {
     L.closest_tenths = 6;
     L.any_tenths = 4;
+#ifdef PK_SHADE_TENTHS_PIPED
+    L.shade_tenths = PK_SHADE_TENTHS_PIPED;
+#endif
   } else if (ov) {
     L.any_tenths = 4;
   }

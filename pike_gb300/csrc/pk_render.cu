@@ -1357,7 +1357,7 @@ void launch_compact_shadow(const LaunchCtx& L, const uint32_t* flags, RayQ S, Ra
 
 void launch_shade(const LaunchCtx& L, const uint32_t* hit_list, const uint4* hrec, RayQ Rin, RayQ Rout, RayQ S,
                   uint32_t* ticket, unsigned long long* tiles) {
-  k_shade<<<L.shade_blocks, SHADE_THREADS, 0, L.stream>>>(L.scene, L.env, L.ctr, hit_list, hrec, Rin, Rout, S,
+  k_shade<<<std::max(1u, L.shade_blocks * L.shade_tenths / 10u), SHADE_THREADS, 0, L.stream>>>(L.scene, L.env, L.ctr, hit_list, hrec, Rin, Rout, S,
                                                           L.capacity, L.color, L.npix, ticket, tiles);
 }
 
