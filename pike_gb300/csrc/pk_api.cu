@@ -836,12 +836,12 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   // one frame with overlap: 10/10 2351, 10/4 2373, 6/2 2286, 4/2 2119).  A
   // persistent kernel that fills every SM until its last rays finish keeps
   // the other frames' kernels waiting; a smaller grid leaves them room.
+  // The shade kernel's grid likewise, with frames in flight (10/10
+  // 3889-3902, 7/10 3911-3948, 5/10 3915-3932, 3/10 3877-3914).
   if (c->in_flight > 1 && !c->timing) {
     L.closest_tenths = 6;
     L.any_tenths = 4;
-#ifdef PK_SHADE_TENTHS_PIPED
-    L.shade_tenths = PK_SHADE_TENTHS_PIPED;
-#endif
+    L.shade_tenths = 7;
   } else if (ov) {
     L.any_tenths = 4;
   }
