@@ -1281,19 +1281,14 @@ void launch_camera(const LaunchCtx& L, RayQ R, uint32_t n_threads, int64_t offse
   k_camera<<<grid_for(n_threads, 128), 128, 0, L.stream>>>(L.cam, L.ctr, R, n_threads, L.capacity, offset);
 }
 
-#ifndef PK_WIDE_GRID_TENTHS
-#define PK_WIDE_GRID_TENTHS 0
-#endif
 void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, const uint32_t* countp, RayQ R,
                   uint4* hrec, uint32_t* flags, uint32_t* ticket) {
   const dim3 grid(L.trace_blocks), block(TRACE_THREADS);
   const int defer = (L.defer_miss && fused && !any_hit) ? 1 : 0;
   if (L.trace_mode & TRACE_WIDE) {
-#if PK_WIDE_GRID_TENTHS
+    // (concurrent-work grids: 1080p, eight frames in flight, 3399-3423
+    // Mrays/s against 3348-3379 with the full grid)
     const dim3 grid(std::max(1u, L.trace_blocks_wide * (any_hit ? L.any_tenths : L.closest_tenths) / 10u));
-#else
-    const dim3 grid(L.trace_blocks_wide);
-#endif
     const unsigned words = (L.capacity + 31u) / 32u + 1u;
     if (!(any_hit && fused)) cudaMemsetAsync(flags, 0, (size_t)words * 4, L.stream);
 #define PK_TRACEW(A, F, C) \
