@@ -838,10 +838,23 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   // the other frames' kernels waiting; a smaller grid leaves them room.
   // The shade kernel's grid likewise, with frames in flight (10/10
   // 3889-3902, 7/10 3911-3948, 5/10 3915-3932, 3/10 3877-3914).
+#ifndef PK_CLOSEST_TENTHS_PIPED
+#define PK_CLOSEST_TENTHS_PIPED 6
+#endif
+#ifndef PK_ANY_TENTHS_PIPED
+#define PK_ANY_TENTHS_PIPED 4
+#endif
+#ifndef PK_SHADE_TENTHS_PIPED
+#define PK_SHADE_TENTHS_PIPED 7
+#endif
+#ifndef PK_COMPACT_TENTHS_PIPED
+#define PK_COMPACT_TENTHS_PIPED 10
+#endif
   if (c->in_flight > 1 && !c->timing) {
-    L.closest_tenths = 6;
-    L.any_tenths = 4;
-    L.shade_tenths = 7;
+    L.closest_tenths = PK_CLOSEST_TENTHS_PIPED;
+    L.any_tenths = PK_ANY_TENTHS_PIPED;
+    L.shade_tenths = PK_SHADE_TENTHS_PIPED;
+    L.compact_tenths = PK_COMPACT_TENTHS_PIPED;
   } else if (ov) {
     L.any_tenths = 4;
   }

@@ -1341,7 +1341,7 @@ void launch_trace(const LaunchCtx& L, bool any_hit, bool fused, bool count, cons
 
 void launch_compact_trace(const LaunchCtx& L, bool missq, const uint32_t* flags, uint32_t* hit_list, RayQ src,
                           RayQ M, uint32_t* ticket, unsigned long long* tiles, const uint4* miss_rec) {
-  const unsigned grid = L.compact_blocks;
+  const unsigned grid = std::max(1u, L.compact_blocks * L.compact_tenths / 10u);
   if (missq)
     k_compact<0, true><<<grid, COMPACT_THREADS, 0, L.stream>>>(L.ctr, flags, hit_list, src, M, L.miss_capacity,
                                                                 ticket, tiles, nullptr, L.color, L.npix);

@@ -35,7 +35,7 @@ struct LaunchCtx {
   // Persistent grid of the binary traversals in tenths of trace_blocks:
   // smaller when other work runs beside them (frames in flight, overlap).
   unsigned closest_tenths = 10, any_tenths = 10;
-  unsigned shade_tenths = 10;  // the same for the shade kernel's grid
+  unsigned shade_tenths = 10, compact_tenths = 10;  // the same for the shade and compaction grids
 };
 
 // offset >= 0: invocation offset of the rays (else the camera state's own)
