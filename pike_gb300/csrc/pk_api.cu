@@ -838,11 +838,14 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   // the other frames' kernels waiting; a smaller grid leaves them room.
   // The shade kernel's grid likewise, with frames in flight (10/10
   // 3889-3902, 7/10 3911-3948, 5/10 3915-3932, 3/10 3877-3914).
+// (with the shade grid at 7/10: closest/any 6/4 3916-3922, 5/3 3938-3968,
+// 6/3 3923-3924, 7/4 3892-3912; the compaction grid at 5/10 or 7/10 within
+// the noise of 10/10)
 #ifndef PK_CLOSEST_TENTHS_PIPED
-#define PK_CLOSEST_TENTHS_PIPED 6
+#define PK_CLOSEST_TENTHS_PIPED 5
 #endif
 #ifndef PK_ANY_TENTHS_PIPED
-#define PK_ANY_TENTHS_PIPED 4
+#define PK_ANY_TENTHS_PIPED 3
 #endif
 #ifndef PK_SHADE_TENTHS_PIPED
 #define PK_SHADE_TENTHS_PIPED 7
