@@ -296,7 +296,7 @@ int pk_env_alias_download(pk_ctx* ctx, uint32_t* table2, float* pdf);
  * persistent and 8-wide traversal modes without per-kernel timing. */
 #define PK_OVERLAP_AUTO (-1)
 int pk_set_frame_overlap(pk_ctx* ctx, int overlap);
-/* Frames of pk_render_frame in flight, 1 to 8 (4 by default): with 2 or more,
+/* Frames of pk_render_frame in flight, 1 to 16 (4 by default): with 2 or more,
  * consecutive frames render on separate sets of queues and streams so one
  * frame's kernels fill the idle time of another's; accumulation and
  * postprocessing stay in frame order and images are bit-identical to 1 (one

@@ -1224,7 +1224,7 @@ int pk_set_frame_overlap(pk_ctx* c, int on) {
 
 int pk_set_frames_in_flight(pk_ctx* c, int n) {
   return guarded(c, [&]() {
-    if (n < 1 || n > MAX_IN_FLIGHT) return fail(c, PK_ERR_ARG, "frames in flight must be 1 to 8");
+    if (n < 1 || n > MAX_IN_FLIGHT) return fail(c, PK_ERR_ARG, "frames in flight must be 1 to 16");
     c->in_flight = n;
     c->next_slot = 0;
     c->invalidate_graph();

@@ -12,7 +12,7 @@
 namespace pk {
 
 constexpr uint32_t MAX_BOUNCES = 16;
-constexpr int MAX_IN_FLIGHT = 8;  // frame slots
+constexpr int MAX_IN_FLIGHT = 16;  // frame slots
 constexpr int N_KINDS = 8;
 enum Kind { K_CAMERA = 0, K_TRACE, K_COMPACT, K_SHADE, K_SHADOW, K_ACCUM, K_POST, K_OTHER };
 

@@ -322,15 +322,15 @@ def test_frame_scheduling_arguments(oracle, pk_built):
     src = synth.small_scene(width=32, height=32)
     pair = Pair(src, oracle)
     c = pair.ctx
-    for bad in (0, 9, -1):
+    for bad in (0, 17, -1):
         with pytest.raises(_lib.PikeError) as e:
             c.call("pk_set_frames_in_flight", bad)
         assert e.value.code == _lib.PK_ERR_ARG
-    for n in (1, 8):
+    for n in (1, 8, 16):
         c.call("pk_set_frames_in_flight", n)
         c.call("pk_set_frame_overlap", 1 if n == 8 else _lib.PK_OVERLAP_AUTO)
-        fused_frames(pair, 9, 3)  # more frames than slots
-        assert pair.counters()["samples"] == 9 and pair.counters()["err"] == 0
+        fused_frames(pair, 17, 3)  # more frames than slots
+        assert pair.counters()["samples"] == 17 and pair.counters()["err"] == 0
 
 
 @pytest.mark.parametrize("batch,bounces", [(512, 3), (500, 8)])
