@@ -67,7 +67,7 @@ def parse():
                     help="run one small case of a form kernel (for ncu captures) and exit")
     ap.add_argument("--frames-in-flight", type=int, default=8, choices=list(range(1, 17)),
                     help="frames of pk_render_frame rendered concurrently (accumulation stays in order); "
-                         "8 measured 1-2%% above 4 at 1080p")
+                         "8 measured 1-2%% above 4 at 1080p, 12 and 16 no faster than 8")
     ap.add_argument("--overlap", choices=["auto", "on", "off"], default="auto",
                     help="shadow traversal beside the next bounce's closest-hit traversal "
                          "(auto: with one frame in flight or below 2^20 pixels)")
