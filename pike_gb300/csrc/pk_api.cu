@@ -810,6 +810,34 @@ int pk_postprocess(pk_ctx* c) {
   });
 }
 
+// Persistent grids, in tenths of the full grid, when other frames run beside
+// a frame's kernels: a persistent kernel that fills every SM until its last
+// rays finish keeps the other frames' kernels waiting, and a smaller grid
+// leaves them room.  1080p, eight frames in flight, closest-hit / any-hit
+// traversal: 10/10 3756-3780 Mrays/s, 10/4 3811, 10/2 3878-3887, 6/4
+// 3907-3920, 6/2 3905-3914, 6/1 3908-3940, 4/2 3876-3908, 3/2 3847-3871;
+// the shade kernel then (10/10 3889-3902, 7/10 3911-3948, 5/10 3915-3932,
+// 3/10 3877-3914), and with it closest/any 6/4 3916-3922, 5/3 3938-3968, 6/3
+// 3923-3924, 7/4 3892-3912; the compaction grid at 5/10 or 7/10 within the
+// noise of 10/10.  One frame with its shadow traversal overlapped: any-hit
+// 10/10 2351, 4/10 2373; a smaller closest-hit grid costs there (6/2 2286,
+// 4/2 2119).  The 8-wide traversal takes the same fractions of its grid.
+#ifndef PK_CLOSEST_TENTHS_PIPED
+#define PK_CLOSEST_TENTHS_PIPED 5
+#endif
+#ifndef PK_ANY_TENTHS_PIPED
+#define PK_ANY_TENTHS_PIPED 3
+#endif
+#ifndef PK_SHADE_TENTHS_PIPED
+#define PK_SHADE_TENTHS_PIPED 7
+#endif
+#ifndef PK_COMPACT_TENTHS_PIPED
+#define PK_COMPACT_TENTHS_PIPED 10
+#endif
+#ifndef PK_ANY_TENTHS_OVERLAP
+#define PK_ANY_TENTHS_OVERLAP 4
+#endif
+
 // One frame of slot k as its launch sequence on `st`.  With overlap
 // (persistent or 8-wide traversal, no per-kernel timing) each bounce's shadow
 // traversal forks onto the slot's side stream after shading and joins before
@@ -829,37 +857,14 @@ static void render_frame_launches(pk_ctx* c, int k, cudaStream_t st, uint32_t bo
   const bool want = c->overlap == PK_OVERLAP_AUTO ? (c->in_flight == 1 || c->cap < (1u << 20)) : c->overlap != 0;
   const bool ov = want && !c->timing && (c->trace_mode & (pk::TRACE_PERSISTENT | pk::TRACE_WIDE)) != 0;
   L.defer_miss = ov;
-  // Persistent traversal grids beside concurrent work (1080p, eight frames in
-  // flight, tenths of the full grid for closest-hit / any-hit: 10/10
-  // 3756-3780 Mrays/s, 10/4 3811, 10/2 3878-3887, 6/4 3907-3920, 5/3
-  // 3910-3930, 6/2 3905-3914, 6/1 3908-3940, 4/2 3876-3908, 3/2 3847-3871;
-  // one frame with overlap: 10/10 2351, 10/4 2373, 6/2 2286, 4/2 2119).  A
-  // persistent kernel that fills every SM until its last rays finish keeps
-  // the other frames' kernels waiting; a smaller grid leaves them room.
-  // The shade kernel's grid likewise, with frames in flight (10/10
-  // 3889-3902, 7/10 3911-3948, 5/10 3915-3932, 3/10 3877-3914).
-// (with the shade grid at 7/10: closest/any 6/4 3916-3922, 5/3 3938-3968,
-// 6/3 3923-3924, 7/4 3892-3912; the compaction grid at 5/10 or 7/10 within
-// the noise of 10/10)
-#ifndef PK_CLOSEST_TENTHS_PIPED
-#define PK_CLOSEST_TENTHS_PIPED 5
-#endif
-#ifndef PK_ANY_TENTHS_PIPED
-#define PK_ANY_TENTHS_PIPED 3
-#endif
-#ifndef PK_SHADE_TENTHS_PIPED
-#define PK_SHADE_TENTHS_PIPED 7
-#endif
-#ifndef PK_COMPACT_TENTHS_PIPED
-#define PK_COMPACT_TENTHS_PIPED 10
-#endif
+  // Persistent grids beside concurrent work (the constants above).
   if (c->in_flight > 1 && !c->timing) {
     L.closest_tenths = PK_CLOSEST_TENTHS_PIPED;
     L.any_tenths = PK_ANY_TENTHS_PIPED;
     L.shade_tenths = PK_SHADE_TENTHS_PIPED;
     L.compact_tenths = PK_COMPACT_TENTHS_PIPED;
   } else if (ov) {
-    L.any_tenths = 4;
+    L.any_tenths = PK_ANY_TENTHS_OVERLAP;
   }
   LaunchCtx Ls = L;
   Ls.stream = fs.side;
