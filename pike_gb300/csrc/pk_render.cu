@@ -142,24 +142,19 @@ constexpr int DYN_LOCAL = 64 - DYN_SMEM;
 
 // Any-hit rays report only whether some triangle is hit, and the set of leaves
 // a ray can reach (every box on the path from the root hit) does not depend
-// on the visiting order, so the production any-hit kernel may postpone leaves
-// (Aila & Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG
-// 2009, speculative while-while): a lane that reaches a leaf keeps it and goes
-// on popping inner nodes until every active lane of the warp holds a leaf, and
-// the leaves are then tested together.  Closest-hit rays cannot: trace.wgsl
-// culls a child box against the best distance found so far and its snorm16
-// boxes are truncated inward, so a hit can lie outside its leaf's box, and
-// testing a leaf later changes which boxes are culled and so, on rare rays,
-// the hit.  The counting variant keeps the reference order for its counts.
-// Measured on the 1080p benchmark (paired runs, same call), postponing was
-// slower: 2971-2976 Mrays/s against 3000-3002 without (the any-hit share of
-// the frame rose from 0.288 to 0.304: with about 2 leaves per shadow ray the
-// extra inner steps cost more than the coherent leaf tests save), so it is
-// off by default (PK_ANY_SPEC=1 builds it).
-#ifndef PK_ANY_SPEC
-#define PK_ANY_SPEC 0
-#endif
-constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
+// on the visiting order, so the any-hit kernel could postpone leaves (Aila &
+// Laine, "Understanding the Efficiency of Ray Traversal on GPUs", HPG 2009,
+// speculative while-while): a lane that reaches a leaf keeps it and goes on
+// popping inner nodes until every active lane of the warp holds a leaf.
+// Closest-hit rays cannot: trace.wgsl culls a child box against the best
+// distance found so far and its snorm16 boxes are truncated inward, so a hit
+// can lie outside its leaf's box, and testing a leaf later changes which boxes
+// are culled and so, on rare rays, the hit.  Measured on the 1080p benchmark
+// (paired runs, same call), postponing was slower: 2971-2976 Mrays/s against
+// 3000-3002 without (the any-hit share of the frame rose from 0.288 to 0.304:
+// with about 2 leaves per shadow ray the extra inner steps cost more than the
+// coherent leaf tests save), and it was removed.  So was a bound on the
+// leaves a lane tests before the warp meets again (no gain).
 // Inner-node steps a lane takes before the warp meets again at the top of the
 // loop (0: until it reaches a leaf).  Lanes whose rays need many steps no
 // longer hold the warp while the others wait in the leaf loop or idle for a
@@ -175,9 +170,6 @@ constexpr int SPEC_DONE = 0x7fffffff;  // "stack empty" for the speculative loop
 #define PK_ANY_BUDGET PK_INNER_BUDGET
 #endif
 constexpr int INNER_BUDGET = PK_INNER_BUDGET;
-#ifndef PK_LEAF_BUDGET
-#define PK_LEAF_BUDGET 0
-#endif
 // Unroll of the leaf loop (the compiler then issues the next triangle's loads
 // early).  1080p, three paired runs: unrolled by 4 3753-3769 Mrays/s and a
 // 0.357-0.359 ms closest-hit launch, not unrolled 3727-3747 and 0.364-0.366
@@ -186,7 +178,6 @@ constexpr int INNER_BUDGET = PK_INNER_BUDGET;
 #define PK_LEAF_UNROLL 4
 #endif
 constexpr int LEAF_UNROLL = PK_LEAF_UNROLL;
-constexpr int LEAF_BUDGET = PK_LEAF_BUDGET;
 
 constexpr int ANY_BUDGET = PK_ANY_BUDGET;
 
@@ -248,8 +239,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
   int best_i = -1;
   uint32_t best_b = 0u;
   int sp = 0, cur = 0;
-  constexpr bool SPEC = ANY && !COUNT && !EXACT && PK_ANY_SPEC;
-  int pl = 0;  // SPEC: the postponed leaf (a leaf code, < 0), or 0
   for (;;) {
     const uint32_t idle = __ballot_sync(0xffffffffu, !have && !exhausted);
     const uint32_t busy = __ballot_sync(0xffffffffu, have);
@@ -264,7 +253,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
           const float4 o = __ldcs(R.o + j), d = __ldcs(R.d + j);  // read once
           ox = o.x; oy = o.y; oz = o.z;
           dx = d.x; dy = d.y; dz = d.z;
-          pl = 0;
           if (EXACT) {
             ix = wide_inverse(dx); iy = wide_inverse(dy); iz = wide_inverse(dz);
             wr = wt_setup(ox, oy, oz, dx, dy, dz);
@@ -283,71 +271,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
     if (!__any_sync(0xffffffffu, have)) break;
     if (!have) continue;
     bool fin = false;
-    if (SPEC) {
-      // inner nodes; the first leaf reached is postponed and popping goes on
-      while ((uint32_t)cur < (uint32_t)SPEC_DONE) {
-        float lh, rh;
-        int cl, cr;
-        inner_children(sc, cur, ox, oy, oz, ix, iy, iz, lh, rh, cl, cr);
-        const bool lok = lh < MAX_T, rok = rh < MAX_T;
-        if (lok && rok) {
-          int nearc, farc;
-          if (lh > rh) { nearc = cr; farc = cl; } else { nearc = cl; farc = cr; }
-          if (sp < DYN_SMEM) sstack[sp][tid] = farc;
-          else if (sp < DYN_SMEM + DYN_LOCAL) lstack[sp - DYN_SMEM] = farc;
-          else { atomicOr(&ctr->err, ERR_STACK); fin = true; break; }
-          ++sp;
-          cur = nearc;
-        } else if (lok) {
-          cur = cl;
-        } else if (rok) {
-          cur = cr;
-        } else if (sp == 0) {
-          cur = SPEC_DONE;
-        } else {
-          --sp;
-          cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM];
-        }
-        if (cur < 0 && pl == 0) {
-          pl = cur;
-          if (sp == 0) cur = SPEC_DONE;
-          else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
-        }
-        if (__all_sync(__activemask(), pl != 0)) break;
-      }
-      // leaves: the postponed one, then any leaf that comes next
-      if (!fin && pl == 0 && cur < 0) {
-        pl = cur;
-        if (sp == 0) cur = SPEC_DONE;
-        else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
-      }
-      while (!fin && pl < 0) {
-        const uint32_t word = (uint32_t)pl & 0x7fffffffu;
-        const int size = (int)(word >> 24);
-        const int base = (int)(word & 0x00ffffffu);
-        for (int i = 0; i < size; i++) {
-          float res, u, v;
-          if (mt_test(sc, base + i, ox, oy, oz, dx, dy, dz, eps, res, u, v) && res < MAX_T) {
-            best_t = res;
-            best_i = base + i;
-            break;
-          }
-        }
-        if (best_i != -1) { fin = true; break; }
-        pl = 0;
-        if (cur < 0) {
-          pl = cur;
-          if (sp == 0) cur = SPEC_DONE;
-          else { --sp; cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM]; }
-        }
-      }
-      if (!fin && pl == 0 && cur == SPEC_DONE) fin = true;
-    }
     // inner nodes (at most INNER_BUDGET steps before the warp meets again at
     // the top of the loop, when the budget is not 0)
     constexpr int BUDGET = ANY ? ANY_BUDGET : INNER_BUDGET;
     int budget = BUDGET;
-    while (!SPEC && cur >= 0 && (BUDGET == 0 || budget-- > 0)) {
+    while (cur >= 0 && (BUDGET == 0 || budget-- > 0)) {
       if (COUNT) nfetch += 3;
       float lh, rh;
       int cl, cr;
@@ -378,9 +306,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
       --sp;
       cur = sp < DYN_SMEM ? sstack[sp][tid] : lstack[sp - DYN_SMEM];
     }
-    // leaves (at most LEAF_BUDGET before the warp meets, when not 0)
-    int lbudget = LEAF_BUDGET;
-    while (!SPEC && !fin && cur < 0 && (LEAF_BUDGET == 0 || lbudget-- > 0)) {
+    // leaves
+    while (!fin && cur < 0) {
       if (COUNT) nfetch += 1;
       const uint32_t word = (uint32_t)cur & 0x7fffffffu;
       const int size = (int)(word >> 24);
@@ -447,12 +374,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
 // children of one node, visited in the ray's octant order (lowest bit
 // first); a triangle group {tri_base, triangle bits} for its hit leaf
 // triangles.  Each step visits one child of the current node group (pushing
-// the rest of the group) and then tests the triangle group in hand.  With
-// PK_CW_POSTPONE = p > 0, while fewer than p lanes of the warp have triangles
-// and this lane still has nodes to visit, the triangle group is pushed
-// instead and tested later (Ylitie et al.'s triangle postponing); measured on
-// the 1080p benchmark it costs more than it saves (p = 4: 2669 Mrays/s,
-// p = 8: 2569, p = 0: 2939), so it is off by default.  Lanes take new rays as
+// the rest of the group) and then tests the triangle group in hand.  Ylitie
+// et al.'s triangle postponing (while fewer than p lanes of the warp have
+// triangles and this lane still has nodes to visit, push the triangle group
+// and test it later) cost more than it saved on the 1080p benchmark (p = 4:
+// 2669 Mrays/s, p = 8: 2569, without: 2939) and was removed.  Lanes take new rays as
 // in k_trace_dyn.  Unlike the binary traversal, letting a lane visit several
 // nodes in a row before the warp meets again did not pay (1080p: one visit
 // 3102-3108 Mrays/s, up to two 2893-2900, up to four 1753-1767), and the
@@ -470,11 +396,6 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
 #endif
 constexpr int CW_STACK_SMEM = PK_CW_SMEM;       // group entries per thread in shared memory
 constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local memory
-#ifndef PK_CW_POSTPONE
-#define PK_CW_POSTPONE 0
-#endif
-
-constexpr int CW_POSTPONE = PK_CW_POSTPONE;
 
 __device__ __forceinline__ bool cw_push(uint2 (*sstack)[TRACE_THREADS], uint2* lstack, int tid, int& sp, uint2 g) {
   if (sp < CW_STACK_SMEM) sstack[sp][tid] = g;
@@ -565,16 +486,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
       cw_node(sc.wide, node, ox, oy, oz, ix, iy, iz, oct, best_t, cb, tb, im, ih, th);
       G = ih ? make_uint2(cb, (ih << 24) | im) : make_uint2(0u, 0u);
       T = make_uint2(tb, th);
-    } else {  // a triangle group taken from the stack
-      T = G;
-      G = make_uint2(0u, 0u);
     }
     while (!fin && T.y != 0u) {
-      if (CW_POSTPONE > 0 && G.y > 0x00ffffffu && __popc(__activemask()) < CW_POSTPONE) {
-        if (!cw_push(sstack, lstack, tid, sp, T)) { atomicOr(&ctr->err, ERR_STACK); fin = true; }
-        T.y = 0u;
-        break;
-      }
       const uint32_t i = (uint32_t)__ffs(T.y) - 1u;
       T.y &= T.y - 1u;
       if (COUNT) ntest += 1;
@@ -629,11 +542,8 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_CW_MINBLOCKS) k_trace_cw(Sce
 #endif
 constexpr int COMPACT_THREADS = PK_COMPACT_THREADS;
 // The compaction and shade kernels take their tile's prefix with a whole warp
-// (lookback2_warp) rather than one thread (lookback2).
-#ifndef PK_LOOKBACK_WARP
-#define PK_LOOKBACK_WARP 1
-#endif
-constexpr bool LOOKBACK_WARP = PK_LOOKBACK_WARP;
+// (lookback2_warp) rather than one thread (lookback2): 3137-3140 against
+// 3020-3026 Mrays/s at 1080p when it was introduced.
 
 template <int MODE, bool MISSQ>
 __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restrict__ ctr,
@@ -673,13 +583,9 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
     const uint32_t cb = (MODE == 1 || MISSQ) ? (uint32_t)__popc(mm) : 0u;
     uint32_t ea, eb, ta, tb;
     block_scan2<COMPACT_THREADS / 32>(ca, cb, ea, eb, ta, tb, s_warp);
-    if (LOOKBACK_WARP) {
-      if (threadIdx.x < 32) {
-        const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
-        if (threadIdx.x == 0) s_excl = e;
-      }
-    } else if (threadIdx.x == 0) {
-      s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    if (threadIdx.x < 32) {
+      const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
+      if (threadIdx.x == 0) s_excl = e;
     }
     __syncthreads();
     const uint32_t pa = unpack_a(s_excl) + ea;
@@ -874,13 +780,9 @@ __global__ void __launch_bounds__(SHADE_THREADS, PK_SHADE_BLOCKS) k_shade(SceneD
     }
     uint32_t ea, es2, ta, tb;
     block_scan2<SHADE_THREADS / 32>(eb ? 1u : 0u, es ? 1u : 0u, ea, es2, ta, tb, s_warp);
-    if (LOOKBACK_WARP) {
-      if (threadIdx.x < 32) {
-        const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
-        if (threadIdx.x == 0) s_excl = e;
-      }
-    } else if (threadIdx.x == 0) {
-      s_excl = lookback2(tiles, tile, pack2(ta, tb), &ctr->err);
+    if (threadIdx.x < 32) {
+      const unsigned long long e = lookback2_warp(tiles, tile, pack2(ta, tb), &ctr->err);
+      if (threadIdx.x == 0) s_excl = e;
     }
     __syncthreads();
     const uint32_t pb = unpack_a(s_excl) + ea, ps = unpack_b(s_excl) + es2;
