@@ -162,7 +162,9 @@ constexpr int DYN_LOCAL = 64 - DYN_SMEM;
 // 2749-2754, 2: 3082, 3: 3171-3190, 4: 3288-3342, 6: 3281-3294, 8:
 // 3365-3418, 12: 3345-3349, 16: 3248-3267, 24: 3165-3167.  PK_ANY_BUDGET
 // is the any-hit kernel's (default: the same; 0, 4, 12 and 16 measured within
-// the noise of 8: 3702-3745 Mrays/s).
+// the noise of 8: 3702-3745 Mrays/s).  Measured again with the concurrent-work
+// grids: 8 3899-3928, 6 3736-3752, 12 3877-3885; refill threshold 16
+// 3899-3928, 8 3898-3933, 12 3903-3962, 20 3868-3880.
 #ifndef PK_INNER_BUDGET
 #define PK_INNER_BUDGET 8
 #endif
