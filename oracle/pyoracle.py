@@ -233,7 +233,7 @@ class EnvF32:
             self._h = None
 
 
-def env_alias(rgbe: np.ndarray):
+def env_alias(rgbe: np.ndarray, return_weights: bool = False):
     """PK_ENV_ALIAS's table restated in numpy (the precision form; no
     reference counterpart): the radiance of env_sampler.js:43-48 in FP64,
     its total summed in the GPU builder's grouping (blocks of 1024 texels:
@@ -243,7 +243,7 @@ def env_alias(rgbe: np.ndarray):
     and the sweep of Huebschle-Schneider & Sanders ("Parallel Weighted
     Random Sampling", 2022) evaluated from exact integer prefix sums.
     Returns (table (n, 2) uint32 {keep threshold, alias}, pdf (n,) float32),
-    or None for a black map."""
+    or None for a black map; with return_weights, (q, f) instead."""
     c = np.asarray(rgbe, np.uint8).reshape(-1, 4)
     cf = c.astype(np.float64)
     r = np.ldexp(1.0, c[:, 3].astype(np.int64) - 128) * (0.2126 * cf[:, 0] + 0.7152 * cf[:, 1] + 0.0722 * cf[:, 2]) / 255.0
@@ -279,6 +279,8 @@ def env_alias(rgbe: np.ndarray):
     frac = 61 - lg
     one = np.uint64(1 << frac)
     q = np.rint(r * (np.ldexp(float(n), frac) / total)).astype(np.uint64)
+    if return_weights:
+        return q, frac
     light = q < one
     L = np.nonzero(light)[0]
     H = np.nonzero(~light)[0]

@@ -37,3 +37,50 @@ def test_restated_alias_table_is_exact(env_size):
 def test_restated_alias_table_rejects_black_map():
     from oracle import pyoracle
     assert pyoracle.env_alias(np.zeros((4, 8, 4), np.uint8)) is None
+
+
+def sequential_sweep(q, frac):
+    """The sweeping alias construction run in order (Huebschle-Schneider &
+    Sanders 2022, the sequential algorithm the parallel evaluation restates):
+    lights in index order are served by the current heavy while its weight is
+    at least one; a heavy whose weight falls below one keeps it and takes the
+    next heavy as its alias, which pays its deficit."""
+    one = 1 << frac
+    q = [int(x) for x in q]
+    n = len(q)
+    L = [i for i in range(n) if q[i] < one]
+    H = [i for i in range(n) if q[i] >= one]
+    keep = [one] * n
+    alias = list(range(n))
+    if not H:
+        return keep, alias
+    a, b, w = 0, 0, q[H[0]]
+    while a < len(L) or w < one:
+        if w >= one and a < len(L):
+            keep[L[a]] = q[L[a]]
+            alias[L[a]] = H[b]
+            w -= one - q[L[a]]
+            a += 1
+        elif w < one and b + 1 < len(H):
+            keep[H[b]] = w
+            alias[H[b]] = H[b + 1]
+            w = q[H[b + 1]] - (one - w)
+            b += 1
+        else:
+            break
+    return keep, alias
+
+
+@pytest.mark.parametrize("env_size", [(96, 48), (40, 20), (5, 3)])
+def test_parallel_sweep_equals_sequential_sweep(env_size):
+    """The prefix-sum evaluation of the sweep gives the sequential sweep's
+    table entry for entry."""
+    from oracle import pyoracle
+    src = synth.displaced_sphere_scene(subdivisions=1, width=8, height=8, env_size=(max(env_size[0], 4), max(env_size[1], 2)))
+    rgbe = np.ascontiguousarray(np.asarray(src.env_rgbe, np.uint8)[:env_size[1], :env_size[0]])
+    q, frac = pyoracle.env_alias(rgbe, return_weights=True)
+    keep, alias = sequential_sweep(q, frac)
+    thr = [0xFFFFFFFF if k >= (1 << frac) else min(k >> (frac - 32), 0xFFFFFFFE) for k in keep]
+    table, _ = pyoracle.env_alias(rgbe)
+    assert table[:, 1].tolist() == alias
+    assert table[:, 0].tolist() == thr
