@@ -264,6 +264,38 @@ def test_bvh_two_separated_triangles_known_answer(oracle):
     assert b.nodes[0, 2] == struct.unpack("<i", struct.pack("<hh", 32767, -32768))[0]
 
 
+def test_bvh_coincident_triangles_make_one_leaf(oracle):
+    """bvh.js:137 makes a leaf when the best split costs more than the
+    triangle count.  Two copies of one triangle: every box equals the
+    parent's, so both candidates cost 0.5 + 1*1 + 1*1 = 2.5 (i = 0) and
+    0.5 + 1*2 + 0 = 2.5 (i = 1), both above 2: one leaf of two triangles, in
+    input order."""
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    tris = np.array([[0, 1, 2, 0], [3, 4, 5, 0]], np.int32)
+    b = oracle.BVH(pos, tris)
+    assert b.n_nodes == 1
+    assert b.nodes[0, 0] == -1 and b.nodes[0, 1] == (2 << 24) | 0
+
+
+def test_bvh_cost_tie_goes_to_x(oracle):
+    """bvh.js:194-207 keeps a candidate only when it is strictly cheaper, axes
+    in order x, y, z.  Two unit right triangles offset by (5, 5, 0): the
+    candidate right box areasBack[n - 1 - i] still holds ref i (the right
+    side of split i is refs[i..n-1]), so split 0 costs 0.5 + 2/72 + 72/72 on
+    every axis (z included, where both centroids are 0 and the stable sort
+    keeps input order) and split 1 costs 2.5; the first, x, wins: the root's
+    left child is the triangle at the smaller x."""
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [5, 5, 0], [6, 5, 0], [5, 6, 0]], float)
+    tris = np.array([[3, 4, 5, 0], [0, 1, 2, 0]], np.int32)
+    b = oracle.BVH(pos, tris)
+    assert b.n_nodes == 3
+    assert b.nodes[0, 0] == 1 and b.nodes[0, 1] == -1
+    # left child: the triangle with the smaller x centroid (input index 1),
+    # leaf-ordered first; right child: input index 0
+    assert b.nodes[1, 1] == (1 << 24) | 0 and b.nodes[2, 1] == (1 << 24) | 1
+    assert [int(v) for v in b.tris[:, 0]] == [0, 3]
+
+
 # ---------------- env_sampler.js, restated in Python ----------------
 def py_env_tables(rgbe):
     h, w = rgbe.shape[:2]
