@@ -649,7 +649,8 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact(Counters* __restric
 // 3334-3337 Mrays/s, 128 x 12 3519-3526, 256 x 6 3690-3692, 512 x 3
 // 3706-3718, 1024 x 1 3514-3551; fewer resident threads at 256 (5 blocks
 // 3665-3676, 4 blocks 3638-3639).  Larger tiles mean fewer look-back steps
-// per hit.  One warp per 32-hit tile with its own look-back and no block
+// per hit (with the concurrent-work grids, 256 x 6 measured 3606-3661
+// against 3871-3970 for 512 x 3).  One warp per 32-hit tile with its own look-back and no block
 // barrier (bit-identical queues) measured slower again with the warp-wide
 // look-back: 3405-3415 against 3718-3759.
 #ifndef PK_SHADE_THREADS
