@@ -134,6 +134,8 @@ constexpr int REFILL_MIN = PK_REFILL_MIN;
 // 3541-3546, 8: 3552-3572, 4: 3511-3523).  The driver's own carveout for the
 // resulting shared memory was kept: asking for 25% gave 3547-3556, 50%
 // 3495-3514, and 0% (all L1) cut the resident blocks: 975.
+// (with the concurrent-work grids: 4 entries 3826-3867, 8 3905-3971, 12
+// 3870-3980, 16 3908-3972 in paired runs: 8 kept)
 #ifndef PK_DYN_SMEM
 #define PK_DYN_SMEM 8
 #endif
