@@ -394,9 +394,11 @@ __global__ void __launch_bounds__(TRACE_THREADS, PK_DYN_MINBLOCKS) k_trace_dyn(S
 // Closest hit = min (t, slot) over accepted triangles, any hit = the first
 // accepted triangle: the answer does not depend on the visiting order.
 // =====================================================================
-// (1080p, wide traversal: 16 entries 3118-3137 Mrays/s, 8: 3155-3168, 4: 3156-3172)
+// (1080p, wide traversal: 16 entries 3118-3137 Mrays/s, 8: 3155-3168, 4:
+// 3156-3172; with the concurrent-work grids 16: 3377-3394, 8: 3400-3412, 4:
+// 3432-3451)
 #ifndef PK_CW_SMEM
-#define PK_CW_SMEM 8
+#define PK_CW_SMEM 4
 #endif
 constexpr int CW_STACK_SMEM = PK_CW_SMEM;       // group entries per thread in shared memory
 constexpr int CW_STACK_LOCAL = 32 - PK_CW_SMEM;  // overflow entries in local memory
